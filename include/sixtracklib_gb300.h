@@ -1,0 +1,457 @@
+/* sixtracklib_gb300.h -- C ABI of the GB300-native tracking engine.
+ *
+ * A drop-in for the tracking hot path of SixTrackLib: the same `st_`-prefixed
+ * entry points, the same CObjects buffer encoding of lattices and particle
+ * sets, the same NS(Particles) SoA with state / at_turn / at_element_id
+ * bookkeeping and the same int32 status convention (0 success, -1 failure,
+ * OR-accumulated over particles).  Every tracking call runs on the GPU;
+ * there is no CPU fallback: without a usable CUDA device the calls return
+ * failure and report the reason through st_last_error().
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * the SixTrackLib tree).  Only plain C types cross this boundary.
+ */
+#ifndef SIXTRACKLIB_GB300_H
+#define SIXTRACKLIB_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------- types */
+/* sixtracklib/common/definitions.h, track/definitions.h:12-24 */
+typedef int32_t st_track_status_t;
+typedef uint64_t st_buffer_size_t;
+typedef uint64_t st_buffer_addr_t;
+typedef uint64_t st_object_type_id_t;
+typedef int64_t st_particle_index_t;
+typedef int64_t st_particle_num_elements_t;
+typedef double st_particle_real_t;
+
+#define ST_TRACK_SUCCESS 0
+#define ST_TRACK_STATUS_GENERAL_FAILURE (-1)
+
+/* object type ids: sixtracklib/common/internal/objects_type_id.h:16-55 */
+#define ST_OBJECT_TYPE_PARTICLE 1
+#define ST_OBJECT_TYPE_DRIFT 2
+#define ST_OBJECT_TYPE_DRIFT_EXACT 3
+#define ST_OBJECT_TYPE_MULTIPOLE 4
+#define ST_OBJECT_TYPE_CAVITY 5
+#define ST_OBJECT_TYPE_XYSHIFT 6
+#define ST_OBJECT_TYPE_SROTATION 7
+#define ST_OBJECT_TYPE_BEAM_BEAM_4D 8
+#define ST_OBJECT_TYPE_BEAM_BEAM_6D 9
+#define ST_OBJECT_TYPE_BEAM_MONITOR 10
+#define ST_OBJECT_TYPE_LIMIT_RECT 11
+#define ST_OBJECT_TYPE_LIMIT_ELLIPSE 12
+#define ST_OBJECT_TYPE_SC_COASTING 13
+#define ST_OBJECT_TYPE_SC_QGAUSSIAN_PROF 14
+#define ST_OBJECT_TYPE_LIMIT_RECT_ELLIPSE 16
+#define ST_OBJECT_TYPE_DIPEDGE 24
+#define ST_OBJECT_TYPE_RF_MULTIPOLE 256
+#define ST_OBJECT_TYPE_SC_INTERPOLATED_PROF 257
+#define ST_OBJECT_TYPE_LINE_DENSITY_PROF_DATA 258
+#define ST_OBJECT_TYPE_TRICUB_DATA 260
+#define ST_OBJECT_TYPE_TRICUB 261
+#define ST_OBJECT_TYPE_ELEM_BY_ELEM_CONF 65534
+
+/* NS(Object): sixtracklib/common/buffer/buffer_object.h:24-30 */
+typedef struct st_Object {
+    st_buffer_addr_t begin_addr;
+    st_object_type_id_t type_id;
+    st_buffer_size_t size;
+} st_Object;
+
+/* NS(Particles): sixtracklib/common/particles.h:38-67 */
+typedef struct st_Particles {
+    int64_t num_particles;
+    double *q0, *mass0, *beta0, *gamma0, *p0c;
+    double *s, *x, *y, *px, *py, *zeta;
+    double *psigma, *delta, *rpp, *rvv, *chi, *charge_ratio;
+    int64_t *particle_id, *at_element_id, *at_turn, *state;
+} st_Particles;
+
+/* Beam-element structs, byte-identical to the reference's
+ * (sixtracklib/common/be_<kind>/be_<kind>.h). */
+typedef struct st_Drift { double length; } st_Drift;             /* be_drift.h:28-31 */
+typedef struct st_DriftExact { double length; } st_DriftExact;   /* be_drift.h:159-162 */
+typedef struct st_Multipole {                                    /* be_multipole.h:27-34 */
+    int64_t order;
+    double length, hxl, hyl;
+    st_buffer_addr_t bal_addr;
+} st_Multipole;
+typedef struct st_RFMultipole {                                  /* be_rfmultipole.h */
+    int64_t order;
+    double voltage, frequency, lag;
+    st_buffer_addr_t bal_addr, phase_addr;
+} st_RFMultipole;
+typedef struct st_Cavity { double voltage, frequency, lag; } st_Cavity; /* be_cavity.h:27-32 */
+typedef struct st_XYShift { double dx, dy; } st_XYShift;         /* be_xyshift.h:26-30 */
+typedef struct st_SRotation { double cos_z, sin_z; } st_SRotation; /* be_srotation.h:26-30 */
+typedef struct st_LimitRect { double min_x, max_x, min_y, max_y; } st_LimitRect;
+typedef struct st_LimitEllipse { double a_squ, b_squ, a_b_squ; } st_LimitEllipse;
+typedef struct st_LimitRectEllipse {
+    double max_x, max_y, a_squ, b_squ, a_squ_b_squ;
+} st_LimitRectEllipse;
+typedef struct st_DipoleEdge { double r21, r43; } st_DipoleEdge; /* be_dipedge.h */
+typedef struct st_BeamMonitor {                                  /* be_monitor.h:35-45 */
+    int64_t num_stores, start, skip;
+    st_buffer_addr_t out_address;
+    int64_t max_particle_id, min_particle_id;
+    int64_t is_rolling, is_turn_ordered;
+} st_BeamMonitor;
+typedef struct st_BeamBeam4D { uint64_t data_size; st_buffer_addr_t data_addr; } st_BeamBeam4D;
+typedef struct st_BeamBeam6D { uint64_t data_size; st_buffer_addr_t data_addr; } st_BeamBeam6D;
+typedef struct st_SCCoasting {                                   /* be_beamfields.h:418-429 */
+    double number_of_particles, circumference, sigma_x, sigma_y, length;
+    double x_co, y_co, min_sigma_diff;
+    uint64_t enabled;
+} st_SCCoasting;
+typedef struct st_SCQGaussProfile {                              /* be_beamfields.h:638-651 */
+    double number_of_particles, bunchlength_rms, sigma_x, sigma_y, length;
+    double x_co, y_co, min_sigma_diff, q_param, cq;
+    uint64_t enabled;
+} st_SCQGaussProfile;
+
+/* NS(ElemByElemConfig): output/elem_by_elem_config.h:39-54 */
+typedef struct st_ElemByElemConfig {
+    int64_t order;
+    int64_t num_particles_to_store, num_elements_to_store, num_turns_to_store;
+    int64_t min_particle_id, min_element_id, min_turn;
+    int64_t max_particle_id, max_element_id, max_turn;
+    int64_t is_rolling;
+    st_buffer_addr_t out_store_addr;
+} st_ElemByElemConfig;
+
+/* Opaque handles. */
+typedef struct st_Buffer st_Buffer;
+typedef struct st_TrackJob st_TrackJob;
+typedef st_TrackJob st_TrackJobBase;     /* legacy name, track_job.h:139 */
+typedef st_TrackJob st_TrackJobBaseNew;  /* track/track_job_base.h:53 */
+typedef st_TrackJob st_CudaTrackJob;     /* cuda/track_job.h:42 */
+
+/* ------------------------------------------------------ error reporting */
+/* No reference counterpart: the last failure's reason, per thread. */
+const char *st_last_error(void);
+
+/* ------------------------------------------------------ CObjects buffer */
+/* sixtracklib/common/buffer.h (NS(Buffer_new) ... NS(Buffer_delete)) */
+st_Buffer *st_Buffer_new(st_buffer_size_t buffer_capacity);
+st_Buffer *st_Buffer_new_from_file(const char *path);
+/* Copy of an existing CObjects image (remapped to its new address). */
+st_Buffer *st_Buffer_new_from_copy(const st_Buffer *other);
+st_Buffer *st_Buffer_new_on_data(const unsigned char *data, st_buffer_size_t size);
+void st_Buffer_delete(st_Buffer *buffer);
+int32_t st_Buffer_write_to_file(const st_Buffer *buffer, const char *path);
+int32_t st_Buffer_reset(st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_size(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_capacity(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_slot_size(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_num_of_objects(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_num_of_slots(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_num_of_dataptrs(const st_Buffer *buffer);
+unsigned char *st_Buffer_get_data_begin(st_Buffer *buffer);
+const unsigned char *st_Buffer_get_const_data_begin(const st_Buffer *buffer);
+st_buffer_addr_t st_Buffer_get_data_begin_addr(const st_Buffer *buffer);
+st_Object *st_Buffer_get_objects_begin(st_Buffer *buffer);
+st_Object *st_Buffer_get_objects_end(st_Buffer *buffer);
+const st_Object *st_Buffer_get_const_objects_begin(const st_Buffer *buffer);
+const st_Object *st_Buffer_get_const_objects_end(const st_Buffer *buffer);
+const st_Object *st_Buffer_get_const_object(const st_Buffer *buffer, st_buffer_size_t index);
+st_Object *st_Buffer_get_object(st_Buffer *buffer, st_buffer_size_t index);
+/* Generic object append: struct bytes plus float64/int64 arrays the given
+ * pointer fields (by 8-byte word index in the struct) reference. */
+void *st_Buffer_add_object(st_Buffer *buffer, const void *struct_data,
+                           st_buffer_size_t struct_size, st_object_type_id_t type_id,
+                           st_buffer_size_t num_dataptrs, const st_buffer_size_t *field_word_index,
+                           const void *const *array_data, const st_buffer_size_t *array_words);
+st_object_type_id_t st_Object_get_type_id(const st_Object *obj);
+st_buffer_addr_t st_Object_get_begin_addr(const st_Object *obj);
+st_buffer_size_t st_Object_get_size(const st_Object *obj);
+
+/* ------------------------------------------------------- beam elements */
+/* be_drift/be_drift.h, be_multipole/be_multipole.h, ... (NS(X_new),
+ * NS(X_add), NS(X_type_id)) */
+st_Drift *st_Drift_new(st_Buffer *buffer);
+st_Drift *st_Drift_add(st_Buffer *buffer, double length);
+st_DriftExact *st_DriftExact_new(st_Buffer *buffer);
+st_DriftExact *st_DriftExact_add(st_Buffer *buffer, double length);
+st_Multipole *st_Multipole_new(st_Buffer *buffer, int64_t order);
+st_Multipole *st_Multipole_add(st_Buffer *buffer, int64_t order, const double *bal,
+                               double length, double hxl, double hyl);
+double *st_Multipole_bal(st_Multipole *mp);
+st_RFMultipole *st_RFMultipole_new(st_Buffer *buffer, int64_t order);
+st_RFMultipole *st_RFMultipole_add(st_Buffer *buffer, int64_t order, double voltage,
+                                   double frequency, double lag, const double *bal,
+                                   const double *phase);
+st_Cavity *st_Cavity_new(st_Buffer *buffer);
+st_Cavity *st_Cavity_add(st_Buffer *buffer, double voltage, double frequency, double lag);
+st_XYShift *st_XYShift_new(st_Buffer *buffer);
+st_XYShift *st_XYShift_add(st_Buffer *buffer, double dx, double dy);
+st_SRotation *st_SRotation_new(st_Buffer *buffer);
+st_SRotation *st_SRotation_add(st_Buffer *buffer, double angle_rad);
+st_SRotation *st_SRotation_add_detailed(st_Buffer *buffer, double cos_z, double sin_z);
+st_LimitRect *st_LimitRect_new(st_Buffer *buffer);
+st_LimitRect *st_LimitRect_add(st_Buffer *buffer, double min_x, double max_x,
+                               double min_y, double max_y);
+st_LimitEllipse *st_LimitEllipse_new(st_Buffer *buffer);
+st_LimitEllipse *st_LimitEllipse_add(st_Buffer *buffer, double x_half_axis,
+                                     double y_half_axis);
+st_LimitRectEllipse *st_LimitRectEllipse_new(st_Buffer *buffer);
+st_LimitRectEllipse *st_LimitRectEllipse_add(st_Buffer *buffer, double max_x, double max_y,
+                                             double a_squ, double b_squ);
+st_DipoleEdge *st_DipoleEdge_new(st_Buffer *buffer);
+st_DipoleEdge *st_DipoleEdge_add(st_Buffer *buffer, double r21, double r43);
+st_BeamMonitor *st_BeamMonitor_new(st_Buffer *buffer);
+st_BeamMonitor *st_BeamMonitor_add(st_Buffer *buffer, int64_t num_stores, int64_t start,
+                                   int64_t skip, st_buffer_addr_t out_address,
+                                   int64_t min_particle_id, int64_t max_particle_id,
+                                   bool is_rolling, bool is_turn_ordered);
+st_BeamBeam4D *st_BeamBeam4D_new(st_Buffer *buffer, st_buffer_size_t data_size);
+st_BeamBeam4D *st_BeamBeam4D_add(st_Buffer *buffer, st_buffer_size_t data_size,
+                                 const double *data);
+st_BeamBeam6D *st_BeamBeam6D_new(st_Buffer *buffer, st_buffer_size_t data_size);
+st_BeamBeam6D *st_BeamBeam6D_add(st_Buffer *buffer, st_buffer_size_t data_size,
+                                 const double *data);
+st_SCCoasting *st_SCCoasting_new(st_Buffer *buffer);
+st_SCCoasting *st_SCCoasting_add(st_Buffer *buffer, double number_of_particles,
+                                 double circumference, double sigma_x, double sigma_y,
+                                 double length, double x_co, double y_co,
+                                 double min_sigma_diff, bool enabled);
+st_SCQGaussProfile *st_SCQGaussProfile_new(st_Buffer *buffer);
+st_SCQGaussProfile *st_SCQGaussProfile_add(st_Buffer *buffer, double number_of_particles,
+                                           double bunchlength_rms, double sigma_x,
+                                           double sigma_y, double length, double x_co,
+                                           double y_co, double min_sigma_diff,
+                                           double q_param, bool enabled);
+
+/* ------------------------------------------------------------ particles */
+/* particles.h:152-170 (NS(Particles_new)), NS(Particles_buffer_get_particles),
+ * NS(Particles_managed_buffer_get_particles) */
+st_Particles *st_Particles_new(st_Buffer *buffer, st_buffer_size_t num_particles);
+st_Particles *st_Particles_add_copy(st_Buffer *buffer, const st_Particles *orig);
+st_Particles *st_Particles_buffer_get_particles(st_Buffer *buffer, st_buffer_size_t index);
+const st_Particles *st_Particles_buffer_get_const_particles(const st_Buffer *buffer,
+                                                            st_buffer_size_t index);
+int64_t st_Particles_get_num_of_particles(const st_Particles *p);
+st_buffer_size_t st_Particles_buffer_get_num_of_particle_blocks(const st_Buffer *buffer);
+/* Reference momentum helpers (particles.h NS(Particles_update_delta_value),
+ * NS(Particles_set_...)): beta0/gamma0 from p0c, delta-dependent columns. */
+void st_Particles_set_reference(st_Particles *p, double p0c, double mass0, double q0);
+void st_Particles_update_delta_value(st_Particles *p, int64_t index, double delta);
+int32_t st_Particles_copy(st_Particles *dest, const st_Particles *src);
+
+/* ----------------------------------------------------- free tracking calls */
+/* common/track/track.h:86-132; each call uploads the particle set to the
+ * GPU, tracks there and writes the result back into the caller's columns. */
+st_track_status_t st_Track_particle_until_turn(st_Particles *particles, int64_t index,
+                                               const st_Buffer *beam_elements,
+                                               int64_t until_turn);
+st_track_status_t st_Track_all_particles_until_turn(st_Particles *particles,
+                                                    const st_Buffer *beam_elements,
+                                                    int64_t until_turn);
+st_track_status_t st_Track_particle_element_by_element_until_turn(
+    st_Particles *particles, int64_t index, const st_ElemByElemConfig *config,
+    const st_Buffer *beam_elements, int64_t until_turn);
+st_track_status_t st_Track_all_particles_element_by_element_until_turn(
+    st_Particles *particles, const st_ElemByElemConfig *config,
+    const st_Buffer *beam_elements, int64_t until_turn);
+st_track_status_t st_Track_particle_line(st_Particles *particles, int64_t index,
+                                         const st_Buffer *beam_elements,
+                                         st_buffer_size_t line_begin_idx,
+                                         st_buffer_size_t line_end_idx, bool finish_turn);
+st_track_status_t st_Track_all_particles_line(st_Particles *particles,
+                                              const st_Buffer *beam_elements,
+                                              st_buffer_size_t line_begin_idx,
+                                              st_buffer_size_t line_end_idx,
+                                              bool finish_turn);
+
+/* Elem-by-elem configuration (output/elem_by_elem_config.h:667-763). */
+int32_t st_ElemByElemConfig_init_detailed(st_ElemByElemConfig *config, int64_t order,
+                                          int64_t min_particle_id, int64_t max_particle_id,
+                                          int64_t min_element_id, int64_t max_element_id,
+                                          int64_t min_turn, int64_t max_turn,
+                                          bool is_rolling);
+int64_t st_ElemByElemConfig_get_particles_store_index_details(
+    const st_ElemByElemConfig *config, int64_t particle_id, int64_t at_element,
+    int64_t at_turn);
+int64_t st_ElemByElemConfig_get_stored_num_particles(const st_ElemByElemConfig *config);
+
+/* ------------------------------------------------------------- TrackJob */
+/* Legacy TrackJob, common/track_job.h:139-190 and
+ * common/internal/track_job.cpp:47-186.  `arch` is "cuda" (also accepted:
+ * "gb300", "gpu"); the reference's "cpu" / "opencl" backends are not part
+ * of this engine and are rejected with NULL.  `config_str` accepts
+ * whitespace-separated key=value pairs (see st_TrackJob_get_config_str):
+ *   mode=exact|fast  threads_per_block=N  device=N  aperture=always|never|
+ *   conditional  aperture_min_length=L  x_limit=X  y_limit=Y
+ * and the reference's TOML form "[cuda]\n track_threads_per_block = N". */
+st_TrackJob *st_TrackJob_create(const char *arch, const char *config_str);
+st_TrackJob *st_TrackJob_new(const char *arch, st_Buffer *particles_buffer,
+                             st_Buffer *beam_elements_buffer, const char *config_str);
+st_TrackJob *st_TrackJob_new_with_output(const char *arch, st_Buffer *particles_buffer,
+                                         st_Buffer *beam_elements_buffer,
+                                         st_Buffer *output_buffer,
+                                         st_buffer_size_t until_turn_elem_by_elem,
+                                         const char *config_str);
+st_TrackJob *st_TrackJob_new_detailed(const char *arch, st_Buffer *particles_buffer,
+                                      st_buffer_size_t num_particle_sets,
+                                      const st_buffer_size_t *particle_set_indices,
+                                      st_Buffer *beam_elements_buffer,
+                                      st_Buffer *output_buffer,
+                                      st_buffer_size_t until_turn_elem_by_elem,
+                                      const char *config_str);
+bool st_TrackJob_reset(st_TrackJob *job, st_Buffer *particles_buffer,
+                       st_Buffer *beam_elements_buffer, st_Buffer *output_buffer);
+bool st_TrackJob_reset_with_output(st_TrackJob *job, st_Buffer *particles_buffer,
+                                   st_Buffer *beam_elements_buffer, st_Buffer *output_buffer,
+                                   st_buffer_size_t until_turn_elem_by_elem);
+bool st_TrackJob_reset_detailed(st_TrackJob *job, st_Buffer *particles_buffer,
+                                st_buffer_size_t num_particle_sets,
+                                const st_buffer_size_t *particle_set_indices,
+                                st_Buffer *beam_elements_buffer, st_Buffer *output_buffer,
+                                st_buffer_size_t until_turn_elem_by_elem);
+void st_TrackJob_delete(st_TrackJob *job);
+void st_TrackJob_clear(st_TrackJob *job);
+st_track_status_t st_TrackJob_track_until(st_TrackJob *job, st_buffer_size_t until_turn);
+st_track_status_t st_TrackJob_track_elem_by_elem(st_TrackJob *job,
+                                                 st_buffer_size_t until_turn);
+st_track_status_t st_TrackJob_track_line(st_TrackJob *job, st_buffer_size_t begin_idx,
+                                         st_buffer_size_t end_idx, bool finish_turn);
+void st_TrackJob_collect(st_TrackJob *job);
+void st_TrackJob_collect_detailed(st_TrackJob *job, uint16_t flags);
+void st_TrackJob_collect_particles(st_TrackJob *job);
+void st_TrackJob_collect_beam_elements(st_TrackJob *job);
+void st_TrackJob_collect_output(st_TrackJob *job);
+void st_TrackJob_push(st_TrackJob *job, uint16_t flags);
+void st_TrackJob_push_particles(st_TrackJob *job);
+void st_TrackJob_push_beam_elements(st_TrackJob *job);
+void st_TrackJob_push_output(st_TrackJob *job);
+void st_TrackJob_enable_collect_particles(st_TrackJob *job);
+void st_TrackJob_disable_collect_particles(st_TrackJob *job);
+bool st_TrackJob_is_collecting_particles(const st_TrackJob *job);
+void st_TrackJob_enable_collect_beam_elements(st_TrackJob *job);
+void st_TrackJob_disable_collect_beam_elements(st_TrackJob *job);
+bool st_TrackJob_is_collecting_beam_elements(const st_TrackJob *job);
+void st_TrackJob_enable_collect_output(st_TrackJob *job);
+void st_TrackJob_disable_collect_output(st_TrackJob *job);
+bool st_TrackJob_is_collecting_output(const st_TrackJob *job);
+uint16_t st_TrackJob_get_collect_flags(const st_TrackJob *job);
+void st_TrackJob_set_collect_flags(st_TrackJob *job, uint16_t flags);
+bool st_TrackJob_requires_collecting(const st_TrackJob *job);
+int64_t st_TrackJob_get_type_id(const st_TrackJob *job);
+const char *st_TrackJob_get_type_str(const st_TrackJob *job);
+bool st_TrackJob_has_device_id_str(const st_TrackJob *job);
+const char *st_TrackJob_get_device_id_str(const st_TrackJob *job);
+bool st_TrackJob_has_config_str(const st_TrackJob *job);
+const char *st_TrackJob_get_config_str(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_num_particle_sets(const st_TrackJob *job);
+const st_buffer_size_t *st_TrackJob_get_particle_set_indices_begin(const st_TrackJob *job);
+const st_buffer_size_t *st_TrackJob_get_particle_set_indices_end(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_particle_set_index(const st_TrackJob *job, st_buffer_size_t n);
+st_buffer_size_t st_TrackJob_get_total_num_particles_in_sets(const st_TrackJob *job);
+int64_t st_TrackJob_get_min_particle_id(const st_TrackJob *job);
+int64_t st_TrackJob_get_max_particle_id(const st_TrackJob *job);
+int64_t st_TrackJob_get_min_element_id(const st_TrackJob *job);
+int64_t st_TrackJob_get_max_element_id(const st_TrackJob *job);
+int64_t st_TrackJob_get_min_initial_turn_id(const st_TrackJob *job);
+int64_t st_TrackJob_get_max_initial_turn_id(const st_TrackJob *job);
+st_Buffer *st_TrackJob_get_particles_buffer(st_TrackJob *job);
+const st_Buffer *st_TrackJob_get_const_particles_buffer(const st_TrackJob *job);
+st_Buffer *st_TrackJob_get_beam_elements_buffer(st_TrackJob *job);
+const st_Buffer *st_TrackJob_get_const_beam_elements_buffer(const st_TrackJob *job);
+bool st_TrackJob_has_output_buffer(const st_TrackJob *job);
+bool st_TrackJob_owns_output_buffer(const st_TrackJob *job);
+st_Buffer *st_TrackJob_get_output_buffer(st_TrackJob *job);
+const st_Buffer *st_TrackJob_get_const_output_buffer(const st_TrackJob *job);
+bool st_TrackJob_has_elem_by_elem_output(const st_TrackJob *job);
+bool st_TrackJob_has_beam_monitor_output(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_elem_by_elem_output_buffer_offset(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_beam_monitor_output_buffer_offset(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_num_elem_by_elem_turns(const st_TrackJob *job);
+bool st_TrackJob_has_elem_by_elem_config(const st_TrackJob *job);
+const st_ElemByElemConfig *st_TrackJob_get_elem_by_elem_config(const st_TrackJob *job);
+bool st_TrackJob_is_elem_by_elem_config_rolling(const st_TrackJob *job);
+bool st_TrackJob_get_default_elem_by_elem_config_rolling_flag(const st_TrackJob *job);
+void st_TrackJob_set_default_elem_by_elem_config_rolling_flag(st_TrackJob *job, bool rolling);
+int64_t st_TrackJob_get_elem_by_elem_config_order(const st_TrackJob *job);
+bool st_TrackJob_has_beam_monitors(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_num_beam_monitors(const st_TrackJob *job);
+const st_buffer_size_t *st_TrackJob_get_beam_monitor_indices_begin(const st_TrackJob *job);
+const st_buffer_size_t *st_TrackJob_get_beam_monitor_indices_end(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_get_beam_monitor_index(const st_TrackJob *job, st_buffer_size_t n);
+
+/* TrackJobNew / CudaTrackJob names (track/track_job_base.h:53-65,
+ * cuda/track_job.h:42-66): the same job object. */
+st_CudaTrackJob *st_CudaTrackJob_create(void);
+st_CudaTrackJob *st_CudaTrackJob_new_from_config_str(const char *config_str);
+st_CudaTrackJob *st_CudaTrackJob_new(const char *node_id_str, st_Buffer *particles_buffer,
+                                     st_Buffer *beam_elements_buffer);
+st_CudaTrackJob *st_CudaTrackJob_new_with_output(const char *node_id_str,
+                                                 st_Buffer *particles_buffer,
+                                                 st_Buffer *beam_elements_buffer,
+                                                 st_Buffer *output_buffer,
+                                                 st_buffer_size_t until_turn_elem_by_elem);
+st_CudaTrackJob *st_CudaTrackJob_new_detailed(const char *node_id_str,
+                                              st_Buffer *particles_buffer,
+                                              st_buffer_size_t num_particle_sets,
+                                              const st_buffer_size_t *particle_set_indices,
+                                              st_Buffer *beam_elements_buffer,
+                                              st_Buffer *output_buffer,
+                                              st_buffer_size_t until_turn_elem_by_elem,
+                                              const char *config_str);
+void st_TrackJobNew_delete(st_TrackJobBaseNew *job);
+st_track_status_t st_TrackJobNew_track_until(st_TrackJobBaseNew *job, st_buffer_size_t until_turn);
+st_track_status_t st_TrackJobNew_track_elem_by_elem(st_TrackJobBaseNew *job,
+                                                    st_buffer_size_t until_turn);
+st_track_status_t st_TrackJobNew_track_line(st_TrackJobBaseNew *job, st_buffer_size_t begin_idx,
+                                            st_buffer_size_t end_idx, bool finish_turn);
+int32_t st_TrackJobNew_collect_particles(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_collect_beam_elements(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_collect_output(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
+uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *job);
+uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *job);
+
+/* --------------------------------------------- device-resident interface */
+/* No reference counterpart: the engine's own entry points for callers that
+ * keep particle columns resident on the GPU (the Python/PyTorch layer, the
+ * benchmark).  `d_cols` is a device pointer to a 21 x n column block (see
+ * sixtracklib_gb300/particles.py), `stream` a cudaStream_t (0 = default).
+ * A compiled lattice is an engine-side device copy of a CObjects lattice. */
+typedef struct st_DeviceLattice st_DeviceLattice;
+st_DeviceLattice *st_DeviceLattice_new(const unsigned char *lattice_image,
+                                       st_buffer_size_t image_size, const char *config_str);
+void st_DeviceLattice_delete(st_DeviceLattice *lat);
+int64_t st_DeviceLattice_num_elements(const st_DeviceLattice *lat);
+int64_t st_DeviceLattice_num_chunks(const st_DeviceLattice *lat);
+st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *lat, void *d_cols,
+                                               int64_t num_particles, int64_t until_turn,
+                                               void *stream);
+st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *lat, void *d_cols,
+                                              int64_t num_particles, uint64_t begin_idx,
+                                              uint64_t end_idx, bool finish_turn,
+                                              void *stream);
+/* Launch without waiting for the status word (asynchronous on `stream`);
+ * st_DeviceLattice_last_status() synchronises and returns it. */
+int32_t st_DeviceLattice_launch_until(st_DeviceLattice *lat, void *d_cols,
+                                      int64_t num_particles, int64_t until_turn, void *stream);
+st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *lat);
+/* Kernel-launch counter (for launch accounting in benchmarks). */
+uint64_t st_engine_kernel_launches(void);
+/* Compile-time properties of the engine build. */
+const char *st_engine_build_info(void);
+/* Measured dense FP64 FMA throughput of `device` in TFLOP/s (FMA = 2 flops);
+ * the denominator of the tracking kernel's roofline. */
+double st_engine_measure_fp64_peak(int device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SIXTRACKLIB_GB300_H */

@@ -1,0 +1,511 @@
+"""Beam-element classes that encode into / decode from CObjects buffers.
+
+Class names, constructor arguments and stored layouts follow the reference's
+Python layer (python/sixtracklib/beam_elements.py:42-700) and C structs
+(sixtracklib/common/be_*/be_*.h); the type ids are those of
+sixtracklib/common/internal/objects_type_id.h:16-55.  Unlike the reference,
+these classes need no ``cobjects`` package: they write the buffer through
+:mod:`sixtracklib_gb300.cbuffer`.
+"""
+
+from __future__ import annotations
+
+from math import factorial
+
+import numpy as np
+
+from .cbuffer import CBuffer, CObject
+
+QELEM = 1.60217662e-19  # sixtracklib/common/constants.h:35
+
+TYPE_DRIFT = 2
+TYPE_DRIFT_EXACT = 3
+TYPE_MULTIPOLE = 4
+TYPE_CAVITY = 5
+TYPE_XYSHIFT = 6
+TYPE_SROTATION = 7
+TYPE_BEAM_BEAM_4D = 8
+TYPE_BEAM_BEAM_6D = 9
+TYPE_BEAM_MONITOR = 10
+TYPE_LIMIT_RECT = 11
+TYPE_LIMIT_ELLIPSE = 12
+TYPE_SC_COASTING = 13
+TYPE_SC_QGAUSSIAN_PROF = 14
+TYPE_LIMIT_RECT_ELLIPSE = 16
+TYPE_DIPEDGE = 24
+TYPE_RF_MULTIPOLE = 256
+TYPE_SC_INTERPOLATED_PROF = 257
+TYPE_LINE_DENSITY_PROF_DATA = 258
+TYPE_TRICUB_DATA = 260
+TYPE_TRICUB = 261
+TYPE_PARTICLE = 1
+
+
+class _Element:
+    """Base: ``_fields`` lists ``(name, kind)`` with kind 'f' (float64),
+    'i' (int64), 'u' (uint64) or ('p', length_expr) for a pointer to a
+    float64 array whose length is computed from the other fields."""
+
+    _typeid = 0
+    _fields: tuple = ()
+
+    def __init__(self, cbuffer=None, **kwargs):
+        for name, kind in self._fields:
+            default = 0.0 if kind == "f" else 0
+            if isinstance(kind, tuple):
+                default = None
+            setattr(self, name, kwargs.pop(name, getattr(self, "_default_" + name, default)))
+        self._index = None
+        self._cbuffer = None
+        if cbuffer is not None:
+            self._index = cbuffer.add_object(*self._encode())
+            self._cbuffer = cbuffer
+            cbuffer.typeids.setdefault(self._typeid, type(self))
+
+    def _encode(self):
+        words = np.zeros(len(self._fields), dtype=np.uint64)
+        arrays = []
+        for i, (name, kind) in enumerate(self._fields):
+            v = getattr(self, name)
+            if kind == "f":
+                words[i] = np.float64(v).view(np.uint64)
+            elif kind == "i":
+                words[i] = np.int64(v).view(np.uint64)
+            elif kind == "u":
+                words[i] = np.uint64(int(v))
+            else:
+                arr = np.asarray(v if v is not None else [], dtype=np.float64)
+                arrays.append((i, arr))
+        return self._typeid, words, arrays
+
+    @classmethod
+    def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
+        self = cls.__new__(cls)
+        w = obj.words
+        for i, (name, kind) in enumerate(cls._fields):
+            if kind == "f":
+                setattr(self, name, float(w[i : i + 1].view(np.float64)[0]))
+            elif kind == "i":
+                setattr(self, name, int(w[i : i + 1].view(np.int64)[0]))
+            elif kind == "u":
+                setattr(self, name, int(w[i]))
+            else:
+                off = int(w[i])
+                n = cls._array_len(self, kind[1])
+                setattr(self, name, w[off : off + n].view(np.float64).copy())
+        self._index = index
+        self._cbuffer = cbuffer
+        return self
+
+    @staticmethod
+    def _array_len(self, expr):
+        return int(eval(expr, {}, dict(self.__dict__)))
+
+    def to_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields}
+
+    def __repr__(self):
+        args = ", ".join(f"{k}={v!r}" for k, v in self.to_dict().items())
+        return f"{type(self).__name__}({args})"
+
+
+class Drift(_Element):
+    _typeid = TYPE_DRIFT
+    _fields = (("length", "f"),)
+
+
+class DriftExact(_Element):
+    _typeid = TYPE_DRIFT_EXACT
+    _fields = (("length", "f"),)
+
+
+def _knl_ksl_to_bal(order, knl, ksl):
+    knl = [] if knl is None else list(knl)
+    ksl = [] if ksl is None else list(ksl)
+    order = 0 if order is None else int(order)
+    n = max(order + 1, len(knl), len(ksl))
+    kn = np.zeros(n)
+    ks = np.zeros(n)
+    kn[: len(knl)] = knl
+    ks[: len(ksl)] = ksl
+    inv_fact = np.array([1.0 / factorial(i) for i in range(n)])
+    bal = np.zeros(2 * n)
+    bal[0::2] = kn * inv_fact
+    bal[1::2] = ks * inv_fact
+    return n - 1, bal
+
+
+class Multipole(_Element):
+    """Thin multipole; ``bal[2k] = knl[k]/k!``, ``bal[2k+1] = ksl[k]/k!``
+    (be_multipole.h:449-466)."""
+
+    _typeid = TYPE_MULTIPOLE
+    _fields = (
+        ("order", "i"),
+        ("length", "f"),
+        ("hxl", "f"),
+        ("hyl", "f"),
+        ("bal", ("p", "2*order+2")),
+    )
+
+    def __init__(self, order=None, knl=None, ksl=None, bal=None, cbuffer=None, **kw):
+        if bal is None:
+            order, bal = _knl_ksl_to_bal(order, knl, ksl)
+        else:
+            bal = np.asarray(bal, dtype=np.float64)
+            order = (len(bal) - 2) // 2
+        super().__init__(cbuffer=cbuffer, order=order, bal=bal, **kw)
+
+    @property
+    def knl(self):
+        return np.array([self.bal[2 * k] * factorial(k) for k in range(self.order + 1)])
+
+    @property
+    def ksl(self):
+        return np.array([self.bal[2 * k + 1] * factorial(k) for k in range(self.order + 1)])
+
+
+class RFMultipole(_Element):
+    _typeid = TYPE_RF_MULTIPOLE
+    _fields = (
+        ("order", "i"),
+        ("voltage", "f"),
+        ("frequency", "f"),
+        ("lag", "f"),
+        ("bal", ("p", "2*order+2")),
+        ("phase", ("p", "2*order+2")),
+    )
+
+    def __init__(self, order=None, knl=None, ksl=None, pn=None, ps=None, bal=None,
+                 p=None, cbuffer=None, **kw):
+        if bal is None:
+            lens = [len(a) for a in (knl or [], ksl or [], pn or [], ps or [])]
+            n = max([(order or 0) + 1] + lens)
+            order, bal = _knl_ksl_to_bal(n - 1, knl, ksl)
+            ph = np.zeros(2 * n)
+            ph[0::2][: len(pn or [])] = pn or []
+            ph[1::2][: len(ps or [])] = ps or []
+        else:
+            bal = np.asarray(bal, dtype=np.float64)
+            ph = np.asarray(p if p is not None else kw.pop("phase"), dtype=np.float64)
+            order = (len(bal) - 2) // 2
+        kw.pop("phase", None)
+        super().__init__(cbuffer=cbuffer, order=order, bal=bal, phase=ph, **kw)
+
+
+class Cavity(_Element):
+    _typeid = TYPE_CAVITY
+    _fields = (("voltage", "f"), ("frequency", "f"), ("lag", "f"))
+
+
+class XYShift(_Element):
+    _typeid = TYPE_XYSHIFT
+    _fields = (("dx", "f"), ("dy", "f"))
+
+
+class SRotation(_Element):
+    """Rotation about s; ``angle`` in degrees (beam_elements.py:282-300)."""
+
+    _typeid = TYPE_SROTATION
+    _fields = (("cos_z", "f"), ("sin_z", "f"))
+    _default_cos_z = 1.0
+
+    def __init__(self, angle=None, cbuffer=None, **kw):
+        if angle is not None:
+            a = angle / 180 * np.pi
+            kw["cos_z"] = float(np.cos(a))
+            kw["sin_z"] = float(np.sin(a))
+        super().__init__(cbuffer=cbuffer, **kw)
+
+    @property
+    def angle_deg(self):
+        return float(np.arctan2(self.sin_z, self.cos_z) * 180.0 / np.pi)
+
+
+class BeamMonitor(_Element):
+    _typeid = TYPE_BEAM_MONITOR
+    _fields = (
+        ("num_stores", "i"),
+        ("start", "i"),
+        ("skip", "i"),
+        ("out_address", "u"),
+        ("max_particle_id", "i"),
+        ("min_particle_id", "i"),
+        ("is_rolling", "i"),
+        ("is_turn_ordered", "i"),
+    )
+    _default_skip = 1
+    _default_is_turn_ordered = 1
+
+
+class LimitRect(_Element):
+    _typeid = TYPE_LIMIT_RECT
+    _fields = (("min_x", "f"), ("max_x", "f"), ("min_y", "f"), ("max_y", "f"))
+
+    def __init__(self, min_x=None, max_x=None, min_y=None, max_y=None,
+                 min_coord=-1.0, max_coord=1.0, cbuffer=None, **kw):
+        min_x = min_coord if min_x is None else min_x
+        min_y = min_coord if min_y is None else min_y
+        max_x = max_coord if max_x is None else max_x
+        max_y = max_coord if max_y is None else max_y
+        if min_x > max_x:
+            min_x, max_x = max_x, min_x
+        if min_y > max_y:
+            min_y, max_y = max_y, min_y
+        if (max_x - min_x) * (max_y - min_y) <= 0.0:
+            raise ValueError("min_x, max_x, min_y, max_y have to delimit a non-vanishing rectangle")
+        super().__init__(cbuffer=cbuffer, min_x=min_x, max_x=max_x, min_y=min_y, max_y=max_y, **kw)
+
+
+class LimitEllipse(_Element):
+    _typeid = TYPE_LIMIT_ELLIPSE
+    _fields = (("a_squ", "f"), ("b_squ", "f"), ("a_b_squ", "f"))
+
+    def __init__(self, a_squ=None, b_squ=None, a=None, b=None, cbuffer=None, **kw):
+        if a_squ is None:
+            a_squ = a * a if (a is not None and a > 0.0) else 1.0
+        if b_squ is None:
+            b_squ = b * b if (b is not None and b > 0.0) else 1.0
+        if not (a_squ > 0.0 and b_squ > 0.0):
+            raise ValueError("a_squ and b_squ have to be positive definite")
+        kw.pop("a_b_squ", None)
+        super().__init__(cbuffer=cbuffer, a_squ=a_squ, b_squ=b_squ, a_b_squ=a_squ * b_squ, **kw)
+
+
+class LimitRectEllipse(_Element):
+    _typeid = TYPE_LIMIT_RECT_ELLIPSE
+    _fields = (("max_x", "f"), ("max_y", "f"), ("a_squ", "f"), ("b_squ", "f"), ("a_b_squ", "f"))
+
+    def __init__(self, max_x=1.0, max_y=1.0, a_squ=None, b_squ=None, a=None, b=None,
+                 cbuffer=None, **kw):
+        if a_squ is None:
+            a_squ = a * a if (a is not None and a > 0.0) else 1.0
+        if b_squ is None:
+            b_squ = b * b if (b is not None and b > 0.0) else 1.0
+        if max_x < 0.0 or max_y < 0.0 or a_squ < 0.0 or b_squ < 0.0:
+            raise ValueError("LimitRectEllipse parameters have to be positive definite")
+        kw.pop("a_b_squ", None)
+        super().__init__(cbuffer=cbuffer, max_x=max_x, max_y=max_y, a_squ=a_squ,
+                         b_squ=b_squ, a_b_squ=a_squ * b_squ, **kw)
+
+
+class DipoleEdge(_Element):
+    _typeid = TYPE_DIPEDGE
+    _fields = (("r21", "f"), ("r43", "f"))
+
+    def __init__(self, r21=None, r43=None, h=0.0, e1=0.0, hgap=0.0, fint=0.0,
+                 cbuffer=None, **kw):
+        if r21 is None and r43 is None:
+            corr = 2.0 * h * hgap * fint
+            r21 = h * np.tan(e1)
+            temp = corr / np.cos(e1) * (1.0 + np.sin(e1) * np.sin(e1))
+            r43 = -h * np.tan(e1 - temp)
+        super().__init__(cbuffer=cbuffer, r21=float(r21), r43=float(r43), **kw)
+
+
+class _DataElement(_Element):
+    """{size, data_addr} elements whose payload is a float64 array."""
+
+    _fields = (("size", "u"), ("data", ("p", "size")))
+
+    def __init__(self, data=None, cbuffer=None, **kw):
+        data = np.asarray(data if data is not None else [], dtype=np.float64)
+        kw.pop("size", None)
+        super().__init__(cbuffer=cbuffer, size=data.size, data=data, **kw)
+
+
+class BeamBeam4D(_DataElement):
+    """4D weak-strong beam-beam; payload = [q_part, N_part, sigma_x, sigma_y,
+    beta_s, min_sigma_diff, Delta_x, Delta_y, Dpx_sub, Dpy_sub, enabled]
+    (be_beamfields.h:36-56, beam_elements.py:470-494)."""
+
+    _typeid = TYPE_BEAM_BEAM_4D
+
+    def __init__(self, data=None, cbuffer=None, **kw):
+        if data is None and "x_bb" in kw:
+            keys = ("charge", "sigma_x", "sigma_y", "beta_r", "min_sigma_diff",
+                    "x_bb", "y_bb", "d_px", "d_py", "enabled")
+            data = [QELEM] + [float(kw.pop(k)) for k in keys]
+        super().__init__(data=data, cbuffer=cbuffer, **kw)
+
+
+class BeamBeam6D(_DataElement):
+    """6D synchro-beam; payload = the BB6D data block
+    (be_beamfields.h:222-250), see :func:`bb6d_data`."""
+
+    _typeid = TYPE_BEAM_BEAM_6D
+
+
+class SCCoasting(_Element):
+    _typeid = TYPE_SC_COASTING
+    _fields = (
+        ("number_of_particles", "f"),
+        ("circumference", "f"),
+        ("sigma_x", "f"),
+        ("sigma_y", "f"),
+        ("length", "f"),
+        ("x_co", "f"),
+        ("y_co", "f"),
+        ("min_sigma_diff", "f"),
+        ("enabled", "u"),
+    )
+    _default_circumference = 1.0
+    _default_sigma_x = 1.0
+    _default_sigma_y = 1.0
+    _default_min_sigma_diff = 1e-10
+    _default_enabled = 1
+
+
+class SCQGaussProfile(_Element):
+    _typeid = TYPE_SC_QGAUSSIAN_PROF
+    _fields = (
+        ("number_of_particles", "f"),
+        ("bunchlength_rms", "f"),
+        ("sigma_x", "f"),
+        ("sigma_y", "f"),
+        ("length", "f"),
+        ("x_co", "f"),
+        ("y_co", "f"),
+        ("min_sigma_diff", "f"),
+        ("q_param", "f"),
+        ("cq", "f"),
+        ("enabled", "u"),
+    )
+    _default_bunchlength_rms = 1.0
+    _default_sigma_x = 1.0
+    _default_sigma_y = 1.0
+    _default_min_sigma_diff = 1e-10
+    _default_q_param = 1.0
+    _default_cq = float(np.sqrt(np.pi))
+    _default_enabled = 1
+
+    def __init__(self, cbuffer=None, **kw):
+        if "cq" not in kw:
+            kw["cq"] = q_gauss_cq(kw.get("q_param", 1.0))
+        super().__init__(cbuffer=cbuffer, **kw)
+
+
+def q_gauss_cq(q):
+    """Normalisation of the q-Gaussian (internal/math_qgauss.h:140-165)."""
+    from math import gamma, sqrt, pi
+
+    eps = 1e-6
+    cq = sqrt(pi)
+    if q >= 1.0 + eps:
+        cq *= gamma((3.0 - q) / (2.0 * (q - 1.0)))
+        cq /= sqrt(q - 1.0) * gamma(1.0 / (q - 1.0))
+    elif q <= 1.0 - eps:
+        cq *= 2.0 * gamma(1.0 / (1.0 - q))
+        cq /= (3.0 - q) * sqrt(1.0 - q) * gamma((3.0 - q) / (2.0 * (1.0 - q)))
+    return cq
+
+
+# Aliases used by the reference's naming of the space-charge kicks.
+SpaceChargeCoasting = SCCoasting
+SpaceChargeQGaussianProfile = SCQGaussProfile
+SpaceChargeBunched = SCQGaussProfile
+
+ELEMENT_TYPES = {
+    TYPE_DRIFT: Drift,
+    TYPE_DRIFT_EXACT: DriftExact,
+    TYPE_MULTIPOLE: Multipole,
+    TYPE_RF_MULTIPOLE: RFMultipole,
+    TYPE_CAVITY: Cavity,
+    TYPE_XYSHIFT: XYShift,
+    TYPE_SROTATION: SRotation,
+    TYPE_BEAM_MONITOR: BeamMonitor,
+    TYPE_LIMIT_RECT: LimitRect,
+    TYPE_LIMIT_ELLIPSE: LimitEllipse,
+    TYPE_LIMIT_RECT_ELLIPSE: LimitRectEllipse,
+    TYPE_DIPEDGE: DipoleEdge,
+    TYPE_BEAM_BEAM_4D: BeamBeam4D,
+    TYPE_BEAM_BEAM_6D: BeamBeam6D,
+    TYPE_SC_COASTING: SCCoasting,
+    TYPE_SC_QGAUSSIAN_PROF: SCQGaussProfile,
+}
+
+
+class Elements:
+    """Lattice container (python/sixtracklib/beam_elements.py:705-800):
+    ``Elements().Drift(length=1.0)`` appends a drift to ``self.cbuffer``."""
+
+    element_types = {cls.__name__: cls for cls in ELEMENT_TYPES.values()}
+
+    def __init__(self, cbuffer=None):
+        self.cbuffer = CBuffer() if cbuffer is None else cbuffer
+        for tid, cls in ELEMENT_TYPES.items():
+            self.cbuffer.typeids[tid] = cls
+        for name, cls in self.element_types.items():
+            setattr(self, name, self._mk(cls))
+
+    def _mk(self, cls):
+        def fun(*args, **kw):
+            return cls(*args, cbuffer=self.cbuffer, **kw)
+
+        return fun
+
+    @classmethod
+    def fromfile(cls, filename):
+        return cls(cbuffer=CBuffer.fromfile(filename))
+
+    def to_file(self, filename):
+        self.cbuffer.tofile(filename)
+        return self
+
+    def get_elements(self):
+        return [self.cbuffer.get_object(i) for i in range(self.cbuffer.n_objects)]
+
+    def get(self, i):
+        return self.cbuffer.get_object(i)
+
+    def __len__(self):
+        return self.cbuffer.n_objects
+
+
+def bb6d_data(q_part, phi, alpha, delta_x, delta_y, n_part_per_slice, z_slices,
+              sigmas, co=(0, 0, 0, 0, 0, 0), min_sigma_diff=1e-10,
+              threshold_singular=1e-28, d_sub=(0, 0, 0, 0, 0, 0), enabled=1.0):
+    """Build a BeamBeam6D payload (layout be_beamfields.h:222-250).
+
+    The reference delegates this initialisation to pysixtrack
+    (``BB6Ddata.BB6D_init``, called at python/sixtracklib/beam_elements.py:
+    496-543), which is not part of the reference tree.  This is an own
+    implementation from the physics of the Hirata boost:
+
+    * boost parameters: ``sin/cos/tan`` of the half crossing angle ``phi`` and
+      ``sin/cos`` of the crossing-plane angle ``alpha``;
+    * the boosted sigma matrix: the boost scales transverse momenta by
+      ``1/cos(phi)``, so entries with one momentum index scale by
+      ``1/cos(phi)`` and entries with two by ``1/cos(phi)**2``;
+    * the strong-beam slice centroids (x=px=y=py=delta=0, sigma=z) are
+      transformed with the same linear boost the tracking map applies to the
+      weak beam: ``x* = cos(alpha) tan(phi) z``, ``y* = sin(alpha) tan(phi) z``,
+      ``sigma* = z / cos(phi)``.
+
+    ``sigmas`` = (S11, S12, S13, S14, S22, S23, S24, S33, S34, S44) in the lab
+    frame; ``co`` = closed orbit (x, px, y, py, zeta, delta); ``d_sub`` =
+    (Dx, Dpx, Dy, Dpy, Dzeta, Ddelta) dipolar subtraction.
+    """
+    sphi, cphi, tphi = np.sin(phi), np.cos(phi), np.tan(phi)
+    salpha, calpha = np.sin(alpha), np.cos(alpha)
+    z = np.asarray(z_slices, dtype=np.float64)
+    n = z.size
+    s11, s12, s13, s14, s22, s23, s24, s33, s34, s44 = [float(v) for v in sigmas]
+    c2 = cphi * cphi
+    sig_star = (s11, s12 / cphi, s13, s14 / cphi, s22 / c2, s23 / cphi,
+                s24 / c2, s33, s34 / cphi, s44 / c2)
+    head = [q_part, sphi, cphi, tphi, salpha, calpha, *sig_star,
+            min_sigma_diff, threshold_singular, 0.0, delta_x, delta_y, *co,
+            *d_sub, enabled]
+    assert len(head) == 34
+    words = np.zeros(38 + 4 * n, dtype=np.float64)
+    words[:34] = head
+    w = words.view(np.uint64)
+    w[18] = np.uint64(n)
+    for k, f in enumerate(range(34, 38)):
+        w[f] = np.uint64(38 + k * n - f - 1)
+    words[38 : 38 + n] = np.asarray(n_part_per_slice, dtype=np.float64)
+    words[38 + n : 38 + 2 * n] = calpha * tphi * z
+    words[38 + 2 * n : 38 + 3 * n] = salpha * tphi * z
+    words[38 + 3 * n : 38 + 4 * n] = z / cphi
+    return words

@@ -1,0 +1,1233 @@
+// engine.cu -- host engine: devices, device lattices, particle transfers,
+// the free tracking calls and the TrackJob (common/track/track.c:21-141,
+// common/internal/track_job.cpp:47-186,417-445, cuda/track/track_job.cpp).
+//
+// Data on the GPU:
+//   * particle sets: one 21 x n column block (NS(Particles) field order),
+//     all sets of a job concatenated, resident between calls;
+//   * lattice: the compiled element stream (lattice.cpp), chunked for the
+//     kernel's shared-memory stages;
+//   * outputs: one column block per output Particles object (elem-by-elem
+//     store, one per BeamMonitor), written by the kernel in place.
+// Every call runs on the GPU; without a usable device the calls fail and
+// st_last_error() names the reason.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernel_api.h"
+#include "lattice.h"
+
+extern "C" uint64_t stg_buffer_generation(const st_Buffer *b);
+
+namespace stg {
+
+// ------------------------------------------------------------- options
+struct Options {
+    bool fast = false;
+    int threads = 256;
+    int device = 0;
+    int aperture_mode = 2;
+    double aperture_min_length = 0.0;
+    double x_limit = 1.0, y_limit = 1.0;
+    int stages = kDefaultStages;
+    int chunk_words = 1024;
+};
+
+static std::string trim(const std::string &s)
+{
+    size_t a = s.find_first_not_of(" \t\r\n\"'");
+    size_t b = s.find_last_not_of(" \t\r\n\"'");
+    return (a == std::string::npos) ? std::string() : s.substr(a, b - a + 1);
+}
+
+// Accepts "key=value" pairs separated by whitespace, ';' or newlines, and
+// the reference's TOML form ("[cuda]" sections, "key = value" lines,
+// cuda/track/track_job.cpp:1775-1830).
+static bool parse_options(const char *cfg, Options *o, std::string *err)
+{
+    if (!cfg) return true;
+    std::string s(cfg);
+    for (char &c : s)
+        if (c == ';' || c == ',') c = '\n';
+    std::istringstream in(s);
+    std::string line;
+    while (std::getline(in, line)) {
+        line = trim(line);
+        if (line.empty() || line[0] == '[' || line[0] == '#') continue;
+        // allow several key=value pairs on one line
+        std::vector<std::string> items;
+        std::string cur;
+        std::istringstream ws(line);
+        std::string tok;
+        while (ws >> tok) {
+            if (tok == "=" || (!cur.empty() && cur.back() == '=')) {
+                cur += tok;
+            } else if (!cur.empty() && tok[0] == '=') {
+                cur += tok;
+            } else {
+                if (!cur.empty()) items.push_back(cur);
+                cur = tok;
+            }
+        }
+        if (!cur.empty()) items.push_back(cur);
+        for (const std::string &it : items) {
+            size_t const eq = it.find('=');
+            if (eq == std::string::npos) {
+                if (err) *err = "config: expected key=value, got '" + it + "'";
+                return false;
+            }
+            std::string const k = trim(it.substr(0, eq));
+            std::string const v = trim(it.substr(eq + 1));
+            try {
+                if (k == "mode") {
+                    if (v == "fast") o->fast = true;
+                    else if (v == "exact") o->fast = false;
+                    else throw std::invalid_argument(v);
+                } else if (k == "threads_per_block" || k == "track_threads_per_block" ||
+                           k == "threads") {
+                    o->threads = std::stoi(v);
+                } else if (k == "device" || k == "device_id") {
+                    o->device = std::stoi(v);
+                } else if (k == "aperture") {
+                    if (v == "always") o->aperture_mode = 2;
+                    else if (v == "conditional") o->aperture_mode = 1;
+                    else if (v == "never") o->aperture_mode = 0;
+                    else throw std::invalid_argument(v);
+                } else if (k == "aperture_min_length") {
+                    o->aperture_min_length = std::stod(v);
+                } else if (k == "x_limit") {
+                    o->x_limit = std::stod(v);
+                } else if (k == "y_limit") {
+                    o->y_limit = std::stod(v);
+                } else if (k == "stages") {
+                    o->stages = std::stoi(v);
+                } else if (k == "chunk_words") {
+                    o->chunk_words = std::stoi(v);
+                } else {
+                    if (err) *err = "config: unknown key '" + k + "'";
+                    return false;
+                }
+            } catch (...) {
+                if (err) *err = "config: bad value for '" + k + "': '" + v + "'";
+                return false;
+            }
+        }
+    }
+    if (o->threads < 32 || o->threads > kMaxThreads || o->threads % 32 != 0) {
+        if (err) *err = "config: threads_per_block must be a multiple of 32 in [32, 512]";
+        return false;
+    }
+    if (o->stages < 2 || o->stages > 8) {
+        if (err) *err = "config: stages must be in [2, 8]";
+        return false;
+    }
+    if (o->chunk_words < 64 || o->chunk_words > 8192 || o->chunk_words % 2 != 0) {
+        if (err) *err = "config: chunk_words must be even and in [64, 8192]";
+        return false;
+    }
+    return true;
+}
+
+// -------------------------------------------------------------- device
+struct Device {
+    int id = -1;
+    cudaStream_t stream = nullptr;
+    int32_t *d_flags = nullptr;  // [0] status, [1] error
+    int32_t *h_flags = nullptr;  // pinned
+};
+
+static std::mutex g_dev_mu;
+static std::map<int, Device *> g_devices;
+static std::atomic<uint64_t> g_launches{0};
+
+static bool cuda_ok(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+static Device *get_device(int id)
+{
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    auto it = g_devices.find(id);
+    if (it != g_devices.end()) return it->second;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        set_error("no CUDA device available: this engine tracks on the GPU only");
+        return nullptr;
+    }
+    if (id < 0 || id >= count) {
+        set_error("device id out of range");
+        return nullptr;
+    }
+    if (!cuda_ok(cudaSetDevice(id), "cudaSetDevice")) return nullptr;
+    Device *d = new Device();
+    d->id = id;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaMalloc(&d->d_flags, 2 * sizeof(int32_t)), "cudaMalloc") ||
+        !cuda_ok(cudaMallocHost(&d->h_flags, 2 * sizeof(int32_t)), "cudaMallocHost")) {
+        delete d;
+        return nullptr;
+    }
+    g_devices[id] = d;
+    return d;
+}
+
+// ------------------------------------------------------- device stream
+struct DevStream {
+    CompiledStream cs;
+    uint64_t *d = nullptr;
+    int device = -1;
+    DevStream() = default;
+    DevStream(const DevStream &) = delete;
+    ~DevStream()
+    {
+        if (d) cudaFree(d);
+    }
+};
+
+static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b, uint64_t e,
+                                               const Options &opt, CompileOptions copt,
+                                               Device *dev)
+{
+    std::unique_ptr<DevStream> s(new DevStream());
+    copt.aperture_mode = opt.aperture_mode;
+    copt.aperture_min_length = opt.aperture_min_length;
+    copt.min_chunk_words = opt.chunk_words;
+    std::string err;
+    if (!compile_lattice(img, b, e, copt, &s->cs, &err)) {
+        set_error(err);
+        return nullptr;
+    }
+    size_t const bytes = s->cs.words.size() * 8;
+    if (!cuda_ok(cudaSetDevice(dev->id), "cudaSetDevice") ||
+        !cuda_ok(cudaMalloc(&s->d, bytes), "cudaMalloc(lattice)") ||
+        !cuda_ok(cudaMemcpy(s->d, s->cs.words.data(), bytes, cudaMemcpyHostToDevice),
+                 "cudaMemcpy(lattice)"))
+        return nullptr;
+    s->device = dev->id;
+    return s;
+}
+
+// Run one tracking pass and wait for it; returns the OR-ed status (0/-1).
+static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, uint64_t *d_cols,
+                         int64_t n, int64_t i0, int64_t i1, int mode, int64_t until_turn,
+                         bool finish_turn, uint64_t *ebe_out, int64_t ebe_cap,
+                         const EbeDevConfig *ebe, cudaStream_t stream, bool wait = true)
+{
+    TrackParams prm{};
+    prm.stream = ds.d;
+    prm.n_chunks = ds.cs.info.num_chunks;
+    prm.chunk_words = ds.cs.info.chunk_words;
+    prm.stages = opt.stages;
+    prm.mode = mode;
+    prm.num_elements = ds.cs.info.num_elements;
+    prm.cols = d_cols;
+    prm.n = n;
+    prm.i0 = i0;
+    prm.i1 = i1;
+    prm.until_turn = until_turn;
+    prm.finish_turn = finish_turn ? 1 : 0;
+    prm.xlim_bits = aperture_bits(opt.x_limit);
+    prm.ylim_bits = aperture_bits(opt.y_limit);
+    prm.status = dev->d_flags;
+    prm.error = dev->d_flags + 1;
+    prm.ebe_out = ebe_out;
+    prm.ebe_cap = ebe_cap;
+    if (ebe) prm.ebe = *ebe;
+    if (!stream) stream = dev->stream;
+    if (!cuda_ok(cudaMemsetAsync(dev->d_flags, 0, 2 * sizeof(int32_t), stream), "cudaMemsetAsync"))
+        return -1;
+    if (i1 > i0) {
+        int const rc = launch_track(prm, opt.fast, opt.threads, stream);
+        if (rc != 0) {
+            set_error(std::string("track kernel launch: ") + cudaGetErrorString((cudaError_t)rc));
+            return -1;
+        }
+        g_launches.fetch_add(1);
+    }
+    if (!wait) return 0;
+    if (!cuda_ok(cudaMemcpyAsync(dev->h_flags, dev->d_flags, 2 * sizeof(int32_t),
+                                 cudaMemcpyDeviceToHost, stream),
+                 "cudaMemcpyAsync(status)") ||
+        !cuda_ok(cudaStreamSynchronize(stream), "track kernel"))
+        return -1;
+    if (dev->h_flags[1] != 0) {
+        set_error("track kernel: shared-memory pipeline wait timed out; particles left unchanged");
+        return -1;
+    }
+    return dev->h_flags[0];
+}
+
+// ------------------------------------------------ particle columns (host)
+static double *const *real_cols(const st_Particles *p) { return &p->q0; }
+static int64_t *const *int_cols(const st_Particles *p) { return &p->particle_id; }
+
+static void gather(const st_Particles *p, int64_t i0, int64_t cnt, uint64_t *blk)
+{
+    for (int c = 0; c < 17; ++c) std::memcpy(blk + (size_t)c * cnt, real_cols(p)[c] + i0, cnt * 8);
+    for (int c = 0; c < 4; ++c)
+        std::memcpy(blk + (size_t)(17 + c) * cnt, int_cols(p)[c] + i0, cnt * 8);
+}
+
+static void scatter(st_Particles *p, int64_t i0, int64_t cnt, const uint64_t *blk)
+{
+    for (int c = 0; c < 17; ++c) std::memcpy(real_cols(p)[c] + i0, blk + (size_t)c * cnt, cnt * 8);
+    for (int c = 0; c < 4; ++c)
+        std::memcpy(int_cols(p)[c] + i0, blk + (size_t)(17 + c) * cnt, cnt * 8);
+}
+
+// Host "generic address" output (NS(ParticlesGenericAddr), particles.h:70-98):
+// 1 word count + 21 column addresses.
+struct GenericOut {
+    const uint64_t *desc = nullptr;
+    int64_t n = 0;
+    uint64_t *d = nullptr;
+    bool download(cudaStream_t s)
+    {
+        std::vector<uint64_t> blk((size_t)n * 21);
+        if (!cuda_ok(cudaMemcpyAsync(blk.data(), d, blk.size() * 8, cudaMemcpyDeviceToHost, s),
+                     "cudaMemcpy(output)") ||
+            !cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize"))
+            return false;
+        for (int c = 0; c < 21; ++c)
+            std::memcpy((void *)(uintptr_t)desc[1 + c], blk.data() + (size_t)c * n, (size_t)n * 8);
+        return true;
+    }
+    bool upload(cudaStream_t s)
+    {
+        std::vector<uint64_t> blk((size_t)n * 21);
+        for (int c = 0; c < 21; ++c)
+            std::memcpy(blk.data() + (size_t)c * n, (const void *)(uintptr_t)desc[1 + c], (size_t)n * 8);
+        if (!cuda_ok(cudaMalloc(&d, blk.size() * 8 + 8), "cudaMalloc(output)")) return false;
+        return cuda_ok(cudaMemcpyAsync(d, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice, s),
+                       "cudaMemcpy(output)") &&
+               cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+    ~GenericOut()
+    {
+        if (d) cudaFree(d);
+    }
+};
+
+// One-shot tracking of host particles (the free functions).
+static int32_t track_host(st_Particles *p, int64_t i0, int64_t i1, const st_Buffer *belems,
+                          int mode, int64_t until, uint64_t lb, uint64_t le, bool finish,
+                          const st_ElemByElemConfig *ebe_cfg)
+{
+    clear_error();
+    if (!p || !belems) {
+        set_error("null particles or beam-elements buffer");
+        return -1;
+    }
+    if (i0 < 0 || i1 > p->num_particles || i0 > i1) {
+        set_error("particle index out of range");
+        return -1;
+    }
+    Options opt;
+    const char *env = std::getenv("SIXTRACKLIB_GB300_CONFIG");
+    std::string perr;
+    if (env && !parse_options(env, &opt, &perr)) {
+        set_error(perr);
+        return -1;
+    }
+    Device *dev = get_device(opt.device);
+    if (!dev) return -1;
+    cudaSetDevice(dev->id);
+    ImageView img;
+    std::string err;
+    if (!img.open(st_Buffer_get_const_data_begin(belems), st_Buffer_get_size(belems), &err)) {
+        set_error(err);
+        return -1;
+    }
+    if (mode == MODE_UNTIL && img.num_objects == 0) return i1 > i0 ? -1 : 0;
+    if (mode == MODE_LINE) {
+        if (lb > le || le > img.num_objects) {
+            set_error("line range outside the lattice");
+            return -1;
+        }
+    }
+    cudaStream_t const s = dev->stream;
+    std::vector<std::unique_ptr<GenericOut>> outs;
+    CompileOptions copt;
+    copt.monitor_output = [&](uint64_t ei) -> std::pair<uint64_t, int64_t> {
+        const uint64_t *m = img.words(ei);
+        if (m[3] == 0) return {0, 0};
+        std::unique_ptr<GenericOut> o(new GenericOut());
+        o->desc = (const uint64_t *)(uintptr_t)m[3];
+        o->n = (int64_t)o->desc[0];
+        if (o->n <= 0 || !o->upload(s)) return {0, 0};
+        uint64_t const ptr = (uint64_t)(uintptr_t)o->d;
+        int64_t const cap = o->n;
+        outs.push_back(std::move(o));
+        return {ptr, cap};
+    };
+    uint64_t b = 0, e = img.num_objects;
+    if (mode == MODE_LINE) {
+        b = lb;
+        e = le;
+    }
+    auto ds = build_stream(img, b, e, opt, copt, dev);
+    if (!ds) return -1;
+    int64_t const cnt = i1 - i0;
+    std::vector<uint64_t> blk((size_t)cnt * 21);
+    gather(p, i0, cnt, blk.data());
+    uint64_t *d_cols = nullptr;
+    GenericOut ebe_out;
+    EbeDevConfig ebe{};
+    if (mode == MODE_EBE) {
+        if (ebe_cfg && ebe_cfg->out_store_addr != 0) {
+            ebe_out.desc = (const uint64_t *)(uintptr_t)ebe_cfg->out_store_addr;
+            ebe_out.n = (int64_t)ebe_out.desc[0];
+            if (!ebe_out.upload(s)) return -1;
+            std::memcpy(&ebe, ebe_cfg, sizeof(ebe));
+        } else {
+            mode = MODE_UNTIL;  // track/track.h:770-775: no output -> until_turn
+        }
+    }
+    int32_t st = -1;
+    if (cuda_ok(cudaMalloc(&d_cols, blk.size() * 8 + 8), "cudaMalloc(particles)") &&
+        cuda_ok(cudaMemcpyAsync(d_cols, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice, s),
+                "cudaMemcpy(particles)")) {
+        st = run_track(dev, opt, *ds, d_cols, cnt, 0, cnt, mode, until, finish, ebe_out.d,
+                       ebe_out.n, mode == MODE_EBE ? &ebe : nullptr, s);
+        bool const ok = cuda_ok(cudaMemcpyAsync(blk.data(), d_cols, blk.size() * 8,
+                                                cudaMemcpyDeviceToHost, s),
+                                "cudaMemcpy(particles)") &&
+                        cuda_ok(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        if (ok) {
+            scatter(p, i0, cnt, blk.data());
+            for (auto &o : outs) o->download(s);
+            if (ebe_out.d) ebe_out.download(s);
+        } else {
+            st = -1;
+        }
+    }
+    if (d_cols) cudaFree(d_cols);
+    return st;
+}
+
+}  // namespace stg
+
+using namespace stg;
+
+// =================================================================== C ABI
+extern "C" {
+
+st_track_status_t st_Track_particle_until_turn(st_Particles *p, int64_t idx,
+                                               const st_Buffer *be, int64_t until_turn)
+{
+    return track_host(p, idx, idx + 1, be, MODE_UNTIL, until_turn, 0, 0, false, nullptr);
+}
+
+st_track_status_t st_Track_all_particles_until_turn(st_Particles *p, const st_Buffer *be,
+                                                    int64_t until_turn)
+{
+    return track_host(p, 0, p ? p->num_particles : 0, be, MODE_UNTIL, until_turn, 0, 0, false,
+                      nullptr);
+}
+
+st_track_status_t st_Track_particle_element_by_element_until_turn(
+    st_Particles *p, int64_t idx, const st_ElemByElemConfig *cfg, const st_Buffer *be,
+    int64_t until_turn)
+{
+    return track_host(p, idx, idx + 1, be, MODE_EBE, until_turn, 0, 0, false, cfg);
+}
+
+st_track_status_t st_Track_all_particles_element_by_element_until_turn(
+    st_Particles *p, const st_ElemByElemConfig *cfg, const st_Buffer *be, int64_t until_turn)
+{
+    return track_host(p, 0, p ? p->num_particles : 0, be, MODE_EBE, until_turn, 0, 0, false, cfg);
+}
+
+st_track_status_t st_Track_particle_line(st_Particles *p, int64_t idx, const st_Buffer *be,
+                                         st_buffer_size_t b, st_buffer_size_t e, bool finish)
+{
+    return track_host(p, idx, idx + 1, be, MODE_LINE, 0, b, e, finish, nullptr);
+}
+
+st_track_status_t st_Track_all_particles_line(st_Particles *p, const st_Buffer *be,
+                                              st_buffer_size_t b, st_buffer_size_t e,
+                                              bool finish)
+{
+    return track_host(p, 0, p ? p->num_particles : 0, be, MODE_LINE, 0, b, e, finish, nullptr);
+}
+
+uint64_t st_engine_kernel_launches(void) { return g_launches.load(); }
+
+const char *st_engine_build_info(void)
+{
+    return "sixtracklib_gb300: sm_103a, FP64 tracking kernel (exact | fast), "
+           "TMA bulk-copy lattice staging";
+}
+
+}  // extern "C"
+
+// ============================================================ DeviceLattice
+struct st_DeviceLattice {
+    Options opt;
+    Device *dev = nullptr;
+    std::vector<uint64_t> image;
+    std::unique_ptr<DevStream> full;
+    std::map<std::pair<uint64_t, uint64_t>, std::unique_ptr<DevStream>> lines;
+    cudaStream_t last_stream = nullptr;
+};
+
+extern "C" {
+
+st_DeviceLattice *st_DeviceLattice_new(const unsigned char *image, st_buffer_size_t size,
+                                       const char *config)
+{
+    clear_error();
+    std::unique_ptr<st_DeviceLattice> L(new st_DeviceLattice());
+    std::string err;
+    if (!parse_options(config, &L->opt, &err)) {
+        set_error(err);
+        return nullptr;
+    }
+    L->dev = get_device(L->opt.device);
+    if (!L->dev) return nullptr;
+    L->image.assign((size + 7) / 8, 0);
+    std::memcpy(L->image.data(), image, size);
+    ImageView img;
+    if (!img.open(L->image.data(), size, &err)) {
+        set_error(err);
+        return nullptr;
+    }
+    L->full = build_stream(img, 0, img.num_objects, L->opt, CompileOptions(), L->dev);
+    if (!L->full) return nullptr;
+    return L.release();
+}
+
+void st_DeviceLattice_delete(st_DeviceLattice *L) { delete L; }
+
+int64_t st_DeviceLattice_num_elements(const st_DeviceLattice *L)
+{
+    return L ? L->full->cs.info.num_elements : 0;
+}
+int64_t st_DeviceLattice_num_chunks(const st_DeviceLattice *L)
+{
+    return L ? L->full->cs.info.num_chunks : 0;
+}
+
+st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols, int64_t n,
+                                               int64_t until_turn, void *stream)
+{
+    if (!L || !d_cols) return -1;
+    if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
+    cudaSetDevice(L->dev->id);
+    return run_track(L->dev, L->opt, *L->full, (uint64_t *)d_cols, n, 0, n, MODE_UNTIL,
+                     until_turn, false, nullptr, 0, nullptr, (cudaStream_t)stream);
+}
+
+st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *L, void *d_cols, int64_t n,
+                                              uint64_t b, uint64_t e, bool finish, void *stream)
+{
+    if (!L || !d_cols) return -1;
+    auto key = std::make_pair(b, e);
+    auto it = L->lines.find(key);
+    if (it == L->lines.end()) {
+        ImageView img;
+        std::string err;
+        img.open(L->image.data(), L->image.size() * 8, &err);
+        auto ds = build_stream(img, b, e, L->opt, CompileOptions(), L->dev);
+        if (!ds) return -1;
+        it = L->lines.emplace(key, std::move(ds)).first;
+    }
+    cudaSetDevice(L->dev->id);
+    return run_track(L->dev, L->opt, *it->second, (uint64_t *)d_cols, n, 0, n, MODE_LINE, 0,
+                     finish, nullptr, 0, nullptr, (cudaStream_t)stream);
+}
+
+int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t n,
+                                      int64_t until_turn, void *stream)
+{
+    if (!L || !d_cols) return -1;
+    if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
+    cudaSetDevice(L->dev->id);
+    L->last_stream = stream ? (cudaStream_t)stream : L->dev->stream;
+    return run_track(L->dev, L->opt, *L->full, (uint64_t *)d_cols, n, 0, n, MODE_UNTIL,
+                     until_turn, false, nullptr, 0, nullptr, L->last_stream, false);
+}
+
+st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *L)
+{
+    if (!L) return -1;
+    cudaStream_t s = L->last_stream ? L->last_stream : L->dev->stream;
+    if (!cuda_ok(cudaMemcpyAsync(L->dev->h_flags, L->dev->d_flags, 2 * sizeof(int32_t),
+                                 cudaMemcpyDeviceToHost, s),
+                 "cudaMemcpyAsync(status)") ||
+        !cuda_ok(cudaStreamSynchronize(s), "track kernel"))
+        return -1;
+    if (L->dev->h_flags[1] != 0) {
+        set_error("track kernel: shared-memory pipeline wait timed out");
+        return -1;
+    }
+    return L->dev->h_flags[0];
+}
+
+}  // extern "C"
+
+// ================================================================ TrackJob
+struct OutBlock {
+    uint64_t obj_index = 0;  // Particles object in the output buffer
+    int64_t cap = 0;
+    uint64_t *d = nullptr;   // device column block (inside the job's output arena)
+};
+
+struct st_TrackJob {
+    Options opt;
+    std::string arch = "cuda", config, device_id_str;
+    Device *dev = nullptr;
+    st_Buffer *pbuf = nullptr, *ebuf = nullptr, *obuf = nullptr;
+    bool owns_obuf = false;
+    std::vector<st_buffer_size_t> psets;
+    std::vector<int64_t> pset_off, pset_cnt;
+    int64_t n_total = 0;
+    uint64_t *d_cols = nullptr;
+    std::unique_ptr<DevStream> lat;
+    std::map<std::pair<uint64_t, uint64_t>, std::unique_ptr<DevStream>> lines;
+    uint64_t *d_out = nullptr;
+    std::vector<OutBlock> outs;  // [ebe?] + monitors
+    bool has_ebe = false;
+    st_ElemByElemConfig ebe_cfg{};
+    uint64_t ebe_out_offset = 0, bemon_out_offset = 0;
+    uint64_t until_turn_ebe = 0;
+    std::vector<st_buffer_size_t> monitor_indices;
+    std::map<uint64_t, size_t> monitor_block;  // element index -> outs index
+    int64_t min_pid = 0, max_pid = 0, min_elem = 0, max_elem = 0, min_turn = 0, max_turn = 0;
+    uint16_t collect_flags = 0x05;  // particles | output (track/definitions.h)
+    bool default_rolling = true;
+
+    ~st_TrackJob() { release(); }
+    void release()
+    {
+        if (d_cols) cudaFree(d_cols);
+        if (d_out) cudaFree(d_out);
+        d_cols = nullptr;
+        d_out = nullptr;
+        lat.reset();
+        lines.clear();
+        outs.clear();
+        if (owns_obuf && obuf) st_Buffer_delete(obuf);
+        obuf = nullptr;
+        owns_obuf = false;
+        monitor_block.clear();
+        monitor_indices.clear();
+        has_ebe = false;
+    }
+};
+
+namespace {
+
+st_Particles *pset(st_TrackJob *j, size_t k)
+{
+    return st_Particles_buffer_get_particles(j->pbuf, j->psets[k]);
+}
+
+bool upload_particles(st_TrackJob *j)
+{
+    std::vector<uint64_t> blk((size_t)j->n_total * 21);
+    for (size_t k = 0; k < j->psets.size(); ++k) {
+        st_Particles *p = pset(j, k);
+        int64_t const cnt = j->pset_cnt[k];
+        std::vector<uint64_t> part((size_t)cnt * 21);
+        gather(p, 0, cnt, part.data());
+        for (int c = 0; c < 21; ++c)
+            std::memcpy(blk.data() + (size_t)c * j->n_total + j->pset_off[k],
+                        part.data() + (size_t)c * cnt, (size_t)cnt * 8);
+    }
+    return cuda_ok(cudaMemcpy(j->d_cols, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice),
+                   "cudaMemcpy(particles)");
+}
+
+bool download_particles(st_TrackJob *j)
+{
+    std::vector<uint64_t> blk((size_t)j->n_total * 21);
+    if (!cuda_ok(cudaMemcpy(blk.data(), j->d_cols, blk.size() * 8, cudaMemcpyDeviceToHost),
+                 "cudaMemcpy(particles)"))
+        return false;
+    for (size_t k = 0; k < j->psets.size(); ++k) {
+        int64_t const cnt = j->pset_cnt[k];
+        std::vector<uint64_t> part((size_t)cnt * 21);
+        for (int c = 0; c < 21; ++c)
+            std::memcpy(part.data() + (size_t)c * cnt,
+                        blk.data() + (size_t)c * j->n_total + j->pset_off[k], (size_t)cnt * 8);
+        scatter(pset(j, k), 0, cnt, part.data());
+    }
+    return true;
+}
+
+bool transfer_outputs(st_TrackJob *j, bool to_device)
+{
+    for (const OutBlock &o : j->outs) {
+        st_Particles *p = st_Particles_buffer_get_particles(j->obuf, o.obj_index);
+        if (!p) return false;
+        std::vector<uint64_t> blk((size_t)o.cap * 21);
+        if (to_device) {
+            gather(p, 0, o.cap, blk.data());
+            if (!cuda_ok(cudaMemcpy(o.d, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice),
+                         "cudaMemcpy(output)"))
+                return false;
+        } else {
+            if (!cuda_ok(cudaMemcpy(blk.data(), o.d, blk.size() * 8, cudaMemcpyDeviceToHost),
+                         "cudaMemcpy(output)"))
+                return false;
+            scatter(p, 0, o.cap, blk.data());
+        }
+    }
+    return true;
+}
+
+bool compile_job_lattice(st_TrackJob *j)
+{
+    ImageView img;
+    std::string err;
+    if (!img.open(st_Buffer_get_const_data_begin(j->ebuf), st_Buffer_get_size(j->ebuf), &err)) {
+        set_error(err);
+        return false;
+    }
+    CompileOptions copt;
+    copt.monitor_output = [j](uint64_t ei) -> std::pair<uint64_t, int64_t> {
+        auto it = j->monitor_block.find(ei);
+        if (it == j->monitor_block.end()) return {0, 0};
+        const OutBlock &o = j->outs[it->second];
+        return {(uint64_t)(uintptr_t)o.d, o.cap};
+    };
+    j->lat = build_stream(img, 0, img.num_objects, j->opt, copt, j->dev);
+    j->lines.clear();
+    return j->lat != nullptr;
+}
+
+// Min/max attributes (output/output_buffer.h:461-560,
+// elem_by_elem_output_buffer.h:162-230) and output preparation
+// (output/output_buffer.c:288-360, be_monitor/output_buffer.c).
+bool setup_job(st_TrackJob *j, st_Buffer *pb, st_buffer_size_t nsets, const st_buffer_size_t *idx,
+               st_Buffer *eb, st_Buffer *ob, st_buffer_size_t until_ebe)
+{
+    j->release();
+    if (!pb || !eb) {
+        set_error("TrackJob: particles and beam-elements buffers are required");
+        return false;
+    }
+    j->pbuf = pb;
+    j->ebuf = eb;
+    j->psets.clear();
+    if (nsets > 0 && idx) {
+        j->psets.assign(idx, idx + nsets);
+    } else {
+        for (st_buffer_size_t i = 0; i < st_Buffer_get_num_of_objects(pb); ++i)
+            if (st_Particles_buffer_get_particles(pb, i)) {
+                j->psets.push_back(i);
+                break;
+            }
+    }
+    if (j->psets.empty()) {
+        set_error("TrackJob: no particle set in the particles buffer");
+        return false;
+    }
+    j->pset_off.clear();
+    j->pset_cnt.clear();
+    j->n_total = 0;
+    bool first = true;
+    for (size_t k = 0; k < j->psets.size(); ++k) {
+        st_Particles *p = pset(j, k);
+        if (!p) {
+            set_error("TrackJob: particle set index does not name a Particles object");
+            return false;
+        }
+        j->pset_off.push_back(j->n_total);
+        j->pset_cnt.push_back(p->num_particles);
+        j->n_total += p->num_particles;
+        for (int64_t i = 0; i < p->num_particles; ++i) {
+            int64_t const pid = p->particle_id[i], ae = p->at_element_id[i], at = p->at_turn[i];
+            if (first) {
+                j->min_pid = j->max_pid = pid;
+                j->min_elem = j->max_elem = ae;
+                j->min_turn = j->max_turn = at;
+                first = false;
+            }
+            j->min_pid = std::min(j->min_pid, pid);
+            j->max_pid = std::max(j->max_pid, pid);
+            j->min_elem = std::min(j->min_elem, ae);
+            j->max_elem = std::max(j->max_elem, ae);
+            j->min_turn = std::min(j->min_turn, at);
+            j->max_turn = std::max(j->max_turn, at);
+        }
+    }
+    if (j->min_pid < 0) j->min_pid = 0;
+    if (j->min_elem < 0) j->min_elem = 0;
+    if (j->min_turn < 0) j->min_turn = 0;
+    // element id range of the lattice (every object counts as an element)
+    uint64_t const ne = st_Buffer_get_num_of_objects(eb);
+    if (ne > 0) {
+        j->min_elem = std::min<int64_t>(j->min_elem, 0);
+        j->max_elem = std::max<int64_t>(j->max_elem, (int64_t)ne - 1);
+    }
+    // beam monitors that get output
+    std::vector<uint64_t> mons;
+    const st_Object *ob_begin = st_Buffer_get_const_objects_begin(eb);
+    for (uint64_t i = 0; i < ne; ++i) {
+        if (ob_begin[i].type_id != ST_OBJECT_TYPE_BEAM_MONITOR) continue;
+        j->monitor_indices.push_back(i);
+        st_BeamMonitor *m = (st_BeamMonitor *)(uintptr_t)ob_begin[i].begin_addr;
+        if (m->start >= j->min_turn && m->num_stores > 0) mons.push_back(i);
+    }
+    j->until_turn_ebe = 0;
+    bool const want_ebe = until_ebe > 0 && until_ebe > (uint64_t)j->min_turn;
+    if (want_ebe || !mons.empty()) {
+        if (!ob) {
+            ob = st_Buffer_new(0);
+            if (!ob) return false;
+            j->owns_obuf = true;
+        }
+        j->obuf = ob;
+    } else {
+        j->obuf = ob;
+    }
+    std::vector<std::pair<uint64_t, int64_t>> blocks;  // (obj index, cap)
+    if (want_ebe) {
+        st_ElemByElemConfig_init_detailed(&j->ebe_cfg, 0, j->min_pid, j->max_pid, j->min_elem,
+                                          j->max_elem, j->min_turn, (int64_t)until_ebe - 1,
+                                          j->default_rolling);
+        int64_t const cap = st_ElemByElemConfig_get_stored_num_particles(&j->ebe_cfg);
+        j->ebe_out_offset = st_Buffer_get_num_of_objects(j->obuf);
+        if (!st_Particles_new(j->obuf, (st_buffer_size_t)cap)) return false;
+        blocks.push_back({j->ebe_out_offset, cap});
+        j->has_ebe = true;
+        j->until_turn_ebe = until_ebe;
+    }
+    j->bemon_out_offset = j->obuf ? st_Buffer_get_num_of_objects(j->obuf) : 0;
+    for (uint64_t i : mons) {
+        st_BeamMonitor *m = (st_BeamMonitor *)(uintptr_t)st_Buffer_get_const_objects_begin(eb)[i].begin_addr;
+        m->min_particle_id = j->min_pid;
+        m->max_particle_id = j->max_pid;
+        m->out_address = 0;
+        int64_t const cap = (j->max_pid - j->min_pid + 1) * m->num_stores;
+        uint64_t const oi = st_Buffer_get_num_of_objects(j->obuf);
+        if (!st_Particles_new(j->obuf, (st_buffer_size_t)cap)) return false;
+        j->monitor_block[i] = blocks.size();
+        blocks.push_back({oi, cap});
+    }
+    // device allocations
+    cudaSetDevice(j->dev->id);
+    if (!cuda_ok(cudaMalloc(&j->d_cols, (size_t)std::max<int64_t>(j->n_total, 1) * 21 * 8),
+                 "cudaMalloc(particles)"))
+        return false;
+    size_t total = 0;
+    for (auto &b : blocks) total += (size_t)b.second * 21;
+    if (total > 0 && !cuda_ok(cudaMalloc(&j->d_out, total * 8), "cudaMalloc(output)")) return false;
+    size_t off = 0;
+    for (auto &b : blocks) {
+        OutBlock o;
+        o.obj_index = b.first;
+        o.cap = b.second;
+        o.d = j->d_out + off;
+        off += (size_t)b.second * 21;
+        j->outs.push_back(o);
+    }
+    if (!upload_particles(j) || !transfer_outputs(j, true)) return false;
+    return compile_job_lattice(j);
+}
+
+bool arch_ok(const char *arch)
+{
+    std::string a = arch ? arch : "cuda";
+    std::transform(a.begin(), a.end(), a.begin(), ::tolower);
+    a = trim(a);
+    if (a.empty() || a == "cuda" || a == "gb300" || a == "gpu") return true;
+    set_error("TrackJob: architecture '" + a +
+              "' is not provided by this engine (it tracks on the GPU: use \"cuda\")");
+    return false;
+}
+
+st_TrackJob *make_job(const char *arch, const char *cfg)
+{
+    clear_error();
+    if (!arch_ok(arch)) return nullptr;
+    std::unique_ptr<st_TrackJob> j(new st_TrackJob());
+    std::string err;
+    if (!parse_options(cfg, &j->opt, &err)) {
+        set_error(err);
+        return nullptr;
+    }
+    j->config = cfg ? cfg : "";
+    j->dev = get_device(j->opt.device);
+    if (!j->dev) return nullptr;
+    j->device_id_str = "0." + std::to_string(j->dev->id);
+    return j.release();
+}
+
+}  // namespace
+
+extern "C" {
+
+st_TrackJob *st_TrackJob_create(const char *arch, const char *cfg) { return make_job(arch, cfg); }
+
+st_TrackJob *st_TrackJob_new(const char *arch, st_Buffer *pb, st_Buffer *eb, const char *cfg)
+{
+    return st_TrackJob_new_detailed(arch, pb, 0, nullptr, eb, nullptr, 0, cfg);
+}
+
+st_TrackJob *st_TrackJob_new_with_output(const char *arch, st_Buffer *pb, st_Buffer *eb,
+                                         st_Buffer *ob, st_buffer_size_t until_ebe,
+                                         const char *cfg)
+{
+    return st_TrackJob_new_detailed(arch, pb, 0, nullptr, eb, ob, until_ebe, cfg);
+}
+
+st_TrackJob *st_TrackJob_new_detailed(const char *arch, st_Buffer *pb, st_buffer_size_t nsets,
+                                      const st_buffer_size_t *idx, st_Buffer *eb,
+                                      st_Buffer *ob, st_buffer_size_t until_ebe, const char *cfg)
+{
+    st_TrackJob *j = make_job(arch, cfg);
+    if (!j) return nullptr;
+    if (!setup_job(j, pb, nsets, idx, eb, ob, until_ebe)) {
+        std::string const e = st_last_error();
+        delete j;
+        set_error(e);
+        return nullptr;
+    }
+    return j;
+}
+
+bool st_TrackJob_reset(st_TrackJob *j, st_Buffer *pb, st_Buffer *eb, st_Buffer *ob)
+{
+    return j && setup_job(j, pb, 0, nullptr, eb, ob, 0);
+}
+bool st_TrackJob_reset_with_output(st_TrackJob *j, st_Buffer *pb, st_Buffer *eb, st_Buffer *ob,
+                                   st_buffer_size_t until_ebe)
+{
+    return j && setup_job(j, pb, 0, nullptr, eb, ob, until_ebe);
+}
+bool st_TrackJob_reset_detailed(st_TrackJob *j, st_Buffer *pb, st_buffer_size_t nsets,
+                                const st_buffer_size_t *idx, st_Buffer *eb, st_Buffer *ob,
+                                st_buffer_size_t until_ebe)
+{
+    return j && setup_job(j, pb, nsets, idx, eb, ob, until_ebe);
+}
+
+void st_TrackJob_delete(st_TrackJob *j) { delete j; }
+void st_TrackJob_clear(st_TrackJob *j)
+{
+    if (j) j->release();
+}
+
+st_track_status_t st_TrackJob_track_until(st_TrackJob *j, st_buffer_size_t until_turn)
+{
+    if (!j || !j->lat) return -1;
+    clear_error();
+    cudaSetDevice(j->dev->id);
+    if (j->lat->cs.info.num_elements == 0) return j->n_total > 0 ? -1 : 0;
+    return run_track(j->dev, j->opt, *j->lat, j->d_cols, j->n_total, 0, j->n_total, MODE_UNTIL,
+                     (int64_t)until_turn, false, nullptr, 0, nullptr, j->dev->stream);
+}
+
+st_track_status_t st_TrackJob_track_elem_by_elem(st_TrackJob *j, st_buffer_size_t until_turn)
+{
+    if (!j || !j->lat) return -1;
+    clear_error();
+    if (!j->has_ebe || j->outs.empty()) {
+        set_error("TrackJob: no elem-by-elem output configured (until_turn_elem_by_elem)");
+        return -1;
+    }
+    cudaSetDevice(j->dev->id);
+    EbeDevConfig ebe;
+    std::memcpy(&ebe, &j->ebe_cfg, sizeof(ebe));
+    const OutBlock &o = j->outs[0];
+    return run_track(j->dev, j->opt, *j->lat, j->d_cols, j->n_total, 0, j->n_total, MODE_EBE,
+                     (int64_t)until_turn, false, o.d, o.cap, &ebe, j->dev->stream);
+}
+
+st_track_status_t st_TrackJob_track_line(st_TrackJob *j, st_buffer_size_t b, st_buffer_size_t e,
+                                         bool finish)
+{
+    if (!j || !j->lat) return -1;
+    clear_error();
+    uint64_t const ne = st_Buffer_get_num_of_objects(j->ebuf);
+    if (b > e || e > ne) {
+        set_error("TrackJob: line range outside the lattice");
+        return -1;
+    }
+    auto key = std::make_pair((uint64_t)b, (uint64_t)e);
+    auto it = j->lines.find(key);
+    if (it == j->lines.end()) {
+        ImageView img;
+        std::string err;
+        if (!img.open(st_Buffer_get_const_data_begin(j->ebuf), st_Buffer_get_size(j->ebuf), &err)) {
+            set_error(err);
+            return -1;
+        }
+        CompileOptions copt;
+        copt.monitor_output = [j](uint64_t ei) -> std::pair<uint64_t, int64_t> {
+            auto mit = j->monitor_block.find(ei);
+            if (mit == j->monitor_block.end()) return {0, 0};
+            const OutBlock &o = j->outs[mit->second];
+            return {(uint64_t)(uintptr_t)o.d, o.cap};
+        };
+        auto ds = build_stream(img, b, e, j->opt, copt, j->dev);
+        if (!ds) return -1;
+        it = j->lines.emplace(key, std::move(ds)).first;
+    }
+    cudaSetDevice(j->dev->id);
+    return run_track(j->dev, j->opt, *it->second, j->d_cols, j->n_total, 0, j->n_total, MODE_LINE,
+                     0, finish, nullptr, 0, nullptr, j->dev->stream);
+}
+
+void st_TrackJob_collect_particles(st_TrackJob *j)
+{
+    if (j && j->d_cols) download_particles(j);
+}
+void st_TrackJob_collect_beam_elements(st_TrackJob *j) { (void)j; }
+void st_TrackJob_collect_output(st_TrackJob *j)
+{
+    if (j && !j->outs.empty()) transfer_outputs(j, false);
+}
+void st_TrackJob_collect_detailed(st_TrackJob *j, uint16_t flags)
+{
+    if (!j) return;
+    if (flags & 0x01) st_TrackJob_collect_particles(j);
+    if (flags & 0x02) st_TrackJob_collect_beam_elements(j);
+    if (flags & 0x04) st_TrackJob_collect_output(j);
+}
+void st_TrackJob_collect(st_TrackJob *j)
+{
+    if (j) st_TrackJob_collect_detailed(j, j->collect_flags);
+}
+void st_TrackJob_push_particles(st_TrackJob *j)
+{
+    if (j && j->d_cols) upload_particles(j);
+}
+void st_TrackJob_push_beam_elements(st_TrackJob *j)
+{
+    if (j && j->ebuf) compile_job_lattice(j);
+}
+void st_TrackJob_push_output(st_TrackJob *j)
+{
+    if (j && !j->outs.empty()) transfer_outputs(j, true);
+}
+void st_TrackJob_push(st_TrackJob *j, uint16_t flags)
+{
+    if (!j) return;
+    if (flags & 0x01) st_TrackJob_push_particles(j);
+    if (flags & 0x02) st_TrackJob_push_beam_elements(j);
+    if (flags & 0x04) st_TrackJob_push_output(j);
+}
+
+void st_TrackJob_enable_collect_particles(st_TrackJob *j) { if (j) j->collect_flags |= 0x01; }
+void st_TrackJob_disable_collect_particles(st_TrackJob *j) { if (j) j->collect_flags &= ~0x01; }
+bool st_TrackJob_is_collecting_particles(const st_TrackJob *j) { return j && (j->collect_flags & 0x01); }
+void st_TrackJob_enable_collect_beam_elements(st_TrackJob *j) { if (j) j->collect_flags |= 0x02; }
+void st_TrackJob_disable_collect_beam_elements(st_TrackJob *j) { if (j) j->collect_flags &= ~0x02; }
+bool st_TrackJob_is_collecting_beam_elements(const st_TrackJob *j) { return j && (j->collect_flags & 0x02); }
+void st_TrackJob_enable_collect_output(st_TrackJob *j) { if (j) j->collect_flags |= 0x04; }
+void st_TrackJob_disable_collect_output(st_TrackJob *j) { if (j) j->collect_flags &= ~0x04; }
+bool st_TrackJob_is_collecting_output(const st_TrackJob *j) { return j && (j->collect_flags & 0x04); }
+uint16_t st_TrackJob_get_collect_flags(const st_TrackJob *j) { return j ? j->collect_flags : 0; }
+void st_TrackJob_set_collect_flags(st_TrackJob *j, uint16_t f) { if (j) j->collect_flags = f; }
+bool st_TrackJob_requires_collecting(const st_TrackJob *j) { return j != nullptr; }
+
+int64_t st_TrackJob_get_type_id(const st_TrackJob *j) { return j ? 2 : -1; }
+const char *st_TrackJob_get_type_str(const st_TrackJob *j) { return j ? "cuda" : ""; }
+bool st_TrackJob_has_device_id_str(const st_TrackJob *j) { return j && !j->device_id_str.empty(); }
+const char *st_TrackJob_get_device_id_str(const st_TrackJob *j)
+{
+    return j ? j->device_id_str.c_str() : "";
+}
+bool st_TrackJob_has_config_str(const st_TrackJob *j) { return j && !j->config.empty(); }
+const char *st_TrackJob_get_config_str(const st_TrackJob *j) { return j ? j->config.c_str() : ""; }
+st_buffer_size_t st_TrackJob_get_num_particle_sets(const st_TrackJob *j)
+{
+    return j ? j->psets.size() : 0;
+}
+const st_buffer_size_t *st_TrackJob_get_particle_set_indices_begin(const st_TrackJob *j)
+{
+    return (j && !j->psets.empty()) ? j->psets.data() : nullptr;
+}
+const st_buffer_size_t *st_TrackJob_get_particle_set_indices_end(const st_TrackJob *j)
+{
+    return (j && !j->psets.empty()) ? j->psets.data() + j->psets.size() : nullptr;
+}
+st_buffer_size_t st_TrackJob_get_particle_set_index(const st_TrackJob *j, st_buffer_size_t n)
+{
+    return (j && n < j->psets.size()) ? j->psets[n] : (st_buffer_size_t)-1;
+}
+st_buffer_size_t st_TrackJob_get_total_num_particles_in_sets(const st_TrackJob *j)
+{
+    return j ? (st_buffer_size_t)j->n_total : 0;
+}
+int64_t st_TrackJob_get_min_particle_id(const st_TrackJob *j) { return j ? j->min_pid : -1; }
+int64_t st_TrackJob_get_max_particle_id(const st_TrackJob *j) { return j ? j->max_pid : -1; }
+int64_t st_TrackJob_get_min_element_id(const st_TrackJob *j) { return j ? j->min_elem : -1; }
+int64_t st_TrackJob_get_max_element_id(const st_TrackJob *j) { return j ? j->max_elem : -1; }
+int64_t st_TrackJob_get_min_initial_turn_id(const st_TrackJob *j) { return j ? j->min_turn : -1; }
+int64_t st_TrackJob_get_max_initial_turn_id(const st_TrackJob *j) { return j ? j->max_turn : -1; }
+st_Buffer *st_TrackJob_get_particles_buffer(st_TrackJob *j) { return j ? j->pbuf : nullptr; }
+const st_Buffer *st_TrackJob_get_const_particles_buffer(const st_TrackJob *j)
+{
+    return j ? j->pbuf : nullptr;
+}
+st_Buffer *st_TrackJob_get_beam_elements_buffer(st_TrackJob *j) { return j ? j->ebuf : nullptr; }
+const st_Buffer *st_TrackJob_get_const_beam_elements_buffer(const st_TrackJob *j)
+{
+    return j ? j->ebuf : nullptr;
+}
+bool st_TrackJob_has_output_buffer(const st_TrackJob *j) { return j && j->obuf; }
+bool st_TrackJob_owns_output_buffer(const st_TrackJob *j) { return j && j->owns_obuf; }
+st_Buffer *st_TrackJob_get_output_buffer(st_TrackJob *j) { return j ? j->obuf : nullptr; }
+const st_Buffer *st_TrackJob_get_const_output_buffer(const st_TrackJob *j)
+{
+    return j ? j->obuf : nullptr;
+}
+bool st_TrackJob_has_elem_by_elem_output(const st_TrackJob *j) { return j && j->has_ebe; }
+bool st_TrackJob_has_beam_monitor_output(const st_TrackJob *j)
+{
+    return j && !j->monitor_block.empty();
+}
+st_buffer_size_t st_TrackJob_get_elem_by_elem_output_buffer_offset(const st_TrackJob *j)
+{
+    return j ? j->ebe_out_offset : 0;
+}
+st_buffer_size_t st_TrackJob_get_beam_monitor_output_buffer_offset(const st_TrackJob *j)
+{
+    return j ? j->bemon_out_offset : 0;
+}
+st_buffer_size_t st_TrackJob_get_num_elem_by_elem_turns(const st_TrackJob *j)
+{
+    return j ? j->until_turn_ebe : 0;
+}
+bool st_TrackJob_has_elem_by_elem_config(const st_TrackJob *j) { return j && j->has_ebe; }
+const st_ElemByElemConfig *st_TrackJob_get_elem_by_elem_config(const st_TrackJob *j)
+{
+    return (j && j->has_ebe) ? &j->ebe_cfg : nullptr;
+}
+bool st_TrackJob_is_elem_by_elem_config_rolling(const st_TrackJob *j)
+{
+    return j && j->has_ebe && j->ebe_cfg.is_rolling != 0;
+}
+bool st_TrackJob_get_default_elem_by_elem_config_rolling_flag(const st_TrackJob *j)
+{
+    return j && j->default_rolling;
+}
+void st_TrackJob_set_default_elem_by_elem_config_rolling_flag(st_TrackJob *j, bool r)
+{
+    if (j) j->default_rolling = r;
+}
+int64_t st_TrackJob_get_elem_by_elem_config_order(const st_TrackJob *j)
+{
+    return (j && j->has_ebe) ? j->ebe_cfg.order : -1;
+}
+bool st_TrackJob_has_beam_monitors(const st_TrackJob *j) { return j && !j->monitor_indices.empty(); }
+st_buffer_size_t st_TrackJob_get_num_beam_monitors(const st_TrackJob *j)
+{
+    return j ? j->monitor_indices.size() : 0;
+}
+const st_buffer_size_t *st_TrackJob_get_beam_monitor_indices_begin(const st_TrackJob *j)
+{
+    return (j && !j->monitor_indices.empty()) ? j->monitor_indices.data() : nullptr;
+}
+const st_buffer_size_t *st_TrackJob_get_beam_monitor_indices_end(const st_TrackJob *j)
+{
+    return (j && !j->monitor_indices.empty())
+               ? j->monitor_indices.data() + j->monitor_indices.size()
+               : nullptr;
+}
+st_buffer_size_t st_TrackJob_get_beam_monitor_index(const st_TrackJob *j, st_buffer_size_t n)
+{
+    return (j && n < j->monitor_indices.size()) ? j->monitor_indices[n] : (st_buffer_size_t)-1;
+}
+
+// ----------------------------------------------- TrackJobNew / CudaTrackJob
+st_CudaTrackJob *st_CudaTrackJob_create(void) { return make_job("cuda", nullptr); }
+st_CudaTrackJob *st_CudaTrackJob_new_from_config_str(const char *cfg) { return make_job("cuda", cfg); }
+st_CudaTrackJob *st_CudaTrackJob_new(const char *node_id, st_Buffer *pb, st_Buffer *eb)
+{
+    return st_CudaTrackJob_new_detailed(node_id, pb, 0, nullptr, eb, nullptr, 0, nullptr);
+}
+st_CudaTrackJob *st_CudaTrackJob_new_with_output(const char *node_id, st_Buffer *pb,
+                                                 st_Buffer *eb, st_Buffer *ob,
+                                                 st_buffer_size_t until_ebe)
+{
+    return st_CudaTrackJob_new_detailed(node_id, pb, 0, nullptr, eb, ob, until_ebe, nullptr);
+}
+st_CudaTrackJob *st_CudaTrackJob_new_detailed(const char *node_id, st_Buffer *pb,
+                                              st_buffer_size_t nsets,
+                                              const st_buffer_size_t *idx, st_Buffer *eb,
+                                              st_Buffer *ob, st_buffer_size_t until_ebe,
+                                              const char *cfg)
+{
+    // node id "platform.device" (cuda/track_job.h:42-66): the device index
+    // is the part after the dot.
+    std::string c = cfg ? cfg : "";
+    if (node_id && *node_id) {
+        std::string nid(node_id);
+        size_t const dot = nid.find('.');
+        std::string const dev = (dot == std::string::npos) ? nid : nid.substr(dot + 1);
+        if (!dev.empty() && std::all_of(dev.begin(), dev.end(), ::isdigit))
+            c += (c.empty() ? "" : "\n") + std::string("device=") + dev;
+    }
+    return st_TrackJob_new_detailed("cuda", pb, nsets, idx, eb, ob, until_ebe, c.c_str());
+}
+void st_TrackJobNew_delete(st_TrackJobBaseNew *j) { delete j; }
+st_track_status_t st_TrackJobNew_track_until(st_TrackJobBaseNew *j, st_buffer_size_t u)
+{
+    return st_TrackJob_track_until(j, u);
+}
+st_track_status_t st_TrackJobNew_track_elem_by_elem(st_TrackJobBaseNew *j, st_buffer_size_t u)
+{
+    return st_TrackJob_track_elem_by_elem(j, u);
+}
+st_track_status_t st_TrackJobNew_track_line(st_TrackJobBaseNew *j, st_buffer_size_t b,
+                                            st_buffer_size_t e, bool f)
+{
+    return st_TrackJob_track_line(j, b, e, f);
+}
+int32_t st_TrackJobNew_collect_particles(st_TrackJobBaseNew *j)
+{
+    return (j && download_particles(j)) ? 0 : -1;
+}
+int32_t st_TrackJobNew_collect_beam_elements(st_TrackJobBaseNew *j) { return j ? 0 : -1; }
+int32_t st_TrackJobNew_collect_output(st_TrackJobBaseNew *j)
+{
+    return (j && transfer_outputs(j, false)) ? 0 : -1;
+}
+int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *j)
+{
+    if (!j) return -1;
+    st_TrackJob_collect(j);
+    return 0;
+}
+int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *j)
+{
+    return (j && upload_particles(j)) ? 0 : -1;
+}
+int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *j)
+{
+    return (j && compile_job_lattice(j)) ? 0 : -1;
+}
+int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *j)
+{
+    return (j && transfer_outputs(j, true)) ? 0 : -1;
+}
+uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *j)
+{
+    return j ? (uint64_t)j->opt.threads : 0;
+}
+uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *j)
+{
+    return j ? (uint64_t)j->opt.threads : 0;
+}
+
+}  // extern "C"

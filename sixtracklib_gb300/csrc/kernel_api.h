@@ -1,0 +1,49 @@
+// kernel_api.h -- parameters shared between the host engine and the kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace stg {
+
+constexpr int kMaxThreads = 512;  // largest block the kernels are built for
+constexpr int kDefaultStages = 4;
+
+enum TrackMode : int32_t { MODE_UNTIL = 0, MODE_LINE = 1, MODE_EBE = 2 };
+
+enum ErrorBits : int32_t { ERR_PIPELINE_TIMEOUT = 1 };
+
+struct EbeDevConfig {
+    int64_t order;
+    int64_t num_particles_to_store, num_elements_to_store, num_turns_to_store;
+    int64_t min_particle_id, min_element_id, min_turn;
+    int64_t max_particle_id, max_element_id, max_turn;
+    int64_t is_rolling;
+};
+
+struct TrackParams {
+    const uint64_t *stream;  // device: n_chunks * chunk_words words
+    int32_t n_chunks;
+    int32_t chunk_words;
+    int32_t stages;
+    int32_t mode;
+    int64_t num_elements;    // elements in the compiled range
+    uint64_t *cols;          // device: 21 x n column block
+    int64_t n;
+    int64_t i0, i1;          // particle index range
+    int64_t until_turn;
+    int32_t finish_turn;
+    int32_t pad_;
+    uint64_t xlim_bits, ylim_bits;  // global aperture limits as IEEE bits
+    int32_t *status;         // device: OR of per-particle status
+    int32_t *error;          // device: ErrorBits
+    uint64_t *ebe_out;       // device: elem-by-elem column block
+    int64_t ebe_cap;
+    EbeDevConfig ebe;
+};
+
+// Launch one tracking kernel on `stream` (a cudaStream_t).  Returns the CUDA
+// error code of the launch (0 on success).
+int launch_track(const TrackParams &prm, bool fast, int threads, void *stream);
+size_t track_smem_bytes(int stages, int chunk_words);
+
+}  // namespace stg

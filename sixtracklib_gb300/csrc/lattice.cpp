@@ -1,0 +1,246 @@
+// lattice.cpp -- CObjects lattice -> device element stream.
+//
+// Per-element constants that the reference computes on every call are folded
+// here, with the reference's own operation order so results stay
+// bit-identical: the cavity's DEG2RAD*lag and (2*pi/c)*frequency
+// (be_cavity/track.h:46-55), the XYShift's negated offsets
+// (be_xyshift/track.h:45-46).  Slice arrays of BeamBeam6D, addressed by
+// relative offsets in the reference (be_beamfields.h:23-27), are laid out
+// contiguously after the fixed part.
+#include "lattice.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace stg {
+
+namespace {
+
+constexpr double kPi = 3.1415926535897932384626433832795028841971693993751;
+constexpr double kClight = 299792458.0;
+
+struct Emitter {
+    std::vector<uint64_t> recs;     // records, unchunked
+    std::vector<uint64_t> rec_len;  // per record
+    void push(uint32_t op, uint32_t aux, const std::vector<uint64_t> &params)
+    {
+        uint32_t const n = (uint32_t)params.size() + 1;
+        recs.push_back(make_header(op, n, aux));
+        recs.insert(recs.end(), params.begin(), params.end());
+        rec_len.push_back(n);
+    }
+};
+
+bool bad(std::string *err, uint64_t i, const char *what)
+{
+    if (err) *err = "element " + std::to_string(i) + ": " + what;
+    return false;
+}
+
+}  // namespace
+
+bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
+                     const CompileOptions &opt, CompiledStream *out, std::string *err)
+{
+    if (begin > end || end > img.num_objects) return bad(err, end, "line range outside the lattice");
+    Emitter em;
+    out->monitor_elements.clear();
+    uint32_t op_mask = 0;
+    for (uint64_t i = begin; i < end; ++i) {
+        uint64_t const t = img.type_of(i);
+        uint64_t const nw = img.size_bytes(i) / 8;
+        const uint64_t *w = img.words(i);
+        auto need = [&](uint64_t k) { return nw >= k; };
+        auto d = [&](uint64_t k) { return w[k]; };
+        std::vector<uint64_t> p;
+        uint32_t op = OP_FAIL_LOST, aux = 0;
+        switch (t) {
+        case ST_OBJECT_TYPE_DRIFT:
+        case ST_OBJECT_TYPE_DRIFT_EXACT: {
+            if (!need(1)) return bad(err, i, "truncated drift");
+            double const L = w2d(w[0]);
+            op = (t == ST_OBJECT_TYPE_DRIFT) ? OP_DRIFT : OP_DRIFT_EXACT;
+            bool const ap = opt.aperture_mode == 2 ||
+                            (opt.aperture_mode == 1 && L >= opt.aperture_min_length);
+            aux = ap ? DRIFT_APERTURE : 0u;
+            p = {d(0)};
+            break;
+        }
+        case ST_OBJECT_TYPE_MULTIPOLE: {
+            if (!need(5)) return bad(err, i, "truncated multipole");
+            int64_t const order = (int64_t)w[0];
+            if (order < 0 || order > 64) return bad(err, i, "multipole order out of range");
+            const uint64_t *bal = img.deref(i, 4);
+            if (!bal) return bad(err, i, "multipole bal pointer outside the buffer");
+            double const hxl = w2d(w[2]), hyl = w2d(w[3]);
+            bool const curv = (hxl > 0.0) || (hyl > 0.0) || (hxl < 0.0) || (hyl < 0.0);
+            op = curv ? OP_MULTIPOLE_CURV : OP_MULTIPOLE;
+            aux = (uint32_t)order;
+            p.assign(bal, bal + 2 * order + 2);
+            if (curv) {
+                p.push_back(w[2]);
+                p.push_back(w[3]);
+                p.push_back(w[1]);
+            }
+            break;
+        }
+        case ST_OBJECT_TYPE_CAVITY: {
+            if (!need(3)) return bad(err, i, "truncated cavity");
+            double const DEG2RAD = kPi / 180.0;
+            double const K_FACTOR = (2.0 * kPi) / kClight;
+            op = OP_CAVITY;
+            p = {w[0], d2w(K_FACTOR * w2d(w[1])), d2w(DEG2RAD * w2d(w[2]))};
+            break;
+        }
+        case ST_OBJECT_TYPE_XYSHIFT:
+            if (!need(2)) return bad(err, i, "truncated xyshift");
+            op = OP_XYSHIFT;
+            p = {d2w(-(w2d(w[0]))), d2w(-(w2d(w[1])))};
+            break;
+        case ST_OBJECT_TYPE_SROTATION:
+            if (!need(2)) return bad(err, i, "truncated srotation");
+            op = OP_SROTATION;
+            p = {w[0], w[1]};
+            break;
+        case ST_OBJECT_TYPE_LIMIT_RECT:
+            if (!need(4)) return bad(err, i, "truncated limit_rect");
+            op = OP_LIMIT_RECT;
+            p.assign(w, w + 4);
+            break;
+        case ST_OBJECT_TYPE_LIMIT_ELLIPSE:
+            if (!need(3)) return bad(err, i, "truncated limit_ellipse");
+            op = OP_LIMIT_ELLIPSE;
+            p.assign(w, w + 3);
+            break;
+        case ST_OBJECT_TYPE_LIMIT_RECT_ELLIPSE:
+            if (!need(5)) return bad(err, i, "truncated limit_rect_ellipse");
+            op = OP_LIMIT_RECT_ELLIPSE;
+            p.assign(w, w + 5);
+            break;
+        case ST_OBJECT_TYPE_DIPEDGE:
+            if (!need(2)) return bad(err, i, "truncated dipedge");
+            op = OP_DIPEDGE;
+            p.assign(w, w + 2);
+            break;
+        case ST_OBJECT_TYPE_RF_MULTIPOLE: {
+            if (!need(6)) return bad(err, i, "truncated rf multipole");
+            int64_t const order = (int64_t)w[0];
+            if (order < 0 || order > 64) return bad(err, i, "rf multipole order out of range");
+            const uint64_t *bal = img.deref(i, 4);
+            const uint64_t *ph = img.deref(i, 5);
+            if (!bal || !ph) return bad(err, i, "rf multipole pointer outside the buffer");
+            op = OP_RF_MULTIPOLE;
+            aux = (uint32_t)order;
+            p = {w[1], w[2], w[3]};
+            p.insert(p.end(), bal, bal + 2 * order + 2);
+            p.insert(p.end(), ph, ph + 2 * order + 2);
+            break;
+        }
+        case ST_OBJECT_TYPE_BEAM_BEAM_4D: {
+            if (!need(2)) return bad(err, i, "truncated beam-beam 4d");
+            const uint64_t *bd = img.deref(i, 1);
+            if (!bd || w[0] < 11) return bad(err, i, "beam-beam 4d data missing");
+            if (!(w2d(bd[10]) > 0.)) {
+                op = OP_NOP;
+            } else {
+                op = OP_BB4D;
+                p.assign(bd, bd + 11);
+            }
+            break;
+        }
+        case ST_OBJECT_TYPE_BEAM_BEAM_6D: {
+            if (!need(2)) return bad(err, i, "truncated beam-beam 6d");
+            const uint64_t *bd = img.deref(i, 1);
+            if (!bd || w[0] < 38) return bad(err, i, "beam-beam 6d data missing");
+            if (!(w2d(bd[33]) > 0.)) {
+                op = OP_NOP;
+                break;
+            }
+            int64_t const ns = (int64_t)(int)(int64_t)bd[18];
+            if (ns < 0 || ns > 100000) return bad(err, i, "beam-beam 6d slice count out of range");
+            op = OP_BB6D;
+            aux = (uint32_t)ns;
+            p.assign(bd, bd + 34);
+            for (int f = 34; f < 38; ++f) {
+                uint64_t const off = (uint64_t)f + bd[f] + 1;
+                if (off + (uint64_t)ns > w[0]) return bad(err, i, "beam-beam 6d slice array outside data");
+                p.insert(p.end(), bd + off, bd + off + ns);
+            }
+            break;
+        }
+        case ST_OBJECT_TYPE_SC_COASTING:
+            if (!need(9)) return bad(err, i, "truncated space-charge coasting");
+            op = OP_SC_COASTING;
+            p.assign(w, w + 9);
+            break;
+        case ST_OBJECT_TYPE_SC_QGAUSSIAN_PROF:
+            if (!need(11)) return bad(err, i, "truncated space-charge q-gaussian");
+            op = OP_SC_QGAUSS;
+            p.assign(w, w + 11);
+            break;
+        case ST_OBJECT_TYPE_BEAM_MONITOR: {
+            if (!need(8)) return bad(err, i, "truncated beam monitor");
+            op = OP_MONITOR;
+            uint64_t optr = 0;
+            int64_t ocap = 0;
+            if (opt.monitor_output) {
+                auto o = opt.monitor_output(i);
+                optr = o.first;
+                ocap = o.second;
+            }
+            if ((int64_t)w[2] <= 0 || (int64_t)w[0] <= 0) optr = 0;  // skip/num_stores must be > 0
+            p = {w[0], w[1], w[2], w[4], w[5], w[6], w[7], optr, (uint64_t)ocap};
+            out->monitor_elements.push_back(i);
+            break;
+        }
+        case ST_OBJECT_TYPE_TRICUB:
+        case ST_OBJECT_TYPE_TRICUB_DATA:
+            // TriCub is compiled "disabled" in the reference's default build
+            // (Settings.cmake.default): tracking returns failure.
+            op = OP_FAIL;
+            break;
+        default:
+            op = OP_FAIL_LOST;
+            break;
+        }
+        op_mask |= 1u << op;
+        em.push(op, aux, p);
+    }
+    // chunking
+    uint64_t maxrec = 1;
+    for (uint64_t n : em.rec_len) maxrec = std::max<uint64_t>(maxrec, n);
+    uint64_t cw = (uint64_t)std::max<int32_t>(opt.min_chunk_words, 64);
+    while (cw < maxrec + 1) cw *= 2;
+    cw = (cw + 1) & ~(uint64_t)1;
+    out->words.clear();
+    out->words.reserve(em.recs.size() + em.rec_len.size() + cw);
+    uint64_t used = 0, pos = 0;
+    int32_t nchunks = 0;
+    auto close_chunk = [&]() {
+        out->words.push_back(make_header(OP_END, 1, 0));
+        ++used;
+        while (used < cw) {
+            out->words.push_back(0);
+            ++used;
+        }
+        ++nchunks;
+        used = 0;
+    };
+    for (uint64_t r = 0; r < em.rec_len.size(); ++r) {
+        uint64_t const n = em.rec_len[r];
+        if (used + n + 1 > cw) close_chunk();
+        out->words.insert(out->words.end(), em.recs.begin() + pos, em.recs.begin() + pos + n);
+        used += n;
+        pos += n;
+    }
+    if (used > 0 || nchunks == 0) close_chunk();
+    out->info.num_elements = (int64_t)(end - begin);
+    out->info.num_chunks = nchunks;
+    out->info.chunk_words = (int32_t)cw;
+    out->info.max_record_words = (int32_t)maxrec;
+    out->info.num_monitors = (int32_t)out->monitor_elements.size();
+    out->info.op_mask = op_mask;
+    return true;
+}
+
+}  // namespace stg

@@ -1,0 +1,36 @@
+// lattice.h -- compile a CObjects lattice into the device element stream.
+#pragma once
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "stream.h"
+
+namespace stg {
+
+struct CompileOptions {
+    // Global aperture after Drift/DriftExact (SIXTRL_APERTURE_CHECK_AT_DRIFT):
+    // 2 always (reference default), 1 if length >= min_length, 0 never.
+    int aperture_mode = 2;
+    double aperture_min_length = 0.0;
+    int32_t min_chunk_words = 1024;
+    // Output slot for the k-th BeamMonitor of the compiled range (element
+    // index given): returns {device pointer to a column block, capacity};
+    // {0, 0} disables storing for that monitor.
+    std::function<std::pair<uint64_t, int64_t>(uint64_t elem_index)> monitor_output;
+};
+
+struct CompiledStream {
+    std::vector<uint64_t> words;  // num_chunks * chunk_words
+    StreamInfo info;
+    std::vector<uint64_t> monitor_elements;  // element indices of monitors
+};
+
+// Compile elements [begin, end) of the image.  Returns false (and sets the
+// error text) on malformed elements.
+bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
+                     const CompileOptions &opt, CompiledStream *out, std::string *err);
+
+}  // namespace stg

@@ -1,0 +1,651 @@
+// maps.cuh -- element maps on the GPU, FP64, one particle per thread.
+//
+// Each map restates the reference map named in its comment.  The template
+// flag FAST selects the arithmetic policy:
+//   FAST = false: every operation rounded separately, in the reference's
+//                 order (the translation unit is compiled with -fmad=false),
+//                 so results are bit-identical to the reference's CPU build
+//                 except where a CUDA math function (sin, exp, pow) differs
+//                 from the host libm in the last bit;
+//   FAST = true:  fused multiply-adds where they shorten a dependency chain
+//                 (Horner kicks, drift updates, rotations); results agree
+//                 with the reference to rounding level.
+#pragma once
+
+#include <cstdint>
+
+#include "stream.h"
+
+namespace stg {
+
+struct PState {
+    double x, px, y, py, zeta, delta, psigma, rpp, rvv, chi, s;
+    double beta0, q0, p0c, mass0, charge_ratio, gamma0, energy0;
+    int64_t pid, at_element, at_turn, state;
+};
+
+__device__ __forceinline__ double W(uint64_t w) { return __longlong_as_double((long long)w); }
+
+constexpr double kPiD = 3.1415926535897932384626433832795028841971693993751;
+constexpr double kClightD = 299792458.0;
+constexpr double kEps0D = 8.854187817620e-12;
+constexpr double kSqrtPiD = 1.7724538509055160272981674833411451827975494561224;
+constexpr double kQelemD = 1.60217662e-19;
+constexpr double kCharge0SiD = 1.602176634e-19;
+
+// ------------------------------------------------------------------ energy
+// NS(Particles_add_to_energy_value): particles.h:5255-5297
+__device__ __forceinline__ void add_energy(PState &p, double de)
+{
+    double const beta0 = p.beta0;
+    double const db0 = p.delta * beta0;
+    double const ptau_beta0 = de / p.energy0 + sqrt(db0 * db0 + 2.0 * db0 * beta0 + 1.0) - 1.0;
+    double const ptau = ptau_beta0 / beta0;
+    double const psigma = ptau / beta0;
+    double const delta = sqrt(ptau * ptau + 2.0 * psigma + 1.0) - 1.0;
+    double const opd = delta + 1.0;
+    double const rvv = opd / (1.0 + ptau_beta0);
+    p.delta = delta;
+    p.psigma = psigma;
+    p.zeta *= rvv / p.rvv;
+    p.rvv = rvv;
+    p.rpp = 1.0 / opd;
+}
+
+// NS(Particles_update_delta_value): particles.h:5459-5496
+__device__ __forceinline__ void set_delta(PState &p, double nd)
+{
+    double const beta0 = p.beta0;
+    double const db0 = nd * beta0;
+    double const ptau_beta0 = sqrt(db0 * db0 + 2.0 * db0 * beta0 + 1.0) - 1.0;
+    double const opd = 1.0 + nd;
+    p.delta = nd;
+    p.rvv = opd / (1.0 + ptau_beta0);
+    p.rpp = 1.0 / opd;
+    p.psigma = ptau_beta0 / (beta0 * beta0);
+}
+
+// ------------------------------------------------------------------- maps
+// be_drift/track.h:45-67
+template <bool FAST>
+__device__ __forceinline__ void drift(PState &p, double L)
+{
+    double const xp = p.px * p.rpp;
+    double const yp = p.py * p.rpp;
+    if (FAST) {
+        double const t = fma(yp, yp, xp * xp);
+        double const u = fma(t, 0.5, 1.0);
+        p.x = fma(xp, L, p.x);
+        p.y = fma(yp, L, p.y);
+        p.s += L;
+        p.zeta = fma(L, p.rvv - u, p.zeta);
+    } else {
+        double const dzeta = p.rvv - (1.0 + (xp * xp + yp * yp) * 0.5);
+        p.x += xp * L;
+        p.y += yp * L;
+        p.s += L;
+        p.zeta += L * dzeta;
+    }
+}
+
+// be_drift/track.h:71-97
+__device__ __forceinline__ void drift_exact(PState &p, double L)
+{
+    double const opd = p.delta + 1.0;
+    double const lpzi = L / sqrt(opd * opd - (p.px * p.px + p.py * p.py));
+    double const dzeta = p.rvv * L - opd * lpzi;
+    p.x += p.px * lpzi;
+    p.y += p.py * lpzi;
+    p.s += L;
+    p.zeta += dzeta;
+}
+
+// Global aperture (be_limit/track.h:54-88) on the integer pipe:
+// |x| < limit  <=>  bits(|x|) < bits(limit), NaN and inf fail as in the
+// reference's float compare.
+__device__ __forceinline__ bool inside_global(const PState &p, uint64_t xlim, uint64_t ylim)
+{
+    uint64_t const ax = (uint64_t)__double_as_longlong(p.x) & 0x7FFFFFFFFFFFFFFFull;
+    uint64_t const ay = (uint64_t)__double_as_longlong(p.y) & 0x7FFFFFFFFFFFFFFFull;
+    return (ax < xlim) & (ay < ylim);
+}
+
+// be_multipole/track.h:38-112 (bal[2k] = knl[k]/k!, bal[2k+1] = ksl[k]/k!)
+template <bool FAST, bool CURV>
+__device__ __forceinline__ void multipole(PState &p, const uint64_t *rec, int order)
+{
+    const uint64_t *bal = rec + 1;
+    double dpx = W(bal[2 * order]);
+    double dpy = W(bal[2 * order + 1]);
+    double const x = p.x, y = p.y, chi = p.chi;
+    for (int k = order - 1; k >= 0; --k) {
+        if (FAST) {
+            double const tx = fma(-dpy, y, W(bal[2 * k]));
+            double const ty = fma(dpy, x, W(bal[2 * k + 1]));
+            double const nx = fma(dpx, x, tx);
+            dpy = fma(dpx, y, ty);
+            dpx = nx;
+        } else {
+            double const zre = dpx * x - dpy * y;
+            double const zim = dpx * y + dpy * x;
+            dpx = W(bal[2 * k]) + zre;
+            dpy = W(bal[2 * k + 1]) + zim;
+        }
+    }
+    if (!CURV) {
+        if (FAST) {
+            p.px = fma(-chi, dpx, p.px);
+            p.py = fma(chi, dpy, p.py);
+        } else {
+            p.px += -chi * dpx;
+            p.py += chi * dpy;
+        }
+        return;
+    }
+    dpx = -chi * dpx;
+    dpy = chi * dpy;
+    double const hxl = W(bal[2 * order + 2]);
+    double const hyl = W(bal[2 * order + 3]);
+    double const length = W(bal[2 * order + 4]);
+    double const hxlx = x * hxl;
+    double const hyly = y * hyl;
+    p.zeta += chi * (hyly - hxlx);
+    dpx += hxl + hxl * p.delta;
+    dpy -= hyl + hyl * p.delta;
+    if (length > 0.0) {
+        double const b1l = chi * W(bal[0]);
+        double const a1l = chi * W(bal[1]);
+        dpx -= b1l * hxlx / length;
+        dpy += a1l * hyly / length;
+    }
+    p.px += dpx;
+    p.py += dpy;
+}
+
+// be_cavity/track.h:39-67 (rec: voltage, (2 pi / c) * frequency, deg2rad * lag)
+__device__ __forceinline__ void cavity(PState &p, const uint64_t *rec)
+{
+    double const q = p.q0 * p.charge_ratio;
+    double const tau = p.zeta / (p.beta0 * p.rvv);
+    double const phase = W(rec[3]) - W(rec[2]) * tau;
+    double const energy = q * W(rec[1]) * sin(phase);
+    add_energy(p, energy);
+}
+
+// be_srotation/track.h:38-69
+template <bool FAST>
+__device__ __forceinline__ void srotation(PState &p, const uint64_t *rec)
+{
+    double const cz = W(rec[1]), sz = W(rec[2]);
+    double const x = p.x, y = p.y, px = p.px, py = p.py;
+    if (FAST) {
+        p.x = fma(cz, x, sz * y);
+        p.y = fma(-sz, x, cz * y);
+        p.px = fma(cz, px, sz * py);
+        p.py = fma(-sz, px, cz * py);
+    } else {
+        p.x = cz * x + sz * y;
+        p.y = -sz * x + cz * y;
+        p.px = cz * px + sz * py;
+        p.py = -sz * px + cz * py;
+    }
+}
+
+// be_limit/track.h:90-111
+__device__ __forceinline__ bool inside_rect(const PState &p, const uint64_t *rec)
+{
+    return (p.x >= W(rec[1])) && (p.x <= W(rec[2])) && (p.y >= W(rec[3])) && (p.y <= W(rec[4]));
+}
+
+// be_limit/track.h:113-137
+__device__ __forceinline__ bool inside_ellipse(const PState &p, const uint64_t *rec)
+{
+    double t = p.x * p.x;
+    t *= W(rec[2]);
+    double ys = p.y * p.y;
+    ys *= W(rec[1]);
+    t += ys;
+    return t <= W(rec[3]);
+}
+
+// be_limit/track.h:139-162
+__device__ __forceinline__ bool inside_rect_ellipse(const PState &p, const uint64_t *rec)
+{
+    double const x = p.x, y = p.y;
+    double t = x * x * W(rec[4]);
+    t += y * y * W(rec[3]);
+    return (x <= W(rec[1])) && (x >= -W(rec[1])) && (y <= W(rec[2])) && (y >= -W(rec[2])) &&
+           (t <= W(rec[5]));
+}
+
+// be_rfmultipole/track.h:39-118
+__device__ __noinline__ void rf_multipole(PState &p, const uint64_t *rec, int order)
+{
+    double const voltage = W(rec[1]), frequency = W(rec[2]), lag = W(rec[3]);
+    const uint64_t *bal = rec + 4;
+    const uint64_t *phase = rec + 4 + 2 * order + 2;
+    double const DEG2RAD = kPiD / 180.0;
+    double const DEG2RAD_C = 0.0174532925199432957692369076848861271344287188854172546;
+    double const k = frequency * (2.0 * kPiD) / kClightD;
+    double const x = p.x, y = p.y;
+    double const q = p.q0 * p.charge_ratio * 1.0;
+    double const ktau = k * p.zeta / (p.beta0 * p.rvv);
+    double dpx = 0.0, dpy = 0.0, dptr = 0.0, zre = 1.0, zim = 0.0;
+    for (int kk = 0; kk <= order; ++kk) {
+        double const pn = DEG2RAD_C * W(phase[2 * kk]) - ktau;
+        double const ps = DEG2RAD * W(phase[2 * kk + 1]) - ktau;
+        double const bn = W(bal[2 * kk]);
+        double const bs = W(bal[2 * kk + 1]);
+        double const cn = cos(pn), cs = cos(ps), sn = sin(pn), ss = sin(ps);
+        dpx += cn * (bn * zre) - cs * (bs * zim);
+        dpy += cs * (bs * zre) + cn * (bn * zim);
+        double const zret = zre * x - zim * y;
+        zim = zim * x + zre * y;
+        zre = zret;
+        dptr += sn * (bn * zre) - ss * (bs * zim);
+    }
+    double const cav_energy = q * (voltage * sin(lag * DEG2RAD_C - ktau));
+    double const rfm_energy = -q * ((k * p.p0c) * dptr);
+    double const chi = p.chi;
+    p.px += -chi * dpx;
+    p.py += chi * dpy;
+    add_energy(p, cav_energy + rfm_energy);
+}
+
+// ----------------------------------------------------- Gaussian beam fields
+// Complex error function w(z): the CERN algorithm of K. Koelbig (program
+// C335), as used by be_beamfields/faddeeva_cern.h:45-120.  The backward
+// recursion and the series are fused into one loop (the series consumes
+// R[n-1] as soon as the recursion yields it), so no arrays are needed.
+__device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
+{
+    double const a_const = 1.12837916709551;
+    double const xlim = 5.33, ylim = 4.29;
+    double const x = fabs(in_re), y = fabs(in_im);
+    double wx, wy;
+    if (y < ylim && x < xlim) {
+        double const q = (1.0 - y / ylim) * sqrt(1.0 - (x / xlim) * (x / xlim));
+        double const h = 1.0 / (3.2 * q);
+        int const nc = 7 + (int)(23.0 * q);
+        double xl = pow(h, (double)(1 - nc));
+        double const xh = y + 0.5 / h;
+        double const yh = x;
+        int const nu = 10 + (int)(21.0 * q);
+        double rx = 0.0, ry = 0.0, sx = 0.0, sy = 0.0;
+        for (int n = nu; n > 0; n--) {
+            double const tx = xh + n * rx;
+            double const ty = yh - n * ry;
+            double const tn = tx * tx + ty * ty;
+            rx = 0.5 * tx / tn;
+            ry = 0.5 * ty / tn;
+            if (n <= nc) {
+                double const saux = sx + xl;
+                sx = rx * saux - ry * sy;
+                sy = rx * sy + ry * saux;
+                xl = h * xl;
+            }
+        }
+        wx = a_const * sx;
+        wy = a_const * sy;
+    } else {
+        double const xh = y, yh = x;
+        double rx = 0.0, ry = 0.0;
+        for (int n = 9; n > 0; n--) {
+            double const tx = xh + n * rx;
+            double const ty = yh - n * ry;
+            double const tn = tx * tx + ty * ty;
+            rx = 0.5 * tx / tn;
+            ry = 0.5 * ty / tn;
+        }
+        wx = a_const * rx;
+        wy = a_const * ry;
+    }
+    if (y == 0.) wx = exp(-x * x);
+    if (in_im < 0.) {
+        wx = 2.0 * exp(y * y - x * x) * cos(2.0 * x * y) - wx;
+        wy = -2.0 * exp(y * y - x * x) * sin(2.0 * x * y) - wy;
+        if (in_re > 0.) wy = -wy;
+    } else if (in_re < 0.) {
+        wy = -wy;
+    }
+    *w_re = wx;
+    *w_im = wy;
+}
+
+// gauss_fields.h:56-208 (NS(get_Ex_Ey_Gx_Gy_gauss), centred: Delta = 0)
+__device__ __noinline__ void fields_gauss(double x, double y, double sigma_x, double sigma_y,
+                                          double min_sigma_diff, int skip_gs, double *ex_p,
+                                          double *ey_p, double *gx_p, double *gy_p)
+{
+    double ex, ey, gx = 0., gy = 0.;
+    if (fabs(sigma_x - sigma_y) < min_sigma_diff) {
+        double const sigma = 0.5 * (sigma_x + sigma_y);
+        double const r2 = x * x + y * y;
+        double t;
+        if (r2 < 1e-20)
+            t = sqrt(r2) / (2. * kPiD * kEps0D * sigma);
+        else
+            t = (1 - exp(-0.5 * r2 / (sigma * sigma))) / (2. * kPiD * kEps0D * r2);
+        ex = t * x;
+        ey = t * y;
+        if (!skip_gs) {
+            gx = 1 / (2. * (x * x + y * y)) *
+                 (y * ey - x * ex +
+                  1. / (2 * kPiD * kEps0D * sigma * sigma) * x * x *
+                      exp(-(x * x + y * y) / (2. * sigma * sigma)));
+            gy = 1. / (2 * (x * x + y * y)) *
+                 (x * ex - y * ey +
+                  1. / (2 * kPiD * kEps0D * sigma * sigma) * y * y *
+                      exp(-(x * x + y * y) / (2. * sigma * sigma)));
+        }
+    } else {
+        double const abx = fabs(x), aby = fabs(y);
+        double S, fact, wz_re, wz_im, we_re, we_im, e;
+        if (sigma_x > sigma_y) {
+            S = sqrt(2. * (sigma_x * sigma_x - sigma_y * sigma_y));
+            fact = 1. / (2. * kEps0D * kSqrtPiD * S);
+            double const eta_re = sigma_y / sigma_x * abx;
+            double const eta_im = sigma_x / sigma_y * aby;
+            cerrf(abx / S, aby / S, &wz_re, &wz_im);
+            cerrf(eta_re / S, eta_im / S, &we_re, &we_im);
+            e = exp(-abx * abx / (2 * sigma_x * sigma_x) - aby * aby / (2 * sigma_y * sigma_y));
+            ex = fact * (wz_im - we_im * e);
+            ey = fact * (wz_re - we_re * e);
+        } else if (sigma_x < sigma_y) {
+            S = sqrt(2. * (sigma_y * sigma_y - sigma_x * sigma_x));
+            fact = 1. / (2. * kEps0D * kSqrtPiD * S);
+            double const eta_re = sigma_x / sigma_y * aby;
+            double const eta_im = sigma_y / sigma_x * abx;
+            cerrf(aby / S, abx / S, &wz_re, &wz_im);
+            cerrf(eta_re / S, eta_im / S, &we_re, &we_im);
+            e = exp(-aby * aby / (2 * sigma_y * sigma_y) - abx * abx / (2 * sigma_x * sigma_x));
+            ey = fact * (wz_im - we_im * e);
+            ex = fact * (wz_re - we_re * e);
+        } else {
+            ex = ey = __longlong_as_double(0x7FF0000000000000ll);  // 1/0
+        }
+        if (x < 0) ex = -ex;
+        if (y < 0) ey = -ey;
+        if (!skip_gs) {
+            double const s11 = sigma_x * sigma_x, s33 = sigma_y * sigma_y;
+            gx = -1. / (2 * (s11 - s33)) *
+                 (x * ex + y * ey +
+                  1. / (2 * kPiD * kEps0D) *
+                      (sigma_y / sigma_x * exp(-x * x / (2 * s11) - y * y / (2 * s33)) - 1.));
+            gy = 1. / (2 * (s11 - s33)) *
+                 (x * ex + y * ey +
+                  1. / (2 * kPiD * kEps0D) *
+                      (sigma_x / sigma_y * exp(-x * x / (2 * s11) - y * y / (2 * s33)) - 1.));
+        }
+    }
+    *ex_p = ex;
+    *ey_p = ey;
+    if (!skip_gs) {
+        *gx_p = gx;
+        *gy_p = gy;
+    }
+}
+
+// be_beamfields/track.h:89-149
+__device__ __noinline__ void beam_beam_4d(PState &p, const uint64_t *rec)
+{
+    const uint64_t *d = rec + 1;
+    double const charge = 1. * p.q0 * kQelemD;
+    double const x = p.x - W(d[6]);
+    double const y = p.y - W(d[7]);
+    double const beta = p.beta0 / p.rvv;
+    double const p0c = p.p0c * kQelemD;
+    double ex, ey, gx, gy;
+    fields_gauss(x, y, W(d[2]), W(d[3]), W(d[5]), 1, &ex, &ey, &gx, &gy);
+    double const fk = p.chi * W(d[1]) * W(d[0]) * charge * (1. + beta * W(d[4])) /
+                      (p0c * (beta + W(d[4])));
+    p.px += (fk * ex - W(d[8]));
+    p.py += (fk * ey - W(d[9]));
+}
+
+__device__ __forceinline__ double sgn(double a) { return (double)((a >= 0) - (a < 0)); }
+
+// be_beamfields/be_beamfields.h:2232-2385 (NS(BeamBeam6D_propagate_Sigma_matrix))
+__device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr, double *out)
+{
+    double const S11_0 = W(sg[0]), S12_0 = W(sg[1]), S13_0 = W(sg[2]), S14_0 = W(sg[3]),
+                 S22_0 = W(sg[4]), S23_0 = W(sg[5]), S24_0 = W(sg[6]), S33_0 = W(sg[7]),
+                 S34_0 = W(sg[8]), S44_0 = W(sg[9]);
+    double const S11 = S11_0 + 2. * S12_0 * S + S22_0 * S * S;
+    double const S33 = S33_0 + 2. * S34_0 * S + S44_0 * S * S;
+    double const S13 = S13_0 + (S14_0 + S23_0) * S + S24_0 * S * S;
+    double const S12 = S12_0 + S22_0 * S;
+    double const S14 = S14_0 + S24_0 * S;
+    double const S22 = S22_0 + 0. * S;
+    double const S23 = S23_0 + S24_0 * S;
+    double const S24 = S24_0 + 0. * S;
+    double const S34 = S34_0 + S44_0 * S;
+    double const S44 = S44_0 + 0. * S;
+    double const R = S11 - S33;
+    double const Wv = S11 + S33;
+    double const T = R * R + 4 * S13 * S13;
+    double const dS_R = 2. * (S12_0 - S34_0) + 2 * S * (S22_0 - S44_0);
+    double const dS_W = 2. * (S12_0 + S34_0) + 2 * S * (S22_0 + S44_0);
+    double const dS_S13 = S14_0 + S23_0 + 2 * S24_0 * S;
+    double const dS_T = 2 * R * dS_R + 8. * S13 * dS_S13;
+    double s11h, s33h, ct, st, ds11h, ds33h, dct, dst, c2t, dc2t;
+    double const signR = sgn(R);
+    if (T < thr) {
+        double const a = S12 - S34;
+        double const b = S22 - S44;
+        double const c = S14 + S23;
+        double const dd = S24;
+        double sq = sqrt(a * a + c * c);
+        if (sq * sq * sq < thr) {
+            c2t = (fabs(dd) > thr) ? fabs(b) / sqrt(b * b + 4 * dd * dd) : 1.;
+            ct = sqrt(0.5 * (1. + c2t));
+            st = sgn(b) * sgn(dd) * sqrt(0.5 * (1. - c2t));
+            dct = 0.;
+            dst = 0.;
+            s11h = 0.5 * Wv;
+            s33h = 0.5 * Wv;
+            ds11h = 0.5 * dS_W;
+            ds33h = 0.5 * dS_W;
+        } else {
+            sq = sqrt(a * a + c * c);
+            c2t = fabs(2. * a) / (2 * sq);
+            ct = sqrt(0.5 * (1. + c2t));
+            st = sgn(a) * sgn(c) * sqrt(0.5 * (1. - c2t));
+            dc2t = sgn(a) * (0.5 * b / sq - a * (a * b + 2. * c * dd) / (2. * sq * sq * sq));
+            dct = 1. / (4. * ct) * dc2t;
+            if (fabs(st) > thr)
+                dst = -1. / (4. * st) * dc2t;
+            else
+                dst = dd / (2. * a);
+            s11h = 0.5 * Wv;
+            s33h = 0.5 * Wv;
+            ds11h = 0.5 * dS_W + sgn(a) * sq;
+            ds33h = 0.5 * dS_W - sgn(a) * sq;
+        }
+    } else {
+        double const sqrtT = sqrt(T);
+        c2t = signR * R / sqrtT;
+        ct = sqrt(0.5 * (1. + c2t));
+        st = signR * sgn(S13) * sqrt(0.5 * (1. - c2t));
+        s11h = 0.5 * (Wv + signR * sqrtT);
+        s33h = 0.5 * (Wv - signR * sqrtT);
+        dc2t = signR * (dS_R / sqrtT - R / (2 * sqrtT * sqrtT * sqrtT) * dS_T);
+        dct = 1. / (4. * ct) * dc2t;
+        if (fabs(st) < thr)
+            dst = (S14 + S23) / R;
+        else
+            dst = -1. / (4. * st) * dc2t;
+        ds11h = 0.5 * (dS_W + signR * 0.5 / sqrtT * dS_T);
+        ds33h = 0.5 * (dS_W - signR * 0.5 / sqrtT * dS_T);
+    }
+    out[0] = s11h;
+    out[1] = s33h;
+    out[2] = ct;
+    out[3] = st;
+    out[4] = ds11h;
+    out[5] = ds33h;
+    out[6] = dct;
+    out[7] = dst;
+}
+
+// be_beamfields/track.h:342-507 with NS(BeamBeam6D_boost / inv_boost)
+// (be_beamfields.h:2101-2230); rec = [hdr, 34 head words, slices...]
+__device__ __noinline__ void beam_beam_6d(PState &p, const uint64_t *rec, int n_slices)
+{
+    const uint64_t *d = rec + 1;
+    const uint64_t *np_ = d + 34;
+    const uint64_t *xs_ = np_ + n_slices;
+    const uint64_t *ys_ = xs_ + n_slices;
+    const uint64_t *ss_ = ys_ + n_slices;
+    double const sphi = W(d[1]), cphi = W(d[2]), tphi = W(d[3]), salpha = W(d[4]),
+                 calpha = W(d[5]);
+    double const q0 = kQelemD * p.q0;
+    double const P0 = p.p0c / kClightD * kQelemD;
+    double x = p.x - W(d[21]) - W(d[19]);
+    double px = p.px - W(d[22]);
+    double y = p.y - W(d[23]) - W(d[20]);
+    double py = p.py - W(d[24]);
+    double sg = p.zeta - W(d[25]);
+    double dl = p.delta - W(d[26]);
+    {  // boost
+        double const h = dl + 1. - sqrt((1. + dl) * (1. + dl) - px * px - py * py);
+        double const px_st = px / cphi - h * calpha * tphi / cphi;
+        double const py_st = py / cphi - h * salpha * tphi / cphi;
+        double const dl_st = dl - px * calpha * tphi - py * salpha * tphi + h * tphi * tphi;
+        double const pz_st = sqrt((1. + dl_st) * (1. + dl_st) - px_st * px_st - py_st * py_st);
+        double const hx = px_st / pz_st;
+        double const hy = py_st / pz_st;
+        double const hs = 1. - (dl_st + 1) / pz_st;
+        double const L11 = 1. + hx * calpha * sphi;
+        double const L12 = hx * salpha * sphi;
+        double const L13 = calpha * tphi;
+        double const L21 = hy * calpha * sphi;
+        double const L22 = 1. + hy * salpha * sphi;
+        double const L23 = salpha * tphi;
+        double const L31 = hs * calpha * sphi;
+        double const L32 = hs * salpha * sphi;
+        double const L33 = 1. / cphi;
+        double const nx = L11 * x + L12 * y + L13 * sg;
+        double const ny = L21 * x + L22 * y + L23 * sg;
+        double const ns = L31 * x + L32 * y + L33 * sg;
+        x = nx;
+        y = ny;
+        sg = ns;
+        px = px_st;
+        py = py_st;
+        dl = dl_st;
+    }
+    double const thr = W(d[17]);
+    double const msd = W(d[16]);
+    for (int i = 0; i < n_slices; ++i) {
+        double const Ksl = W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
+        double const S = 0.5 * (sg - W(ss_[i]));
+        double sm[8];
+        bb6d_sigma(d + 6, S, thr, sm);
+        double const ct = sm[2], st = sm[3];
+        double const xb = x + px * S - W(xs_[i]);
+        double const yb = y + py * S - W(ys_[i]);
+        double const xbh = xb * ct + yb * st;
+        double const ybh = -xb * st + yb * ct;
+        double const dxbh = xb * sm[6] + yb * sm[7];
+        double const dybh = -xb * sm[7] + yb * sm[6];
+        double ex, ey, gx = 0.0, gy = 0.0;
+        fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
+        double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
+        double const Fx = Fxh * ct - Fyh * st;
+        double const Fy = Fxh * st + Fyh * ct;
+        double const Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * sm[4] + Gyh * sm[5]);
+        dl = dl + Fz + 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy));
+        x = x - S * Fx;
+        px = px + Fx;
+        y = y - S * Fy;
+        py = py + Fy;
+    }
+    {  // inverse boost
+        double const pz = sqrt((1. + dl) * (1. + dl) - px * px - py * py);
+        double const hx = px / pz;
+        double const hy = py / pz;
+        double const hs = 1. - (dl + 1) / pz;
+        double const Det = 1. / cphi + (hx * calpha + hy * salpha - hs * sphi) * tphi;
+        double const Li11 = (1. / cphi + salpha * tphi * (hy - hs * salpha * sphi)) / Det;
+        double const Li12 = (salpha * tphi * (hs * calpha * sphi - hx)) / Det;
+        double const Li13 =
+            -tphi * (calpha - hx * salpha * salpha * sphi + hy * calpha * salpha * sphi) / Det;
+        double const Li21 = (calpha * tphi * (-hy + hs * salpha * sphi)) / Det;
+        double const Li22 = (1. / cphi + calpha * tphi * (hx - hs * calpha * sphi)) / Det;
+        double const Li23 =
+            -tphi * (salpha - hy * calpha * calpha * sphi + hx * calpha * salpha * sphi) / Det;
+        double const Li31 = -hs * calpha * sphi / Det;
+        double const Li32 = -hs * salpha * sphi / Det;
+        double const Li33 = (1. + hx * calpha * sphi + hy * salpha * sphi) / Det;
+        double const xi = Li11 * x + Li12 * y + Li13 * sg;
+        double const yi = Li21 * x + Li22 * y + Li23 * sg;
+        double const si = Li31 * x + Li32 * y + Li33 * sg;
+        double const h = (dl + 1. - pz) * cphi * cphi;
+        double const pxi = px * cphi + h * calpha * tphi;
+        double const pyi = py * cphi + h * salpha * tphi;
+        double const dli = dl + pxi * calpha * tphi + pyi * salpha * tphi - h * tphi * tphi;
+        x = xi;
+        y = yi;
+        sg = si;
+        px = pxi;
+        py = pyi;
+        dl = dli;
+    }
+    p.x = x + W(d[21]) + W(d[19]) - W(d[27]);
+    p.px = px + W(d[22]) - W(d[28]);
+    p.y = y + W(d[23]) + W(d[20]) - W(d[29]);
+    p.py = py + W(d[24]) - W(d[30]);
+    p.zeta = sg + W(d[25]) - W(d[31]);
+    set_delta(p, dl + W(d[26]) - W(d[32]));
+}
+
+// be_beamfields/track.h:154-198
+__device__ __noinline__ void sc_coasting(PState &p, const uint64_t *rec)
+{
+    const uint64_t *c = rec + 1;
+    double const charge = kCharge0SiD * p.q0;
+    double const beta0 = p.beta0;
+    double const pc0 = p.p0c * kCharge0SiD;
+    double fk = W(c[0]) * W(c[4]) * p.chi * p.charge_ratio * charge * charge *
+                (1.0 - beta0 * beta0);
+    fk /= W(c[1]) * pc0 * beta0 * p.rvv;
+    double ex, ey, gx, gy;
+    fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);
+    p.px += fk * ex;
+    p.py += fk * ey;
+}
+
+// be_beamfields/track.h:203-268 with NS(Math_q_gauss) (internal/math_qgauss.h:114-175)
+__device__ __noinline__ void sc_qgauss(PState &p, const uint64_t *rec)
+{
+    const uint64_t *c = rec + 1;
+    double const charge = kCharge0SiD * p.q0;
+    double const beta0 = p.beta0;
+    double const beta = beta0 * p.rvv;
+    double const pc0 = p.p0c * kCharge0SiD;
+    double const z = p.zeta / p.rvv;
+    double fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
+    fk *= W(c[0]);
+    double const sqrt_beta = 1.0 / (sqrt(2.0) * W(c[1]));
+    double const q = W(c[8]);
+    double const arg = -(sqrt_beta * sqrt_beta * z * z);
+    double const omq = 1.0 - q;
+    double const abs_omq = (omq >= 0.0) ? omq : -omq;
+    double e;
+    if (abs_omq >= 1e-6) {
+        double u = 1.0 + omq * arg;
+        if (u < 0.0) u = 0.0;
+        e = pow(u, 1.0 / omq);
+    } else {
+        e = exp(arg);
+    }
+    fk *= (sqrt_beta / W(c[9])) * e;
+    fk /= pc0 * beta;
+    double ex, ey, gx, gy;
+    fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);
+    p.px += fk * ex;
+    p.py += fk * ey;
+}
+
+}  // namespace stg

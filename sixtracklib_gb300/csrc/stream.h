@@ -1,0 +1,69 @@
+// stream.h -- the device element stream: a CObjects lattice compiled into
+// fixed-size chunks of 8-byte words that CTAs stage into shared memory with
+// bulk (TMA) copies and walk as warp-uniform records.
+//
+// Record = header word + parameters.  Header bits: 0-7 opcode, 8-31 record
+// length in words (header included), 32-63 auxiliary value (multipole order,
+// slice count, flags).  One record per lattice element, in lattice order,
+// so the element index is the record ordinal.  Every chunk ends with an
+// OP_END record; records never straddle chunks.
+#pragma once
+
+#include <cstdint>
+
+namespace stg {
+
+enum Op : uint32_t {
+    OP_END = 0,             // end of chunk
+    OP_DRIFT = 1,           // [L]            aux bit0: global aperture check
+    OP_DRIFT_EXACT = 2,     // [L]            aux bit0: global aperture check
+    OP_MULTIPOLE = 3,       // [bal 0..2n+1]  aux = order n
+    OP_MULTIPOLE_CURV = 4,  // [bal..., hxl, hyl, length]  aux = order n
+    OP_CAVITY = 5,          // [voltage, k*frequency, deg2rad*lag]
+    OP_XYSHIFT = 6,         // [-dx, -dy]
+    OP_SROTATION = 7,       // [cos_z, sin_z]
+    OP_LIMIT_RECT = 8,      // [min_x, max_x, min_y, max_y]
+    OP_LIMIT_ELLIPSE = 9,   // [a_squ, b_squ, a_b_squ]
+    OP_LIMIT_RECT_ELLIPSE = 10,  // [max_x, max_y, a_squ, b_squ, a_squ_b_squ]
+    OP_DIPEDGE = 11,        // [r21, r43]
+    OP_RF_MULTIPOLE = 12,   // [voltage, frequency, lag, bal..., phase...] aux = order
+    OP_BB4D = 13,           // [11 BB4D data words]
+    OP_BB6D = 14,           // [34 head words, n_part[N], x[N], y[N], sigma[N]] aux = N
+    OP_SC_COASTING = 15,    // [9 SCCoasting words]
+    OP_SC_QGAUSS = 16,      // [11 SCQGaussProfile words]
+    OP_MONITOR = 17,        // [num_stores, start, skip, max_pid, min_pid, rolling,
+                            //  turn_ordered, out_ptr, out_capacity]
+    OP_NOP = 18,            // success, no effect (disabled beam-beam)
+    OP_FAIL = 19,           // failure (map compiled out, e.g. TriCub)
+    OP_FAIL_LOST = 20,      // failure and particle lost (unknown type id)
+    OP_COUNT
+};
+
+constexpr uint32_t DRIFT_APERTURE = 1u;
+
+inline uint64_t make_header(uint32_t op, uint32_t nwords, uint32_t aux)
+{
+    return (uint64_t)op | ((uint64_t)(nwords & 0xFFFFFFu) << 8) | ((uint64_t)aux << 32);
+}
+
+// Global aperture compare: |x| < limit  <=>  bits(|x|) < bits(limit) for a
+// positive finite limit (IEEE doubles of one sign order like their bit
+// patterns; NaN and inf compare false, as in the reference's float compare).
+inline uint64_t aperture_bits(double limit)
+{
+    if (!(limit > 0.0)) return 0;  // nothing is inside a non-positive limit
+    uint64_t w;
+    __builtin_memcpy(&w, &limit, 8);
+    return w;
+}
+
+struct StreamInfo {
+    int64_t num_elements = 0;
+    int32_t num_chunks = 0;
+    int32_t chunk_words = 0;
+    int32_t max_record_words = 0;
+    int32_t num_monitors = 0;
+    uint32_t op_mask = 0;  // bit per opcode present
+};
+
+}  // namespace stg

@@ -1,0 +1,484 @@
+// track_kernel.cu -- the tracking kernel.
+//
+// One thread per particle; the particle's state lives in registers for the
+// whole call (all turns).  The compiled element stream is staged into shared
+// memory chunk by chunk with cp.async.bulk (the TMA engine's 1-D bulk copy)
+// completing on mbarriers; every warp reads the records as broadcasts and
+// dispatches on the opcode with a warp-uniform switch.  A lattice that fits
+// the shared-memory stages is loaded once and stays resident for all turns;
+// a longer one streams through the stages with STAGES-1 chunks in flight.
+//
+// Loop semantics follow the reference exactly:
+//   until-turn      common/track/track.h:610-670
+//   line            common/track/track.h:779-822
+//   elem-by-elem    common/track/track.h:672-777
+// (at_element_id is start + element ordinal while inside a turn and reset at
+// the turn end, a failing or lost particle freezes where it stopped, status
+// is OR-accumulated, -1 on failure).
+//
+// This translation unit is compiled with -fmad=false; the FAST instantiation
+// uses explicit fma() (maps.cuh).
+#include <cstdint>
+
+#include "kernel_api.h"
+#include "maps.cuh"
+
+namespace stg {
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bulk (TMA) copy global -> shared, completion counted on `bar`.
+// src and dst 16-byte aligned, bytes a multiple of 16 (chunks are).
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Bounded wait: gives up after ~2^31 clock cycles (~1 s) instead of hanging.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    long long const t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > (1ll << 31)) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void load_particle(PState &p, const uint64_t *cols, int64_t n,
+                                              int64_t i)
+{
+    const double *d = reinterpret_cast<const double *>(cols);
+    const int64_t *k = reinterpret_cast<const int64_t *>(cols);
+    p.q0 = d[0 * n + i];
+    p.mass0 = d[1 * n + i];
+    p.beta0 = d[2 * n + i];
+    p.gamma0 = d[3 * n + i];
+    p.p0c = d[4 * n + i];
+    p.s = d[5 * n + i];
+    p.x = d[6 * n + i];
+    p.y = d[7 * n + i];
+    p.px = d[8 * n + i];
+    p.py = d[9 * n + i];
+    p.zeta = d[10 * n + i];
+    p.psigma = d[11 * n + i];
+    p.delta = d[12 * n + i];
+    p.rpp = d[13 * n + i];
+    p.rvv = d[14 * n + i];
+    p.chi = d[15 * n + i];
+    p.charge_ratio = d[16 * n + i];
+    p.pid = k[17 * n + i];
+    p.at_element = k[18 * n + i];
+    p.at_turn = k[19 * n + i];
+    p.state = k[20 * n + i];
+    p.energy0 = sqrt(p.p0c * p.p0c + p.mass0 * p.mass0);
+}
+
+// Write one full record (21 columns) to a column block of capacity cap.
+__device__ __forceinline__ void store_record(const PState &p, uint64_t *out, int64_t cap,
+                                             int64_t j, int64_t at_element, int64_t at_turn)
+{
+    double *d = reinterpret_cast<double *>(out);
+    int64_t *k = reinterpret_cast<int64_t *>(out);
+    d[0 * cap + j] = p.q0;
+    d[1 * cap + j] = p.mass0;
+    d[2 * cap + j] = p.beta0;
+    d[3 * cap + j] = p.gamma0;
+    d[4 * cap + j] = p.p0c;
+    d[5 * cap + j] = p.s;
+    d[6 * cap + j] = p.x;
+    d[7 * cap + j] = p.y;
+    d[8 * cap + j] = p.px;
+    d[9 * cap + j] = p.py;
+    d[10 * cap + j] = p.zeta;
+    d[11 * cap + j] = p.psigma;
+    d[12 * cap + j] = p.delta;
+    d[13 * cap + j] = p.rpp;
+    d[14 * cap + j] = p.rvv;
+    d[15 * cap + j] = p.chi;
+    d[16 * cap + j] = p.charge_ratio;
+    k[17 * cap + j] = p.pid;
+    k[18 * cap + j] = at_element;
+    k[19 * cap + j] = at_turn;
+    k[20 * cap + j] = p.state;
+}
+
+// be_monitor/track.h:48-110: output index for the current turn, or -1.
+__device__ __forceinline__ int64_t monitor_index(const uint64_t *rec, int64_t turn, int64_t pid)
+{
+    int64_t const nstores = (int64_t)rec[1], start = (int64_t)rec[2], skip = (int64_t)rec[3];
+    int64_t const max_pid = (int64_t)rec[4], min_pid = (int64_t)rec[5];
+    int64_t const since = turn - start;
+    int64_t out = -1;
+    if (since >= 0 && (since % skip) == 0) {
+        int64_t idx = since / skip;
+        if (idx >= nstores && rec[6] != 0) idx = idx % nstores;
+        if (idx < nstores) {
+            int64_t const off = pid - min_pid;
+            int64_t const np = max_pid - min_pid + 1;
+            out = (rec[7] != 0) ? np * idx + off : off * np + idx;
+        }
+    }
+    return out;
+}
+
+// output/elem_by_elem_config.h:667-763
+__device__ __forceinline__ int64_t ebe_index(const EbeDevConfig &c, int64_t pid, int64_t elem,
+                                             int64_t turn)
+{
+    int64_t out = -1;
+    if (c.min_particle_id <= pid && c.max_particle_id >= pid && c.min_element_id <= elem &&
+        c.max_element_id >= elem && c.min_turn <= turn &&
+        (c.max_turn >= turn || c.is_rolling != 0)) {
+        int64_t const np = c.num_particles_to_store, ne = c.num_elements_to_store;
+        int64_t cap = 0;
+        if (c.order == 0) {
+            out = (turn - c.min_turn) * np * ne + (elem - c.min_element_id) * np +
+                  (pid - c.min_particle_id);
+            cap = np * ne * c.num_turns_to_store;
+        }
+        if (out >= cap && cap > 0 && c.is_rolling != 0) out = out % cap;
+    }
+    return out;
+}
+
+// Apply one element; returns 0 or -1 (reference status).  `lost` is set when
+// the particle leaves the aperture (state becomes 0).
+template <bool FAST>
+__device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hdr,
+                                     const TrackParams &prm, int64_t cur_elem, int64_t cur_turn)
+{
+    uint32_t const op = (uint32_t)(hdr & 0xFF);
+    uint32_t const aux = (uint32_t)(hdr >> 32);
+    switch (op) {
+    case OP_DRIFT:
+        drift<FAST>(p, W(rec[1]));
+        if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
+        return 0;
+    case OP_MULTIPOLE:
+        multipole<FAST, false>(p, rec, (int)aux);
+        return 0;
+    case OP_SROTATION:
+        srotation<FAST>(p, rec);
+        return 0;
+    case OP_XYSHIFT:
+        p.x += W(rec[1]);
+        p.y += W(rec[2]);
+        return 0;
+    case OP_LIMIT_ELLIPSE:
+        p.state &= (int64_t)inside_ellipse(p, rec);
+        return 0;
+    case OP_CAVITY:
+        cavity(p, rec);
+        return 0;
+    case OP_MULTIPOLE_CURV:
+        multipole<FAST, true>(p, rec, (int)aux);
+        return 0;
+    case OP_DRIFT_EXACT:
+        drift_exact(p, W(rec[1]));
+        if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
+        return 0;
+    case OP_LIMIT_RECT:
+        p.state &= (int64_t)inside_rect(p, rec);
+        return 0;
+    case OP_LIMIT_RECT_ELLIPSE:
+        p.state &= (int64_t)inside_rect_ellipse(p, rec);
+        return 0;
+    case OP_DIPEDGE:
+        p.px += W(rec[1]) * p.x;
+        p.py += W(rec[2]) * p.y;
+        return 0;
+    case OP_RF_MULTIPOLE:
+        rf_multipole(p, rec, (int)aux);
+        return 0;
+    case OP_BB4D:
+        beam_beam_4d(p, rec);
+        return 0;
+    case OP_BB6D:
+        beam_beam_6d(p, rec, (int)aux);
+        return 0;
+    case OP_SC_COASTING:
+        sc_coasting(p, rec);
+        return 0;
+    case OP_SC_QGAUSS:
+        sc_qgauss(p, rec);
+        return 0;
+    case OP_MONITOR: {
+        uint64_t *out = reinterpret_cast<uint64_t *>(rec[8]);
+        if (out == nullptr) return 0;
+        int64_t const j = monitor_index(rec, p.at_turn, p.pid);
+        if (j < 0) return 0;
+        if (j >= (int64_t)rec[9]) {
+            p.state = 0;
+            return -1;
+        }
+        store_record(p, out, (int64_t)rec[9], j, cur_elem, cur_turn);
+        return 0;
+    }
+    case OP_NOP:
+        return 0;
+    case OP_FAIL:
+        return -1;
+    default:  // OP_FAIL_LOST: unknown type id
+        p.state = 0;
+        return -1;
+    }
+}
+
+}  // namespace
+
+// Kernel. Block-uniform control flow: every thread walks every record of
+// every chunk of every turn the block needs; lanes whose particle is done
+// are predicated off inside apply().
+template <bool FAST>
+__global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
+{
+    extern __shared__ __align__(128) uint64_t smem[];
+    int const stages = prm.stages;
+    int const cw = prm.chunk_words;
+    uint64_t *bars = smem;                 // `stages` mbarriers (8 B each, padded to 16 words)
+    uint64_t *bufs = smem + 16;            // stages * cw words
+    __shared__ long long s_tmin;
+
+    int64_t const i = prm.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool const valid = i < prm.i1;
+    PState p;
+    if (valid) load_particle(p, prm.cols, prm.n, i);
+
+    // ---------------------------------------------------- per-mode setup
+    int64_t const start_elem = valid ? p.at_element : 0;
+    bool active;   // still has work in this call
+    if (prm.mode == MODE_UNTIL) {
+        active = valid && p.state == 1 && p.at_turn < prm.until_turn;
+    } else if (prm.mode == MODE_LINE) {
+        active = valid && p.state == 1;
+    } else {  // MODE_EBE: the reference does not check state here
+        active = valid && prm.until_turn > p.at_turn && p.at_turn >= 0 && start_elem >= 0 &&
+                 p.pid >= 0;
+    }
+    int status = 0;
+    int64_t stop_elem = -1;  // element ordinal where tracking stopped
+
+    if (threadIdx.x == 0) {
+        s_tmin = 0x7FFFFFFFFFFFFFFFll;
+        for (int s = 0; s < stages; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (active && prm.mode != MODE_LINE) atomicMin(&s_tmin, (long long)p.at_turn);
+    bool any = __syncthreads_or(active);
+    int64_t turn = (prm.mode == MODE_LINE) ? 0 : (int64_t)s_tmin;
+
+    int const nch = prm.n_chunks;
+    bool const resident = nch <= stages;
+    int64_t issued = 0;    // chunk loads issued (meaningful in thread 0 only)
+    int64_t consumed = 0;  // chunk loads waited for (block-uniform)
+    bool timed_out = false;
+    if (any) {
+        if (threadIdx.x == 0) {
+            int const first = resident ? nch : stages;
+            for (int g = 0; g < first; ++g) {
+                mbar_arrive_expect_tx(&bars[g], (uint32_t)(cw * 8));
+                bulk_copy_g2s(bufs + (size_t)g * cw, prm.stream + (size_t)(g % nch) * cw,
+                              (uint32_t)(cw * 8), &bars[g]);
+            }
+            issued = first;
+        }
+        if (resident) {  // the whole lattice stays in shared memory
+            bool ok = true;
+            for (int g = 0; g < nch; ++g) ok = mbar_wait_bounded(&bars[g], 0u) && ok;
+            consumed = nch;
+            timed_out = __syncthreads_or(!ok);
+        }
+    }
+
+    while (any && !timed_out) {
+        bool part = (prm.mode == MODE_LINE) ? active : (active && (p.at_turn == turn));
+        int64_t ord = 0;  // element ordinal within the turn / line
+        int64_t ae = start_elem;
+        for (int c = 0; c < nch; ++c) {
+            int buf = c;
+            if (!resident) {
+                buf = (int)(consumed % stages);
+                uint32_t const parity = (uint32_t)((consumed / stages) & 1);
+                bool const ok = mbar_wait_bounded(&bars[buf], parity);
+                ++consumed;
+                if (__syncthreads_or(!ok)) {
+                    timed_out = true;
+                    break;
+                }
+            }
+            const uint64_t *rec = bufs + (size_t)buf * cw;
+            while (true) {
+                uint64_t const hdr = rec[0];
+                if ((uint32_t)(hdr & 0xFF) == OP_END) break;
+                if (part) {
+                    if (prm.mode == MODE_EBE) {
+                        int64_t const j = ebe_index(prm.ebe, p.pid, ae, p.at_turn);
+                        if (j >= 0 && j < prm.ebe_cap)
+                            store_record(p, prm.ebe_out, prm.ebe_cap, j, ae, p.at_turn);
+                    }
+                    int const rc = apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn);
+                    if (rc != 0 || p.state != 1) {
+                        status |= rc;
+                        part = false;
+                        active = false;
+                        stop_elem = ord;
+                    } else {
+                        ++ae;
+                    }
+                }
+                ++ord;
+                rec += (hdr >> 8) & 0xFFFFFF;
+            }
+            if (!resident) {
+                __syncthreads();  // every warp is done with this stage buffer
+                if (threadIdx.x == 0) {
+                    int64_t const g = issued;  // next chunk of the cyclic stream
+                    int const b = (int)(g % stages);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive_expect_tx(&bars[b], (uint32_t)(cw * 8));
+                    bulk_copy_g2s(bufs + (size_t)b * cw, prm.stream + (size_t)(g % nch) * cw,
+                                  (uint32_t)(cw * 8), &bars[b]);
+                    issued = g + 1;
+                }
+            }
+        }
+        if (timed_out) break;
+        if (prm.mode == MODE_LINE) {
+            if (part && prm.finish_turn) {  // track/track.h:813-819
+                p.at_turn += 1;
+                p.s = 0.0;
+            }
+            active = false;
+        } else if (part) {  // turn completed
+            p.at_turn += 1;
+            p.s = 0.0;
+            if (p.at_turn >= prm.until_turn) active = false;
+        }
+        ++turn;
+        any = __syncthreads_or(active);
+    }
+
+    // drain bulk copies still in flight before the CTA exits
+    if (threadIdx.x == 0 && !resident) {
+        while (consumed < issued) {
+            int const buf = (int)(consumed % stages);
+            uint32_t const parity = (uint32_t)((consumed / stages) & 1);
+            if (!mbar_wait_bounded(&bars[buf], parity)) {
+                timed_out = true;
+                break;
+            }
+            ++consumed;
+        }
+    }
+    if (timed_out) {
+        if (threadIdx.x == 0) atomicOr(prm.error, ERR_PIPELINE_TIMEOUT);
+        return;  // particle columns are left untouched
+    }
+
+    if (!valid) return;
+    // ------------------------------------------------ final bookkeeping
+    if (prm.mode == MODE_UNTIL) {
+        if (stop_elem >= 0) {
+            p.state = 0;  // track/track.h:663-666
+            p.at_element = start_elem + stop_elem;
+        }
+    } else if (prm.mode == MODE_LINE) {
+        int64_t const done = (stop_elem >= 0) ? stop_elem : prm.num_elements;
+        p.at_element = start_elem + done;
+        if (stop_elem < 0 && prm.finish_turn && p.state == 1) p.at_element = 0;
+    } else {  // EBE
+        if (stop_elem >= 0) p.at_element = start_elem + stop_elem;
+    }
+    if (status != 0) atomicOr(prm.status, status);
+
+    double *d = reinterpret_cast<double *>(prm.cols);
+    int64_t *k = reinterpret_cast<int64_t *>(prm.cols);
+    int64_t const n = prm.n;
+    d[5 * n + i] = p.s;
+    d[6 * n + i] = p.x;
+    d[7 * n + i] = p.y;
+    d[8 * n + i] = p.px;
+    d[9 * n + i] = p.py;
+    d[10 * n + i] = p.zeta;
+    d[11 * n + i] = p.psigma;
+    d[12 * n + i] = p.delta;
+    d[13 * n + i] = p.rpp;
+    d[14 * n + i] = p.rvv;
+    k[18 * n + i] = p.at_element;
+    k[19 * n + i] = p.at_turn;
+    k[20 * n + i] = p.state;
+}
+
+template __global__ void track_kernel<false>(TrackParams);
+template __global__ void track_kernel<true>(TrackParams);
+
+}  // namespace stg
+
+namespace stg {
+
+size_t track_smem_bytes(int stages, int chunk_words)
+{
+    return (size_t)(16 + (size_t)stages * chunk_words) * sizeof(uint64_t);
+}
+
+int launch_track(const TrackParams &prm, bool fast, int threads, void *stream)
+{
+    int64_t const count = prm.i1 - prm.i0;
+    if (count <= 0) return 0;
+    if (threads <= 0 || threads > kMaxThreads || threads % 32 != 0) threads = 256;
+    int64_t const blocks = (count + threads - 1) / threads;
+    size_t const smem = track_smem_bytes(prm.stages, prm.chunk_words);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t err;
+    if (fast) {
+        err = cudaFuncSetAttribute(track_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem);
+        if (err != cudaSuccess) return (int)err;
+        track_kernel<true><<<(unsigned)blocks, threads, smem, s>>>(prm);
+    } else {
+        err = cudaFuncSetAttribute(track_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem);
+        if (err != cudaSuccess) return (int)err;
+        track_kernel<false><<<(unsigned)blocks, threads, smem, s>>>(prm);
+    }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace stg

@@ -1,0 +1,181 @@
+"""Seeded synthetic lattices and particle distributions.
+
+These generate the workloads the engine is measured and checked on.  All are
+synthetic (no public dataset is involved) and fully determined by the seed:
+
+* :func:`fodo_ring` -- 64 FODO cells (drift 2 m, focusing / defocusing quad
+  kicks k1l = +-0.05), one 6 MV / 400 MHz cavity at lag 180 deg and one
+  +-0.02 m LimitRect (258 elements);
+* :func:`synthetic_ring` -- 20,000 elements: 9,000 drifts L~U(0.5,5) m,
+  8,000 multipoles of order U{1..10} (k1l = +-U(0.01,0.05) alternating,
+  b_n ~ N(0, 1e-4 * 10^-n)), 1,000 XYShift N(0,1e-5) m, 1,000 SRotation
+  N(0,1e-4) rad, 16 cavities, 984 LimitEllipse (a=0.015, b=0.01);
+* :func:`bb_sc_ring` -- the FODO ring plus 4 BeamBeam6D (21 slices), 4
+  BeamBeam4D and 200 q-Gaussian space-charge kicks;
+* particle sets: Gaussian 6D and the polar amplitude grid.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .beam_elements import (
+    QELEM, BeamBeam4D, BeamBeam6D, Cavity, Drift, Elements, LimitEllipse,
+    LimitRect, Multipole, SCQGaussProfile, SRotation, XYShift, bb6d_data,
+)
+from .particles import PROTON_MASS_EV, Particles
+
+P0C = 7e12
+
+
+def fodo_cells(elements: Elements, n_cells=64, k1l=0.05, drift=2.0):
+    for _ in range(n_cells):
+        elements.Drift(length=drift)
+        elements.Multipole(knl=[0.0, +k1l])
+        elements.Drift(length=drift)
+        elements.Multipole(knl=[0.0, -k1l])
+
+
+def fodo_ring(n_cells=64, with_cavity=True, with_aperture=True) -> Elements:
+    """The plain FODO ring (258 elements)."""
+    e = Elements()
+    fodo_cells(e, n_cells)
+    if with_cavity:
+        e.Cavity(voltage=6e6, frequency=400e6, lag=180.0)
+    if with_aperture:
+        e.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02)
+    return e
+
+
+def synthetic_ring(seed=20240601, n_cells=4000, n_extra_drift=1000,
+                   n_shift=1000, n_rot=1000, n_cav=16, n_ell=984) -> Elements:
+    """The 20,000-element synthetic ring.
+
+    Linear structure: ``n_cells`` FODO cells [Drift L, QF +k, Drift L, QD -k]
+    with L ~ U(0.5, 5) m per cell and k ~ U(0.01, 0.05).  The drawn k values
+    are arranged as a slow ramp up and back down around the ring so that
+    neighbouring cells are nearly matched; randomly ordered quad strengths
+    make the one-turn map unstable (every particle is lost), this ordering
+    keeps it stable.  Each multipole has order ~ U{1..10} with
+    b_n ~ N(0, 1e-4 * 10^-n) for n >= 2.  ``n_extra_drift`` of the cell drifts
+    (with L >= 1 m) are split in two halves; XYShift N(0,1e-5) m, SRotation
+    N(0,1e-4) rad and LimitEllipse (a=0.015, b=0.01 m) are inserted after
+    randomly chosen quads, the cavities (lag 180 deg) evenly around the ring.
+    """
+    rng = np.random.default_rng(seed)
+    k = np.sort(rng.uniform(0.01, 0.05, n_cells))
+    k = np.concatenate([k[0::2], k[1::2][::-1]])
+    L = rng.uniform(0.5, 5.0, n_cells)
+    orders = rng.integers(1, 11, size=2 * n_cells)
+    split = np.zeros(2 * n_cells, dtype=bool)
+    cand = np.nonzero(np.repeat(L, 2) >= 1.0)[0]
+    split[rng.choice(cand, size=n_extra_drift, replace=False)] = True
+    extras = {}
+    kinds = [2] * n_shift + [3] * n_rot + [5] * n_ell
+    slots = rng.choice(2 * n_cells, size=len(kinds), replace=True)
+    for s_, kd in zip(slots, kinds):
+        extras.setdefault(int(s_), []).append(kd)
+    cav_slots = set(int(i) for i in np.linspace(0, 2 * n_cells, n_cav, endpoint=False))
+    e = Elements()
+    for c in range(n_cells):
+        for h in range(2):
+            j = 2 * c + h
+            if split[j]:
+                e.Drift(length=float(L[c] * 0.5))
+                e.Drift(length=float(L[c] * 0.5))
+            else:
+                e.Drift(length=float(L[c]))
+            order = int(orders[j])
+            knl = np.zeros(order + 1)
+            knl[1] = k[c] if h == 0 else -k[c]
+            for n in range(2, order + 1):
+                knl[n] = float(rng.normal(0.0, 1e-4 * 10.0 ** (-n)))
+            e.Multipole(knl=list(knl))
+            if j in cav_slots:
+                e.Cavity(voltage=6e6 / n_cav, frequency=400e6, lag=180.0)
+            for kd in extras.get(j, ()):
+                if kd == 2:
+                    e.XYShift(dx=float(rng.normal(0, 1e-5)), dy=float(rng.normal(0, 1e-5)))
+                elif kd == 3:
+                    ang = float(rng.normal(0.0, 1e-4))
+                    e.SRotation(cos_z=float(np.cos(ang)), sin_z=float(np.sin(ang)))
+                else:
+                    e.LimitEllipse(a=0.015, b=0.01)
+    return e
+
+
+def bb_sc_ring(seed=7, n_bb6d=4, n_bb4d=4, n_sc=200, n_slices=21,
+               sigma_x=16.7e-6, sigma_y=16.7e-6, sigma_z=0.0755,
+               bunch_charge=1.15e11, elliptic=False) -> Elements:
+    """FODO ring plus beam-beam and space-charge kicks (BB6D uses a Gaussian
+    longitudinal slicing of the strong bunch into equal-charge slices)."""
+    rng = np.random.default_rng(seed)
+    e = fodo_ring()
+    sx, sy = sigma_x, (sigma_y * 1.3 if elliptic else sigma_y)
+    # equal-charge Gaussian slice centroids
+    from math import erf, sqrt
+
+    edges = np.linspace(0, 1, n_slices + 1)
+    z = np.zeros(n_slices)
+    for i in range(n_slices):
+        mid = 0.5 * (edges[i] + edges[i + 1])
+        lo, hi = -8.0, 8.0
+        for _ in range(80):
+            m = 0.5 * (lo + hi)
+            if 0.5 * (1 + erf(m / sqrt(2))) < mid:
+                lo = m
+            else:
+                hi = m
+        z[i] = 0.5 * (lo + hi) * sigma_z
+    n_per_slice = np.full(n_slices, bunch_charge / n_slices)
+    for i in range(n_bb6d):
+        data = bb6d_data(
+            q_part=QELEM, phi=float(rng.uniform(1e-4, 2e-4)), alpha=float(rng.uniform(0, 0.5)),
+            delta_x=float(rng.normal(0, 1e-6)), delta_y=float(rng.normal(0, 1e-6)),
+            n_part_per_slice=n_per_slice, z_slices=z,
+            sigmas=(sx * sx, 0.0, 0.0, 0.0, 1e-12, 0.0, 0.0, sy * sy, 0.0, 1e-12),
+            min_sigma_diff=1e-10, threshold_singular=1e-28)
+        e.BeamBeam6D(data=data)
+        e.Drift(length=1.0)
+    for i in range(n_bb4d):
+        e.BeamBeam4D(charge=bunch_charge, sigma_x=sx, sigma_y=sy, beta_r=1.0,
+                     min_sigma_diff=1e-10, x_bb=float(rng.normal(0, 1e-6)),
+                     y_bb=float(rng.normal(0, 1e-6)), d_px=0.0, d_py=0.0, enabled=1.0)
+        e.Drift(length=1.0)
+    for i in range(n_sc):
+        e.SCQGaussProfile(number_of_particles=1e11, bunchlength_rms=0.1,
+                          sigma_x=1e-3, sigma_y=(1.2e-3 if elliptic else 1e-3),
+                          length=0.1, x_co=0.0, y_co=0.0, min_sigma_diff=1e-10,
+                          q_param=1.0, enabled=1)
+    return e
+
+
+def gaussian_particles(n, seed=12345, sx=1e-3, spx=1e-5, sy=1e-3, spy=1e-5,
+                       sz=0.05, sdelta=1e-4, p0c=P0C) -> Particles:
+    rng = np.random.default_rng(seed)
+    p = Particles(num_particles=n).set_reference(p0c=p0c, mass0=PROTON_MASS_EV, q0=1.0)
+    p.x[:] = rng.normal(0, sx, n)
+    p.px[:] = rng.normal(0, spx, n)
+    p.y[:] = rng.normal(0, sy, n)
+    p.py[:] = rng.normal(0, spy, n)
+    p.zeta[:] = rng.normal(0, sz, n)
+    p.set_delta(rng.normal(0, sdelta, n))
+    return p
+
+
+def polar_grid_particles(n=1_000_000, n_angles=11, max_sigma=20.0, sigma=1e-3,
+                         seed=99, p0c=P0C) -> Particles:
+    """Polar amplitude grid: ceil(n/11) radii in [0, 20 sigma] x 11 angles,
+    truncated to n; delta ~ U(-3e-4, 3e-4)."""
+    rng = np.random.default_rng(seed)
+    n_r = -(-n // n_angles)
+    r = np.linspace(0.0, max_sigma * sigma, n_r)
+    th = np.linspace(0.0, 0.5 * np.pi, n_angles)
+    rr, tt = np.meshgrid(r, th, indexing="ij")
+    x = (rr * np.cos(tt)).reshape(-1)[:n]
+    y = (rr * np.sin(tt)).reshape(-1)[:n]
+    p = Particles(num_particles=n).set_reference(p0c=p0c, mass0=PROTON_MASS_EV, q0=1.0)
+    p.x[:] = x
+    p.y[:] = y
+    p.set_delta(rng.uniform(-3e-4, 3e-4, n))
+    return p

@@ -1,0 +1,182 @@
+"""NS(Particles): the 21-column particle SoA and its CObjects encoding.
+
+Field order and types follow sixtracklib/common/particles.h:38-67 (17 float64
+columns, then particle_id, at_element_id, at_turn, state as int64).  In a
+CObjects buffer a Particles object (type id 1) is ``num_particles`` followed
+by 21 column pointers and the 21 columns.  Python names follow
+python/sixtracklib/particles.py (``at_element`` for ``at_element_id``).
+
+The "column block" used throughout this package (and by the C ABI's
+``st_ParticlesColumns`` helpers and the oracle) is the same 21 columns laid
+out contiguously: column ``c`` occupies words ``[c*n, (c+1)*n)``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .cbuffer import CBuffer, CObject
+
+REAL_FIELDS = (
+    "q0", "mass0", "beta0", "gamma0", "p0c", "s", "x", "y", "px", "py",
+    "zeta", "psigma", "delta", "rpp", "rvv", "chi", "charge_ratio",
+)
+INT_FIELDS = ("particle_id", "at_element", "at_turn", "state")
+FIELDS = REAL_FIELDS + INT_FIELDS
+NUM_COLUMNS = 21
+COL = {name: i for i, name in enumerate(FIELDS)}
+TYPE_PARTICLE = 1
+PROTON_MASS_EV = 938272088.16  # internal/physics_constants.h:53
+
+
+class Particles:
+    """A particle set backed by one contiguous column block.
+
+    ``Particles(num_particles=n)`` creates a fresh set (chi = charge_ratio =
+    state = 1, particle_id = 0..n-1); pass ``cbuffer=`` to append it to a
+    CObjects buffer, in which case the columns live inside the buffer object
+    and edits are visible to whoever serialises the buffer.
+    """
+
+    pmass = PROTON_MASS_EV
+
+    def __init__(self, num_particles=0, cbuffer=None, _words=None, _index=None):
+        n = int(num_particles)
+        self.num_particles = n
+        if _words is None:
+            words = np.zeros(22 + NUM_COLUMNS * n, dtype=np.uint64)
+            words[0] = n
+            for c in range(NUM_COLUMNS):
+                words[1 + c] = 22 + c * n
+            self._words = words
+            self._init_defaults()
+        else:
+            self._words = _words
+        self._cbuffer = None
+        self._index = _index
+        if cbuffer is not None:
+            obj = CObject(TYPE_PARTICLE, self._words, list(range(1, 22)))
+            cbuffer.objects.append(obj)
+            cbuffer.touch()
+            cbuffer.typeids[TYPE_PARTICLE] = Particles
+            self._index = cbuffer.n_objects - 1
+            self._cbuffer = cbuffer
+
+    def _init_defaults(self):
+        n = self.num_particles
+        self.chi[:] = 1.0
+        self.charge_ratio[:] = 1.0
+        self.state[:] = 1
+        self.particle_id[:] = np.arange(n)
+        self.rpp[:] = 1.0
+        self.rvv[:] = 1.0
+
+    # --------------------------------------------------------- columns
+    def column(self, name_or_idx) -> np.ndarray:
+        c = COL[name_or_idx] if isinstance(name_or_idx, str) else int(name_or_idx)
+        off = int(self._words[1 + c])
+        seg = self._words[off : off + self.num_particles]
+        return seg.view(np.float64) if c < 17 else seg.view(np.int64)
+
+    @property
+    def block(self) -> np.ndarray:
+        """The 21 x n column block as u64 words (a view when contiguous)."""
+        n = self.num_particles
+        offs = [int(self._words[1 + c]) for c in range(NUM_COLUMNS)]
+        if offs == [22 + c * n for c in range(NUM_COLUMNS)]:
+            return self._words[22 : 22 + NUM_COLUMNS * n].reshape(NUM_COLUMNS, n)
+        return np.stack([self._words[o : o + n] for o in offs])
+
+    def set_block(self, block: np.ndarray):
+        block = np.asarray(block).reshape(NUM_COLUMNS, -1).view(np.uint64)
+        for c in range(NUM_COLUMNS):
+            off = int(self._words[1 + c])
+            self._words[off : off + self.num_particles] = block[c]
+        if self._cbuffer is not None:
+            self._cbuffer.touch()
+
+    def copy(self) -> "Particles":
+        p = Particles(self.num_particles)
+        p.set_block(self.block.copy())
+        return p
+
+    # --------------------------------------------------------- physics
+    def set_reference(self, p0c=7e12, mass0=PROTON_MASS_EV, q0=1.0):
+        """Reference momentum, mass and charge; beta0/gamma0 from p0c."""
+        energy0 = np.sqrt(p0c * p0c + mass0 * mass0)
+        self.q0[:] = q0
+        self.mass0[:] = mass0
+        self.p0c[:] = p0c
+        self.beta0[:] = p0c / energy0
+        self.gamma0[:] = energy0 / mass0
+        return self
+
+    def set_delta(self, delta):
+        """Set delta and the dependent rvv, rpp, psigma with the arithmetic of
+        NS(Particles_update_delta_value) (particles.h:5459-5496)."""
+        d = np.asarray(delta, dtype=np.float64) * np.ones(self.num_particles)
+        beta0 = self.beta0.copy()
+        delta_beta0 = d * beta0
+        ptau_beta0 = np.sqrt(delta_beta0 * delta_beta0 + 2.0 * delta_beta0 * beta0 + 1.0) - 1.0
+        opd = 1.0 + d
+        self.delta[:] = d
+        self.rvv[:] = opd / (1.0 + ptau_beta0)
+        self.rpp[:] = 1.0 / opd
+        self.psigma[:] = ptau_beta0 / (beta0 * beta0)
+        return self
+
+    @classmethod
+    def from_ref(cls, num_particles=1, mass0=PROTON_MASS_EV, p0c=1e9, q0=1.0):
+        return cls(num_particles=num_particles).set_reference(p0c=p0c, mass0=mass0, q0=q0)
+
+    @classmethod
+    def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
+        n = int(obj.words[0])
+        p = cls(num_particles=n, _words=obj.words, _index=index)
+        p._cbuffer = cbuffer
+        return p
+
+    def __len__(self):
+        return self.num_particles
+
+
+def _make_prop(name):
+    def getter(self):
+        return self.column(name)
+
+    def setter(self, value):
+        self.column(name)[:] = value
+        if self._cbuffer is not None:
+            self._cbuffer.touch()
+
+    return property(getter, setter)
+
+
+for _name in FIELDS:
+    setattr(Particles, _name, _make_prop(_name))
+Particles.at_element_id = _make_prop("at_element")
+
+
+class ParticlesSet:
+    """Container of particle sets in one CObjects buffer
+    (python/sixtracklib/particles.py:417-489)."""
+
+    def __init__(self, cbuffer=None):
+        self.cbuffer = CBuffer() if cbuffer is None else cbuffer
+        self.cbuffer.typeids[TYPE_PARTICLE] = Particles
+
+    def Particles(self, num_particles=0, **kw):
+        return Particles(num_particles=num_particles, cbuffer=self.cbuffer, **kw)
+
+    @property
+    def particles(self):
+        return [self.cbuffer.get_object(i) for i in range(self.cbuffer.n_objects)
+                if self.cbuffer.objects[i].typeid == TYPE_PARTICLE]
+
+    @classmethod
+    def fromfile(cls, filename):
+        return cls(cbuffer=CBuffer.fromfile(filename))
+
+    def to_file(self, filename):
+        self.cbuffer.tofile(filename)
+        return self
