@@ -1,0 +1,411 @@
+"""Benchmark: FP64 element-by-element tracking throughput on the GPU.
+
+Workload (one "step" = one turn of every particle through the ring):
+  the synthetic 20,000-element ring (9,000 drifts, 8,000 multipoles of order
+  1-10, 1,000 XYShift, 1,000 SRotation, 16 cavities, 984 elliptic apertures;
+  sixtracklib_gb300/lattices.py) tracked with 1,000,000 protons on the polar
+  amplitude grid (0-20 sigma x 11 angles, delta ~ U(-3e-4, 3e-4)), FP64.
+Metric: particle-element-turns per second (PET/s); every element a live
+particle passes counts once (lost particles stop counting where they are lost).
+
+  value       device-resident: columns in HBM, one kernel launch per step;
+  e2e         through the C ABI (st_TrackJob_*) with host buffers: each step
+              pushes the particle set host->device, tracks, collects back;
+  roofline    FP64 pipe: algorithmic FLOPs of the maps (roofline.py) per
+              launch / launch time, against the DFMA peak measured in-process;
+  cpu_baseline  the CPU oracle (C restatement of the reference loop, OpenMP
+              over particles) on a bounded sample of the same workload.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-element-turns/s"
+WORKLOAD = "synthetic 20k-element ring, 1M particles polar grid, FP64, 1 turn per step"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--particles", type=int, default=1_000_000)
+    ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (median SM clock, reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# -------------------------------------------------------------- workload
+def make_workload(n):
+    from sixtracklib_gb300 import lattices
+
+    ring = lattices.synthetic_ring()
+    parts = lattices.polar_grid_particles(n)
+    return ring, parts
+
+
+def pet_between(before, after, n_elem):
+    """Exact particle-element-turns done between two column-block states."""
+    import torch
+
+    st0 = before[20]
+    t0, t1 = before[19], after[19]
+    e0, e1 = before[18], after[18]
+    st1 = after[20]
+    alive0 = st0 == 1
+    turns = (t1 - t0).clamp(min=0)
+    lost = alive0 & (st1 == 0)
+    pet = torch.where(alive0, turns * n_elem, torch.zeros_like(turns))
+    pet = pet + torch.where(lost, (e1 - e0) + 1, torch.zeros_like(turns))
+    return int(pet.sum().item())
+
+
+def cpu_baseline(ring, parts, seconds, threads=None):
+    """Time the oracle (OpenMP over particles) on a sample of the workload."""
+    from oracle.pyoracle import Oracle
+
+    orc = Oracle()
+    lat = ring.cbuffer.to_image()
+    n_elem = len(ring)
+    stride = max(1, parts.num_particles // 16384)
+    sample = parts.block[:, ::stride][:, :16384].copy()
+    n = sample.shape[1]
+    t = time.perf_counter()
+    b = sample.copy()
+    orc.track_until(lat, b, 1)
+    dt1 = time.perf_counter() - t
+    turns = max(1, int(seconds / max(dt1, 1e-3)))
+    b = sample.copy()
+    t = time.perf_counter()
+    orc.track_until(lat, b, turns)
+    dt = time.perf_counter() - t
+    alive0 = sample[20].view(np.int64) == 1
+    t1 = b[19].view(np.int64)
+    st1 = b[20].view(np.int64)
+    e1 = b[18].view(np.int64)
+    pet = int((alive0 * t1 * n_elem).sum() + ((alive0 & (st1 == 0)) * (e1 + 1)).sum())
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": pet / dt, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{n} particles (strided) x {turns} turns of the same ring, "
+                      f"{pet:.3e} PET in {dt:.2f} s; oracle/oracle.c, OpenMP over particles"}
+
+
+# ------------------------------------------------------------------- e2e
+def e2e_measure(ring, parts, steps, warmup, mode, threads):
+    """Through the C ABI with host buffers (TrackJob): push, track one turn,
+    collect -- per step."""
+    import ctypes as C
+
+    from sixtracklib_gb300 import ParticlesSet, _native
+
+    lib = _native.load()
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=parts.num_particles)
+    p.set_block(parts.block)
+    img_p = ps.cbuffer.to_image()
+    img_e = ring.cbuffer.to_image()
+    pb = lib.st_Buffer_new_on_data(img_p.ctypes.data, img_p.nbytes)
+    eb = lib.st_Buffer_new_on_data(img_e.ctypes.data, img_e.nbytes)
+    idx = (C.c_uint64 * 1)(0)
+    job = lib.st_TrackJob_new_detailed(b"cuda", pb, 1, idx, eb, None, 0,
+                                       f"mode={mode} threads_per_block={threads}".encode())
+    if not job:
+        raise RuntimeError(_native.last_error())
+    n_elem = len(ring)
+
+    def alive_turns():
+        sp = lib.st_Particles_buffer_get_particles(pb, 0)
+        arr = C.cast(sp, C.POINTER(C.c_uint64))
+        n = int(arr[0])
+        col = lambda c: np.ctypeslib.as_array(  # noqa: E731
+            C.cast(arr[1 + c], C.POINTER(C.c_int64)), shape=(n,)).copy()
+        return col(18), col(19), col(20)  # at_element, at_turn, state
+
+    turn = 0
+    for _ in range(warmup):
+        turn += 1
+        lib.st_TrackJob_push_particles(job)
+        lib.st_TrackJob_track_until(job, turn)
+        lib.st_TrackJob_collect_particles(job)
+    e0, t0, s0 = alive_turns()
+    t = time.perf_counter()
+    for _ in range(steps):
+        turn += 1
+        lib.st_TrackJob_push_particles(job)
+        st = lib.st_TrackJob_track_until(job, turn)
+        lib.st_TrackJob_collect_particles(job)
+        if st != 0:
+            raise RuntimeError(f"track status {st}: {_native.last_error()}")
+    dt = time.perf_counter() - t
+    e1, t1, s1 = alive_turns()
+    alive0 = s0 == 1
+    pet = int(((t1 - t0) * alive0).sum() * n_elem + ((alive0 & (s1 == 0)) * (e1 - e0 + 1)).sum())
+    lib.st_TrackJob_delete(job)
+    lib.st_Buffer_delete(pb)
+    lib.st_Buffer_delete(eb)
+    nbytes = parts.num_particles * 21 * 8
+    return {"value": pet / dt, "unit": METRIC, "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "ms_per_step": dt / steps * 1e3}
+
+
+# ------------------------------------------------------------------- main
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from sixtracklib_gb300 import lattices
+
+    from oracle.pyoracle import Oracle
+
+    ring = lattices.synthetic_ring()
+    parts = lattices.polar_grid_particles(args.particles)
+    orc = Oracle()
+    lat = ring.cbuffer.to_image()
+    n_elem = len(ring)
+    n = 8192
+    stride = max(1, parts.num_particles // n)
+    sample = parts.block[:, ::stride][:, :n].copy()
+    b = sample.copy()
+    turn = 0
+    for _ in range(args.warmup):
+        turn += 1
+        orc.track_until(lat, b, turn)
+    before = b.copy()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        turn += 1
+        orc.track_until(lat, b, turn)
+    dt = time.perf_counter() - t
+    s0 = before[20].view(np.int64) == 1
+    pet = int((((b[19].view(np.int64) - before[19].view(np.int64)) * s0).sum()) * n_elem
+              + ((s0 & (b[20].view(np.int64) == 0)) * (b[18].view(np.int64) + 1)).sum())
+    val = pet / dt
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_particles": n, "lattice_elements": n_elem},
+        "cpu_baseline": {"value": val, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{n} of the {args.particles} particles (strided), one turn "
+                                   "per step; the CPU restatement of the reference loop "
+                                   "(oracle/oracle.c) -- the reference's own build is "
+                                   "x86-only here"},
+        "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    from sixtracklib_gb300 import _native
+    from sixtracklib_gb300.device import DeviceTracker
+    from sixtracklib_gb300.roofline import lattice_flops_per_element
+
+    lib = _native.load()
+    ring, parts = make_workload(args.particles)
+    n_elem = len(ring)
+    trk = DeviceTracker(ring.cbuffer, config=f"mode={args.mode} threads_per_block={args.threads}")
+    cols = torch.from_numpy(parts.block.copy().view(np.int64)).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    turn = 0
+    for _ in range(args.warmup):
+        turn += 1
+        trk.launch_until(cols, turn)
+    assert trk.last_status() == 0, _native.last_error()
+    before = cols[17:].clone()
+    launches0 = lib.st_engine_kernel_launches()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev.index or 0) as clocks:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            turn += 1
+            evs[k][0].record(stream)
+            trk.launch_until(cols, turn)
+            evs[k][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    status = trk.last_status()
+    assert status == 0, f"track status {status}: {_native.last_error()}"
+    launches = lib.st_engine_kernel_launches() - launches0
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    kernel_s = [a.elapsed_time(b) / 1e3 for a, b in evs]
+    after = cols[17:]
+    b4 = torch.zeros(21, before.shape[1], dtype=torch.int64, device=dev)
+    b4[17:] = before
+    af = torch.zeros_like(b4)
+    af[17:] = after
+    pet = pet_between(b4, af, n_elem)
+    pet_total, t_max = pet, elapsed
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        pp = torch.tensor([float(pet)], device=dev, dtype=torch.float64)
+        dist.all_reduce(pp)
+        t_max = float(tt.item())
+        pet_total = float(pp.item())
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    value = pet_total / t_max
+    flops_per_pet = lattice_flops_per_element(ring.cbuffer)
+    pet_per_launch = pet / args.steps
+    avg_launch = float(np.mean(kernel_s))
+    achieved = pet_per_launch * flops_per_pet / avg_launch / 1e12
+    peak = lib.st_engine_measure_fp64_peak(dev.index or 0)
+    hbm_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except Exception:
+        pass
+    alg_bytes = args.particles * 21 * 8 + args.particles * 13 * 8  # read all, write mutable
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lattice and particles)",
+        "config": {"workload": WORKLOAD, "particles_per_gpu": args.particles,
+                   "lattice_elements": n_elem, "turns_per_step": 1, "mode": args.mode,
+                   "threads_per_block": args.threads,
+                   "l2": "inputs larger than L2: 168 MB particle columns per GPU",
+                   "parallelism": f"particles sharded, {world} independent GPU(s)"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak and peak > 0 else None, "traffic": None,
+                     "peak_source": "measured in-process: dense DFMA loop (csrc/probe.cu), "
+                                    "FMA = 2 flops",
+                     "flops_per_pet": flops_per_pet, "launch_ms": avg_launch * 1e3,
+                     "hbm_achieved_gbs": alg_bytes / avg_launch / 1e9,
+                     "hbm_peak_gbs": hbm_peak},
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(ring, parts, args.cpu_seconds)
+    if not args.no_e2e:
+        try:
+            line["e2e"] = e2e_measure(ring, parts, max(2, args.steps // 2), 1, args.mode,
+                                      args.threads)
+        except Exception as exc:  # report, do not hide
+            line["e2e"] = {"error": str(exc)}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

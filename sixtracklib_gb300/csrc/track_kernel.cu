@@ -346,7 +346,8 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
             const uint64_t *rec = bufs + (size_t)buf * cw;
             while (true) {
                 uint64_t const hdr = rec[0];
-                if ((uint32_t)(hdr & 0xFF) == OP_END) break;
+                uint32_t const nw = (uint32_t)((hdr >> 8) & 0xFFFFFF);
+                if ((uint32_t)(hdr & 0xFF) == OP_END || nw == 0) break;
                 if (part) {
                     if (prm.mode == MODE_EBE) {
                         int64_t const j = ebe_index(prm.ebe, p.pid, ae, p.at_turn);
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
                     }
                 }
                 ++ord;
-                rec += (hdr >> 8) & 0xFFFFFF;
+                rec += nw;
             }
             if (!resident) {
                 __syncthreads();  // every warp is done with this stage buffer

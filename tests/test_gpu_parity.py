@@ -1,0 +1,395 @@
+"""GPU parity: the CUDA tracking kernel against the oracle and the
+reference's fixtures, through the C ABI.
+
+Tolerances (the engine's contract):
+* integer columns (particle_id, at_element, at_turn, state) identical;
+* exact mode: bit-identical wherever no libm function is involved (drifts,
+  multipoles, shifts, rotations, apertures: + - * / sqrt are correctly rounded
+  on both sides); where sin/exp/pow enter (cavities, beam-beam, space charge)
+  within 1e-13 of the column scale per turn-block and 1e-10 after 1000 turns;
+* fast mode (explicit FMA): the same 1e-13 (1 turn) / 1e-10 (1000 turns).
+"Column scale" = max |value| of the oracle's column, so coordinates that
+cross zero are judged against their amplitude.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import EbeConfig
+from sixtracklib_gb300 import lattices
+from sixtracklib_gb300.beam_elements import Elements
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    return torch
+
+
+def run_device(torch, lattice, block, until=None, line=None, mode="exact"):
+    from sixtracklib_gb300.device import DeviceTracker
+
+    trk = DeviceTracker(lattice, config=f"mode={mode}")
+    cols = torch.from_numpy(block.copy().view(np.int64)).cuda()
+    if line is not None:
+        st = trk.track_line(cols, *line)
+    else:
+        st = trk.track_until(cols, until)
+    torch.cuda.synchronize()
+    return st, cols.cpu().numpy().view(np.uint64)
+
+
+def max_col_dev(got, exp):
+    g = got[:17].view(np.float64)
+    e = exp[:17].view(np.float64)
+    both_nan = np.isnan(g) & np.isnan(e)
+    scale = np.maximum(np.nanmax(np.abs(np.where(np.isfinite(e), e, 0)), axis=1, keepdims=True),
+                       1e-300)
+    d = np.where(both_nan, 0.0, np.abs(g - e) / scale)
+    return float(np.nanmax(d)) if d.size else 0.0
+
+
+def assert_parity(got, exp, tol, bit_exact=False):
+    assert np.array_equal(got[17:], exp[17:]), "particle ids / at_element / at_turn / state differ"
+    if bit_exact:
+        diff = np.nonzero((got != exp).any(axis=1))[0]
+        assert diff.size == 0, f"columns {diff} not bit-identical"
+    else:
+        dev = max_col_dev(got, exp)
+        assert dev <= tol, f"max deviation {dev:.3e} > {tol:.1e}"
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+# ----------------------------------------------------- reference fixtures
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("case", ["fodo", "synthetic", "bbsc", "bbsc_elliptic", "misc"])
+def test_reference_fixture_until(torch_cuda, case, mode):
+    d = load(f"ref_{case}.npz")
+    lat = d["lattice"] if "lattice" in d else lattices.synthetic_ring().cbuffer.to_image()
+    st, got = run_device(torch_cuda, lat, d["initial"], until=int(d["turns"]), mode=mode)
+    assert st == int(d["status"])
+    assert_parity(got, d["final"], tol=1e-12)
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+@pytest.mark.parametrize("case", ["fodo", "bbsc", "misc"])
+def test_reference_fixture_line(torch_cuda, case, mode):
+    d = load(f"ref_{case}.npz")
+    # the monitor in `misc` stores nothing here: the device path gets no output
+    lat = d["lattice"]
+    st, got = run_device(torch_cuda, lat, d["initial"], line=(3, 9, False), mode=mode)
+    assert st == int(d["line_status"])
+    assert_parity(got, d["line_final"], tol=1e-13)
+
+
+@pytest.mark.parametrize("case", ["fodo", "bbsc", "misc"])
+def test_reference_fixture_elem_by_elem_free_function(torch_cuda, case):
+    """st_Track_all_particles_element_by_element_until_turn with an explicit
+    config and generic-address outputs (track/track.h:672-777)."""
+    from tests import capi
+
+    d = load(f"ref_{case}.npz")
+    L = capi.lib()
+    lat = d["lattice"]
+    be = capi.c_buffer_from_image(lat)
+    blk = d["initial"].copy()
+    sp = capi.particles_view(blk)
+    cfg = capi.StElemByElemConfig(*[int(v) for v in d["ebe_cfg"]], 0)
+    out = np.zeros_like(d["ebe_out"])
+    ga = capi.generic_addr(out)
+    cfg.out_store_addr = C.addressof(ga)
+    # the misc lattice carries a BeamMonitor with a placeholder out_address:
+    # give it a real generic-address output (as the reference's test does)
+    mon_keep = None
+    if "ebe_monitor0" in d:
+        mon = np.zeros_like(d["ebe_monitor0"])
+        mga = capi.generic_addr(mon)
+        mon_keep = (mon, mga)
+        n = L.st_Buffer_get_num_of_objects(be)
+        for i in range(n):
+            o = C.cast(L.st_Buffer_get_const_object(be, i), C.POINTER(C.c_uint64))
+            if o[1] == 10:
+                m = C.cast(o[0], C.POINTER(C.c_uint64))
+                m[3] = C.addressof(mga)
+    st = L.st_Track_all_particles_element_by_element_until_turn(C.byref(sp), C.byref(cfg), be, 2)
+    L.st_Buffer_delete(be)
+    assert st == int(d["ebe_status"]), _err()
+    assert_parity(blk, d["ebe_final"], tol=1e-13)
+    assert_parity(out, d["ebe_out"], tol=1e-13)
+    if mon_keep is not None:
+        assert_parity(mon_keep[0], d["ebe_monitor0"], tol=1e-13)
+
+
+def _err():
+    from sixtracklib_gb300 import _native
+
+    return _native.last_error()
+
+
+# --------------------------------------------------------- exact-mode bits
+def test_exact_mode_bit_identical_without_libm(torch_cuda, oracle):
+    """20k-element ring without cavities: drifts, multipoles (order 1-10),
+    shifts, rotations, elliptic apertures; exact mode reproduces the
+    reference arithmetic bit for bit, losses included."""
+    e = lattices.synthetic_ring(n_cav=0)
+    lat = e.cbuffer.to_image()
+    p = lattices.polar_grid_particles(4096, seed=21)
+    exp = p.block.copy()
+    assert oracle.track_until(lat, exp, 3) == 0
+    st, got = run_device(torch_cuda, lat, p.block, until=3, mode="exact")
+    assert st == 0
+    assert_parity(got, exp, 0.0, bit_exact=True)
+    lost = int((exp[20].view(np.int64) == 0).sum())
+    assert 0 < lost < 4096
+
+
+def test_exact_mode_bit_identical_line_and_misc(torch_cuda, oracle):
+    e = Elements()
+    for _ in range(20):
+        e.Drift(length=1.3)
+        e.DriftExact(length=0.7)
+        e.Multipole(knl=[1e-5, 0.01, 0.02, 0.3], ksl=[0.0, 1e-4], hxl=1e-6, length=1.0)
+        e.SRotation(angle=3.0)
+        e.XYShift(dx=1e-5, dy=-2e-5)
+        e.DipoleEdge(r21=1e-3, r43=-1e-3)
+        e.Multipole(knl=[0.0, -0.01])
+        e.LimitRectEllipse(max_x=0.02, max_y=0.015, a=0.025, b=0.02)
+        e.LimitRect(min_x=-0.019, max_x=0.02, min_y=-0.02, max_y=0.014)
+    lat = e.cbuffer.to_image()
+    p = lattices.gaussian_particles(3000, seed=3, sx=4e-3, sy=4e-3, spx=1e-4, spy=1e-4)
+    for args in ((0, len(e), True), (17, 93, False)):
+        exp = p.block.copy()
+        st0 = oracle.track_line(lat, exp, *args)
+        st, got = run_device(torch_cuda, lat, p.block, line=args, mode="exact")
+        assert st == st0
+        assert_parity(got, exp, 0.0, bit_exact=True)
+    exp = p.block.copy()
+    oracle.track_until(lat, exp, 25)
+    st, got = run_device(torch_cuda, lat, p.block, until=25, mode="exact")
+    assert_parity(got, exp, 0.0, bit_exact=True)
+
+
+# ------------------------------------------------------ long-run tolerance
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_fodo_ring_10k_particles_1000_turns(torch_cuda, oracle, mode):
+    """The plain FODO ring at full size (10,000 protons, 1000 turns):
+    regular orbits within 1e-10, identical loss flags / turn counters."""
+    lat = lattices.fodo_ring().cbuffer.to_image()
+    p = lattices.gaussian_particles(10_000, seed=2024)
+    exp = p.block.copy()
+    assert oracle.track_until(lat, exp, 1000) == 0
+    st, got = run_device(torch_cuda, lat, p.block, until=1000, mode=mode)
+    assert st == 0
+    assert_parity(got, exp, tol=1e-10)
+    # one turn: 1e-13
+    exp1 = p.block.copy()
+    oracle.track_until(lat, exp1, 1)
+    st, got1 = run_device(torch_cuda, lat, p.block, until=1, mode=mode)
+    assert_parity(got1, exp1, tol=1e-13)
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_synthetic_ring_sample(torch_cuda, oracle, mode):
+    lat = lattices.synthetic_ring().cbuffer.to_image()
+    p = lattices.polar_grid_particles(2048, seed=5)
+    exp = p.block.copy()
+    oracle.track_until(lat, exp, 5)
+    st, got = run_device(torch_cuda, lat, p.block, until=5, mode=mode)
+    assert st == 0
+    assert_parity(got, exp, tol=1e-12)
+
+
+@pytest.mark.parametrize("elliptic", [False, True])
+def test_beam_beam_space_charge_ring(torch_cuda, oracle, elliptic):
+    lat = lattices.bb_sc_ring(elliptic=elliptic).cbuffer.to_image()
+    p = lattices.gaussian_particles(1024, seed=17, sx=2e-5, sy=2e-5)
+    exp = p.block.copy()
+    oracle.track_until(lat, exp, 20)
+    for mode in ("exact", "fast"):
+        st, got = run_device(torch_cuda, lat, p.block, until=20, mode=mode)
+        assert st == 0
+        assert_parity(got, exp, tol=1e-12)
+
+
+# ------------------------------------------------------------ edge cases
+def test_edge_cases(torch_cuda, oracle):
+    e = Elements()
+    e.Drift(length=1.0)
+    e.LimitRect(min_x=-0.01, max_x=0.01, min_y=-0.01, max_y=0.01)
+    e.Drift(length=0.0)
+    lat = e.cbuffer.to_image()
+    p = lattices.gaussian_particles(300, seed=4)
+    p.x[:8] = [0.01, -0.01, 0.0100000000001, 1.0, -1.0, 0.99999999, np.nan, np.inf]
+    p.px[:8] = 0.0
+    p.state[8:12] = 0
+    p.at_turn[12:20] = [1, 2, 3, 5, 7, 9, 0, 4]
+    p.at_element[20:30] = 7
+    for until in (0, 1, 5):
+        exp = p.block.copy()
+        s0 = oracle.track_until(lat, exp, until)
+        st, got = run_device(torch_cuda, lat, p.block, until=until)
+        assert st == s0
+        assert_parity(got, exp, 0.0, bit_exact=True)
+    for tid in (777, 261, 260):
+        e2 = Elements()
+        e2.Drift(length=1.0)
+        e2.cbuffer.add_object(tid, np.zeros(3, np.uint64))
+        e2.Drift(length=1.0)
+        lat2 = e2.cbuffer.to_image()
+        exp = p.block.copy()
+        s0 = oracle.track_until(lat2, exp, 3)
+        st, got = run_device(torch_cuda, lat2, p.block, until=3)
+        assert st == s0 == -1
+        assert_parity(got, exp, 0.0, bit_exact=True)
+        exp = p.block.copy()
+        s0 = oracle.track_line(lat2, exp, 0, 3, True)
+        st, got = run_device(torch_cuda, lat2, p.block, line=(0, 3, True))
+        assert st == s0
+        assert_parity(got, exp, 0.0, bit_exact=True)
+
+
+def test_empty_lattice_and_no_particles(torch_cuda):
+    from sixtracklib_gb300 import CBuffer
+
+    empty = CBuffer().to_image()
+    p = lattices.gaussian_particles(10)
+    st, got = run_device(torch_cuda, empty, p.block, until=3)
+    assert st == -1
+    assert np.array_equal(got, p.block)
+    lat = lattices.fodo_ring().cbuffer.to_image()
+    st, _ = run_device(torch_cuda, lat, np.zeros((21, 0), np.uint64), until=3)
+    assert st == 0
+
+
+# ------------------------------------------------ full-size properties
+def test_full_size_config_properties(torch_cuda, oracle):
+    """1M particles on the 20k-element ring (the benchmark workload):
+    (a) 2 turns in one call == 2 calls of 1 turn, bit for bit;
+    (b) the result of a particle does not depend on its slot;
+    (c) a strided sample of 1024 particles agrees with the oracle."""
+    torch = torch_cuda
+    from sixtracklib_gb300.device import DeviceTracker
+
+    e = lattices.synthetic_ring()
+    trk = DeviceTracker(e.cbuffer, config="mode=fast")
+    p = lattices.polar_grid_particles(1_000_000)
+    base = torch.from_numpy(p.block.copy().view(np.int64)).cuda()
+    a = base.clone()
+    assert trk.track_until(a, 2) == 0
+    b = base.clone()
+    assert trk.track_until(b, 1) == 0
+    assert trk.track_until(b, 2) == 0
+    assert torch.equal(a, b)
+    perm = torch.randperm(base.shape[1], device=base.device)
+    c = base[:, perm].contiguous()
+    assert trk.track_until(c, 2) == 0
+    assert torch.equal(c, a[:, perm])
+    idx = np.arange(0, 1_000_000, 977)[:1024]
+    sample = p.block[:, idx].copy()
+    oracle.track_until(e.cbuffer.to_image(), sample, 2)
+    got = a.cpu().numpy().view(np.uint64)[:, idx]
+    assert_parity(got, sample, tol=1e-12)
+
+
+def test_trackjob_until_line_collect(torch_cuda, oracle):
+    """Python TrackJob over the C ABI (python/sixtracklib/trackjob.py)."""
+    from sixtracklib_gb300 import ParticlesSet
+    from sixtracklib_gb300.trackjob import TrackJob
+
+    e = lattices.fodo_ring()
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=500)
+    q = lattices.gaussian_particles(500, seed=8)
+    p.set_block(q.block)
+    job = TrackJob(e, ps, config_str="mode=exact")
+    job.track_until(20)
+    job.collect_particles()
+    exp = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp, 20)
+    assert_parity(p.block.copy(), exp, tol=1e-13)
+    job.track_line(0, 100, False)
+    job.collect()
+    oracle.track_line(e.cbuffer.to_image(), exp, 0, 100, False)
+    assert_parity(p.block.copy(), exp, tol=1e-13)
+    with pytest.raises(RuntimeError):
+        TrackJob(e, ps, arch="opencl")
+
+
+def test_trackjob_beam_monitor_and_elem_by_elem_output(torch_cuda, oracle):
+    """Output buffer: elem-by-elem store first, then one Particles object per
+    BeamMonitor (output/output_buffer.c:288-360)."""
+    from sixtracklib_gb300 import ParticlesSet
+    from sixtracklib_gb300.trackjob import TrackJob
+
+    e = lattices.fodo_ring()
+    e.BeamMonitor(num_stores=5, start=0, skip=2, is_rolling=1, is_turn_ordered=1)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=64)
+    q = lattices.gaussian_particles(64, seed=12)
+    p.set_block(q.block)
+    job = TrackJob(e, ps, until_turn_elem_by_elem=2, config_str="mode=exact")
+    assert job.has_elem_by_elem_output and job.has_beam_monitor_output
+    assert job.elem_by_elem_output_offset == 0 and job.beam_monitor_output_offset == 1
+    job.track_elem_by_elem(2)
+    job.track_until(12)
+    job.collect()
+    out = job.output
+    ebe = out.get_object(0).block.copy()
+    mon = out.get_object(1).block.copy()
+    # oracle with the same configuration
+    lat = job.beam_elements_buffer.to_image()
+    ne = len(e)
+    cfg = EbeConfig(0, 64, ne, 2, 0, 0, 0, 63, ne - 1, 1, 1)
+    exp = q.block.copy()
+    exp_ebe = np.zeros_like(ebe)
+    lat_mon = e.cbuffer.objects[-1].words.copy()
+    # enable the monitor's store in the oracle's copy of the lattice
+    from sixtracklib_gb300 import CBuffer
+
+    cb = CBuffer.from_image(lat)
+    cb.objects[-1].words[3] = 1
+    cb.objects[-1].words[4] = 63
+    cb.objects[-1].words[5] = 0
+    del lat_mon
+    img = cb.to_image()
+    exp_mon = np.zeros_like(mon)
+    oracle.track_elem_by_elem(img, exp, cfg, exp_ebe, 2, monitors=[exp_mon])
+    oracle.track_until(img, exp, 12, monitors=[exp_mon])
+    assert_parity(p.block.copy(), exp, tol=1e-13)
+    assert_parity(ebe, exp_ebe, tol=1e-13)
+    assert_parity(mon, exp_mon, tol=1e-13)
+
+
+def test_free_function_until_single_and_all(torch_cuda, oracle):
+    from tests import capi
+
+    L = capi.lib()
+    e = lattices.fodo_ring()
+    lat = e.cbuffer.to_image()
+    be = capi.c_buffer_from_image(lat)
+    q = lattices.gaussian_particles(256, seed=31)
+    blk = q.block.copy()
+    sp = capi.particles_view(blk)
+    assert L.st_Track_all_particles_until_turn(C.byref(sp), be, 7) == 0, _err()
+    exp = q.block.copy()
+    oracle.track_until(lat, exp, 7)
+    assert_parity(blk, exp, tol=1e-13)
+    blk2 = q.block.copy()
+    sp2 = capi.particles_view(blk2)
+    assert L.st_Track_particle_until_turn(C.byref(sp2), 5, be, 7) == 0
+    exp2 = q.block.copy()
+    oracle.track_until(lat, exp2, 7, i0=5, i1=6)
+    assert_parity(blk2, exp2, tol=1e-13)
+    L.st_Buffer_delete(be)
