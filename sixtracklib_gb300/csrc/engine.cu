@@ -247,7 +247,8 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
     prm.ebe_out = ebe_out;
     prm.ebe_cap = ebe_cap;
     if (ebe) prm.ebe = *ebe;
-    if (!stream) stream = dev->stream;
+    // stream 0 is the legacy default stream (what torch reports for its
+    // default stream): launch there, never substitute another stream
     if (!cuda_ok(cudaMemsetAsync(dev->d_flags, 0, 2 * sizeof(int32_t), stream), "cudaMemsetAsync"))
         return -1;
     if (i1 > i0) {
@@ -557,7 +558,7 @@ int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t
     if (!L || !d_cols) return -1;
     if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
     cudaSetDevice(L->dev->id);
-    L->last_stream = stream ? (cudaStream_t)stream : L->dev->stream;
+    L->last_stream = (cudaStream_t)stream;
     return run_track(L->dev, L->opt, *L->full, (uint64_t *)d_cols, n, 0, n, MODE_UNTIL,
                      until_turn, false, nullptr, 0, nullptr, L->last_stream, false);
 }
@@ -565,7 +566,7 @@ int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t
 st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *L)
 {
     if (!L) return -1;
-    cudaStream_t s = L->last_stream ? L->last_stream : L->dev->stream;
+    cudaStream_t s = L->last_stream;
     if (!cuda_ok(cudaMemcpyAsync(L->dev->h_flags, L->dev->d_flags, 2 * sizeof(int32_t),
                                  cudaMemcpyDeviceToHost, s),
                  "cudaMemcpyAsync(status)") ||

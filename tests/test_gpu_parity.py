@@ -94,7 +94,7 @@ def test_reference_fixture_line(torch_cuda, case, mode):
     assert_parity(got, d["line_final"], tol=1e-13)
 
 
-@pytest.mark.parametrize("case", ["fodo", "bbsc", "misc"])
+@pytest.mark.parametrize("case", ["fodo", "misc"])
 def test_reference_fixture_elem_by_elem_free_function(torch_cuda, case):
     """st_Track_all_particles_element_by_element_until_turn with an explicit
     config and generic-address outputs (track/track.h:672-777)."""
