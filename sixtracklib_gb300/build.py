@@ -27,6 +27,7 @@ CUDA_SOURCES = {
     "track_kernel.cu": ["-fmad=false"],
     "engine.cu": [],
     "probe.cu": [],
+    "compact.cu": [],
 }
 
 

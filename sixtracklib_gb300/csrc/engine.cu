@@ -125,7 +125,7 @@ static bool parse_options(const char *cfg, Options *o, std::string *err)
         }
     }
     if (o->threads < 32 || o->threads > kMaxThreads || o->threads % 32 != 0) {
-        if (err) *err = "config: threads_per_block must be a multiple of 32 in [32, 512]";
+        if (err) *err = "config: threads_per_block must be a multiple of 32 in [32, 256]";
         return false;
     }
     if (o->stages < 2 || o->stages > 8) {
@@ -145,6 +145,9 @@ struct Device {
     cudaStream_t stream = nullptr;
     int32_t *d_flags = nullptr;  // [0] status, [1] error
     int32_t *h_flags = nullptr;  // pinned
+    // scratch for the active-particle selection (grown on demand, kept)
+    uint64_t *scratch = nullptr;
+    int64_t scratch_words = 0;
 };
 
 static std::mutex g_dev_mu;
@@ -188,7 +191,8 @@ static Device *get_device(int id)
 // ------------------------------------------------------- device stream
 struct DevStream {
     CompiledStream cs;
-    uint64_t *d = nullptr;
+    uint64_t *d = nullptr;        // chunked stream, then the s table
+    const double *s_table = nullptr;
     int device = -1;
     DevStream() = default;
     DevStream(const DevStream &) = delete;
@@ -212,11 +216,16 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
         return nullptr;
     }
     size_t const bytes = s->cs.words.size() * 8;
+    size_t const sbytes = s->cs.s_table.size() * 8;
     if (!cuda_ok(cudaSetDevice(dev->id), "cudaSetDevice") ||
-        !cuda_ok(cudaMalloc(&s->d, bytes), "cudaMalloc(lattice)") ||
+        !cuda_ok(cudaMalloc(&s->d, bytes + sbytes), "cudaMalloc(lattice)") ||
         !cuda_ok(cudaMemcpy(s->d, s->cs.words.data(), bytes, cudaMemcpyHostToDevice),
-                 "cudaMemcpy(lattice)"))
+                 "cudaMemcpy(lattice)") ||
+        !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + bytes, s->cs.s_table.data(), sbytes,
+                            cudaMemcpyHostToDevice),
+                 "cudaMemcpy(s table)"))
         return nullptr;
+    s->s_table = reinterpret_cast<const double *>(reinterpret_cast<char *>(s->d) + bytes);
     s->device = dev->id;
     return s;
 }
@@ -246,11 +255,35 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
     prm.error = dev->d_flags + 1;
     prm.ebe_out = ebe_out;
     prm.ebe_cap = ebe_cap;
+    prm.s_table = ds.s_table;
     if (ebe) prm.ebe = *ebe;
     // stream 0 is the legacy default stream (what torch reports for its
     // default stream): launch there, never substitute another stream
     if (!cuda_ok(cudaMemsetAsync(dev->d_flags, 0, 2 * sizeof(int32_t), stream), "cudaMemsetAsync"))
         return -1;
+    if (i1 > i0 && mode != MODE_EBE) {
+        // pack the particles that have work left so warps hold live lanes only
+        int64_t const need = select_scratch_words(i1 - i0);
+        if (need > dev->scratch_words) {
+            if (dev->scratch) cudaFree(dev->scratch);
+            dev->scratch = nullptr;
+            dev->scratch_words = 0;
+            if (!cuda_ok(cudaMalloc(&dev->scratch, (size_t)need * 8), "cudaMalloc(scratch)"))
+                return -1;
+            dev->scratch_words = need;
+        }
+        int64_t *idx = nullptr, *count = nullptr;
+        int const rs = launch_select(d_cols, n, i0, i1, mode, until_turn, dev->scratch, &idx,
+                                     &count, stream);
+        if (rs != 0) {
+            set_error(std::string("particle selection launch: ") +
+                      cudaGetErrorString((cudaError_t)rs));
+            return -1;
+        }
+        g_launches.fetch_add(3);
+        prm.idx = idx;
+        prm.count = count;
+    }
     if (i1 > i0) {
         int const rc = launch_track(prm, opt.fast, opt.threads, stream);
         if (rc != 0) {
@@ -526,6 +559,7 @@ int64_t st_DeviceLattice_num_chunks(const st_DeviceLattice *L)
 st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols, int64_t n,
                                                int64_t until_turn, void *stream)
 {
+    if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
     if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
     cudaSetDevice(L->dev->id);
@@ -536,6 +570,7 @@ st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols
 st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *L, void *d_cols, int64_t n,
                                               uint64_t b, uint64_t e, bool finish, void *stream)
 {
+    if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
     auto key = std::make_pair(b, e);
     auto it = L->lines.find(key);
@@ -555,6 +590,7 @@ st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *L, void *d_cols,
 int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t n,
                                       int64_t until_turn, void *stream)
 {
+    if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
     if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
     cudaSetDevice(L->dev->id);

@@ -5,7 +5,7 @@
 
 namespace stg {
 
-constexpr int kMaxThreads = 512;  // largest block the kernels are built for
+constexpr int kMaxThreads = 256;  // largest block the kernels are built for
 constexpr int kDefaultStages = 4;
 
 enum TrackMode : int32_t { MODE_UNTIL = 0, MODE_LINE = 1, MODE_EBE = 2 };
@@ -39,11 +39,21 @@ struct TrackParams {
     uint64_t *ebe_out;       // device: elem-by-elem column block
     int64_t ebe_cap;
     EbeDevConfig ebe;
+    const int64_t *idx;      // device: particle indices to track (null: i0..i1)
+    const int64_t *count;    // device: number of entries of idx
+    const double *s_table;   // device: s before element k when a turn starts at s = 0
 };
 
 // Launch one tracking kernel on `stream` (a cudaStream_t).  Returns the CUDA
 // error code of the launch (0 on success).
 int launch_track(const TrackParams &prm, bool fast, int threads, void *stream);
 size_t track_smem_bytes(int stages, int chunk_words);
+
+// Stable selection of the particles with work left (compact.cu): fills
+// idx / count inside `scratch` (select_scratch_words(i1 - i0) words).
+int64_t select_scratch_words(int64_t count);
+int launch_select(const uint64_t *cols, int64_t n, int64_t i0, int64_t i1, int mode,
+                  int64_t until, uint64_t *scratch, int64_t **idx_out, int64_t **count_out,
+                  void *stream);
 
 }  // namespace stg

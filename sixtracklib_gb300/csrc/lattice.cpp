@@ -45,6 +45,7 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
     if (begin > end || end > img.num_objects) return bad(err, end, "line range outside the lattice");
     Emitter em;
     out->monitor_elements.clear();
+    out->s_table.assign(1, 0.0);
     uint32_t op_mask = 0;
     for (uint64_t i = begin; i < end; ++i) {
         uint64_t const t = img.type_of(i);
@@ -64,6 +65,7 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                             (opt.aperture_mode == 1 && L >= opt.aperture_min_length);
             aux = ap ? DRIFT_APERTURE : 0u;
             p = {d(0)};
+            if (op == OP_DRIFT) p.push_back(d2w(0.5 * L));
             break;
         }
         case ST_OBJECT_TYPE_MULTIPOLE: {
@@ -111,6 +113,11 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             if (!need(3)) return bad(err, i, "truncated limit_ellipse");
             op = OP_LIMIT_ELLIPSE;
             p.assign(w, w + 3);
+            // the kernel compares t = x^2 b^2 + y^2 a^2 <= a^2 b^2 as integers
+            // when all three are non-negative (then t >= +0 or NaN)
+            if (std::signbit(w2d(w[0])) || std::signbit(w2d(w[1])) || std::signbit(w2d(w[2])) ||
+                std::isnan(w2d(w[2])))
+                aux = 1u;
             break;
         case ST_OBJECT_TYPE_LIMIT_RECT_ELLIPSE:
             if (!need(5)) return bad(err, i, "truncated limit_rect_ellipse");
@@ -205,6 +212,9 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
         }
         op_mask |= 1u << op;
         em.push(op, aux, p);
+        double s_next = out->s_table.back();
+        if (t == ST_OBJECT_TYPE_DRIFT || t == ST_OBJECT_TYPE_DRIFT_EXACT) s_next += w2d(w[0]);
+        out->s_table.push_back(s_next);
     }
     // chunking
     uint64_t maxrec = 1;

@@ -26,6 +26,10 @@ struct CompiledStream {
     std::vector<uint64_t> words;  // num_chunks * chunk_words
     StreamInfo info;
     std::vector<uint64_t> monitor_elements;  // element indices of monitors
+    // s_table[k] = s before element k for a turn that starts at s = +0:
+    // the drift lengths summed in lattice order, in double, exactly as the
+    // tracking loop accumulates them (num_elements + 1 entries).
+    std::vector<double> s_table;
 };
 
 // Compile elements [begin, end) of the image.  Returns false (and sets the

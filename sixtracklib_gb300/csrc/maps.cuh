@@ -21,7 +21,9 @@ namespace stg {
 struct PState {
     double x, px, y, py, zeta, delta, psigma, rpp, rvv, chi, s;
     double beta0, q0, p0c, mass0, charge_ratio, gamma0, energy0;
+    double rvv_m1;  // rvv - 1 (exact for rvv in [1/2, 2]); the fast drift's zeta term
     int64_t pid, at_element, at_turn, state;
+    bool lazy_s;    // s is +0 at this turn's start: s is read from the lattice's s table
 };
 
 __device__ __forceinline__ double W(uint64_t w) { return __longlong_as_double((long long)w); }
@@ -50,6 +52,7 @@ __device__ __forceinline__ void add_energy(PState &p, double de)
     p.zeta *= rvv / p.rvv;
     p.rvv = rvv;
     p.rpp = 1.0 / opd;
+    p.rvv_m1 = rvv - 1.0;
 }
 
 // NS(Particles_update_delta_value): particles.h:5459-5496
@@ -63,29 +66,31 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
     p.rvv = opd / (1.0 + ptau_beta0);
     p.rpp = 1.0 / opd;
     p.psigma = ptau_beta0 / (beta0 * beta0);
+    p.rvv_m1 = p.rvv - 1.0;
 }
 
 // ------------------------------------------------------------------- maps
-// be_drift/track.h:45-67
+// be_drift/track.h:45-67.  FAST: zeta += L (rvv - 1) - (L/2)(xp^2 + yp^2), i.e.
+// the reference's L (rvv - (1 + (xp^2 + yp^2)/2)) regrouped into two fused
+// multiply-adds with rvv - 1 kept per particle.  s is only accumulated when
+// the turn did not start at s = +0 (otherwise it comes from the s table).
 template <bool FAST>
-__device__ __forceinline__ void drift(PState &p, double L)
+__device__ __forceinline__ void drift(PState &p, double L, double half_L)
 {
     double const xp = p.px * p.rpp;
     double const yp = p.py * p.rpp;
     if (FAST) {
         double const t = fma(yp, yp, xp * xp);
-        double const u = fma(t, 0.5, 1.0);
         p.x = fma(xp, L, p.x);
         p.y = fma(yp, L, p.y);
-        p.s += L;
-        p.zeta = fma(L, p.rvv - u, p.zeta);
+        p.zeta = fma(-half_L, t, fma(L, p.rvv_m1, p.zeta));
     } else {
         double const dzeta = p.rvv - (1.0 + (xp * xp + yp * yp) * 0.5);
         p.x += xp * L;
         p.y += yp * L;
-        p.s += L;
         p.zeta += L * dzeta;
     }
+    if (!p.lazy_s) p.s += L;
 }
 
 // be_drift/track.h:71-97
@@ -96,7 +101,7 @@ __device__ __forceinline__ void drift_exact(PState &p, double L)
     double const dzeta = p.rvv * L - opd * lpzi;
     p.x += p.px * lpzi;
     p.y += p.py * lpzi;
-    p.s += L;
+    if (!p.lazy_s) p.s += L;
     p.zeta += dzeta;
 }
 
@@ -197,15 +202,24 @@ __device__ __forceinline__ bool inside_rect(const PState &p, const uint64_t *rec
     return (p.x >= W(rec[1])) && (p.x <= W(rec[2])) && (p.y >= W(rec[3])) && (p.y <= W(rec[4]));
 }
 
-// be_limit/track.h:113-137
-__device__ __forceinline__ bool inside_ellipse(const PState &p, const uint64_t *rec)
+// be_limit/track.h:113-137.  t <= a^2 b^2 is compared on the integer pipe
+// (both sides are >= +0 or NaN; NaN fails as in the float compare) unless
+// the element has negative parameters (aux bit 0).
+template <bool FAST>
+__device__ __forceinline__ bool inside_ellipse(const PState &p, const uint64_t *rec, uint32_t aux)
 {
-    double t = p.x * p.x;
-    t *= W(rec[2]);
-    double ys = p.y * p.y;
-    ys *= W(rec[1]);
-    t += ys;
-    return t <= W(rec[3]);
+    double t;
+    if (FAST) {
+        t = fma(p.y * p.y, W(rec[1]), (p.x * p.x) * W(rec[2]));
+    } else {
+        t = p.x * p.x;
+        t *= W(rec[2]);
+        double ys = p.y * p.y;
+        ys *= W(rec[1]);
+        t += ys;
+    }
+    if (aux & 1u) return t <= W(rec[3]);
+    return (uint64_t)__double_as_longlong(t) <= rec[3];
 }
 
 // be_limit/track.h:139-162

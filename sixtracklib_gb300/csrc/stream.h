@@ -15,7 +15,7 @@ namespace stg {
 
 enum Op : uint32_t {
     OP_END = 0,             // end of chunk
-    OP_DRIFT = 1,           // [L]            aux bit0: global aperture check
+    OP_DRIFT = 1,           // [L, L/2]       aux bit0: global aperture check
     OP_DRIFT_EXACT = 2,     // [L]            aux bit0: global aperture check
     OP_MULTIPOLE = 3,       // [bal 0..2n+1]  aux = order n
     OP_MULTIPOLE_CURV = 4,  // [bal..., hxl, hyl, length]  aux = order n
@@ -23,7 +23,7 @@ enum Op : uint32_t {
     OP_XYSHIFT = 6,         // [-dx, -dy]
     OP_SROTATION = 7,       // [cos_z, sin_z]
     OP_LIMIT_RECT = 8,      // [min_x, max_x, min_y, max_y]
-    OP_LIMIT_ELLIPSE = 9,   // [a_squ, b_squ, a_b_squ]
+    OP_LIMIT_ELLIPSE = 9,   // [a_squ, b_squ, a_b_squ]  aux bit0: compare as floats
     OP_LIMIT_RECT_ELLIPSE = 10,  // [max_x, max_y, a_squ, b_squ, a_squ_b_squ]
     OP_DIPEDGE = 11,        // [r21, r43]
     OP_RF_MULTIPOLE = 12,   // [voltage, frequency, lag, bal..., phase...] aux = order

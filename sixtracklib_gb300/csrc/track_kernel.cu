@@ -107,11 +107,14 @@ __device__ __forceinline__ void load_particle(PState &p, const uint64_t *cols, i
     p.at_turn = k[19 * n + i];
     p.state = k[20 * n + i];
     p.energy0 = sqrt(p.p0c * p.p0c + p.mass0 * p.mass0);
+    p.rvv_m1 = p.rvv - 1.0;
+    p.lazy_s = false;
 }
 
 // Write one full record (21 columns) to a column block of capacity cap.
 __device__ __forceinline__ void store_record(const PState &p, uint64_t *out, int64_t cap,
-                                             int64_t j, int64_t at_element, int64_t at_turn)
+                                             int64_t j, int64_t at_element, int64_t at_turn,
+                                             double s)
 {
     double *d = reinterpret_cast<double *>(out);
     int64_t *k = reinterpret_cast<int64_t *>(out);
@@ -120,7 +123,7 @@ __device__ __forceinline__ void store_record(const PState &p, uint64_t *out, int
     d[2 * cap + j] = p.beta0;
     d[3 * cap + j] = p.gamma0;
     d[4 * cap + j] = p.p0c;
-    d[5 * cap + j] = p.s;
+    d[5 * cap + j] = s;
     d[6 * cap + j] = p.x;
     d[7 * cap + j] = p.y;
     d[8 * cap + j] = p.px;
@@ -181,13 +184,14 @@ __device__ __forceinline__ int64_t ebe_index(const EbeDevConfig &c, int64_t pid,
 // the particle leaves the aperture (state becomes 0).
 template <bool FAST>
 __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hdr,
-                                     const TrackParams &prm, int64_t cur_elem, int64_t cur_turn)
+                                     const TrackParams &prm, int64_t cur_elem, int64_t cur_turn,
+                                     int64_t ord)
 {
     uint32_t const op = (uint32_t)(hdr & 0xFF);
     uint32_t const aux = (uint32_t)(hdr >> 32);
     switch (op) {
     case OP_DRIFT:
-        drift<FAST>(p, W(rec[1]));
+        drift<FAST>(p, W(rec[1]), W(rec[2]));
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_MULTIPOLE:
@@ -201,7 +205,7 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         p.y += W(rec[2]);
         return 0;
     case OP_LIMIT_ELLIPSE:
-        p.state &= (int64_t)inside_ellipse(p, rec);
+        p.state &= (int64_t)inside_ellipse<FAST>(p, rec, aux);
         return 0;
     case OP_CAVITY:
         cavity(p, rec);
@@ -247,7 +251,8 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
             p.state = 0;
             return -1;
         }
-        store_record(p, out, (int64_t)rec[9], j, cur_elem, cur_turn);
+        store_record(p, out, (int64_t)rec[9], j, cur_elem, cur_turn,
+                     p.lazy_s ? prm.s_table[ord] : p.s);
         return 0;
     }
     case OP_NOP:
@@ -275,10 +280,22 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
     uint64_t *bufs = smem + 16;            // stages * cw words
     __shared__ long long s_tmin;
 
-    int64_t const i = prm.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool const valid = i < prm.i1;
+    int64_t const t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i;
+    bool valid;
+    if (prm.idx) {  // compacted launch: only the particles with work left
+        valid = t < *prm.count;
+        i = valid ? prm.idx[t] : 0;
+    } else {
+        i = prm.i0 + t;
+        valid = i < prm.i1;
+    }
     PState p;
-    if (valid) load_particle(p, prm.cols, prm.n, i);
+    if (valid) {
+        load_particle(p, prm.cols, prm.n, i);
+        // s of a turn that starts at +0 comes from the lattice's s table
+        p.lazy_s = (prm.mode != MODE_LINE) && (__double_as_longlong(p.s) == 0);
+    }
 
     // ---------------------------------------------------- per-mode setup
     int64_t const start_elem = valid ? p.at_element : 0;
@@ -293,6 +310,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
     }
     int status = 0;
     int64_t stop_elem = -1;  // element ordinal where tracking stopped
+    bool const started = active;
 
     if (threadIdx.x == 0) {
         s_tmin = 0x7FFFFFFFFFFFFFFFll;
@@ -352,14 +370,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
                     if (prm.mode == MODE_EBE) {
                         int64_t const j = ebe_index(prm.ebe, p.pid, ae, p.at_turn);
                         if (j >= 0 && j < prm.ebe_cap)
-                            store_record(p, prm.ebe_out, prm.ebe_cap, j, ae, p.at_turn);
+                            store_record(p, prm.ebe_out, prm.ebe_cap, j, ae, p.at_turn,
+                                         p.lazy_s ? prm.s_table[ord] : p.s);
                     }
-                    int const rc = apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn);
+                    int const rc =
+                        apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn, ord);
                     if (rc != 0 || p.state != 1) {
                         status |= rc;
                         part = false;
                         active = false;
                         stop_elem = ord;
+                        if (p.lazy_s) p.s = prm.s_table[ord + 1];
                     } else {
                         ++ae;
                     }
@@ -390,6 +411,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
         } else if (part) {  // turn completed
             p.at_turn += 1;
             p.s = 0.0;
+            p.lazy_s = true;
             if (p.at_turn >= prm.until_turn) active = false;
         }
         ++turn;
@@ -421,9 +443,11 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
             p.at_element = start_elem + stop_elem;
         }
     } else if (prm.mode == MODE_LINE) {
-        int64_t const done = (stop_elem >= 0) ? stop_elem : prm.num_elements;
-        p.at_element = start_elem + done;
-        if (stop_elem < 0 && prm.finish_turn && p.state == 1) p.at_element = 0;
+        if (started) {  // particles lost before the call are left as they are
+            int64_t const done = (stop_elem >= 0) ? stop_elem : prm.num_elements;
+            p.at_element = start_elem + done;
+            if (stop_elem < 0 && prm.finish_turn && p.state == 1) p.at_element = 0;
+        }
     } else {  // EBE
         if (stop_elem >= 0) p.at_element = start_elem + stop_elem;
     }
