@@ -42,6 +42,7 @@ struct Options {
     double x_limit = 1.0, y_limit = 1.0;
     int stages = kDefaultStages;
     int chunk_words = 1024;
+    int blocks_per_sm = 1;
 };
 
 static std::string trim(const std::string &s)
@@ -114,6 +115,8 @@ static bool parse_options(const char *cfg, Options *o, std::string *err)
                     o->stages = std::stoi(v);
                 } else if (k == "chunk_words") {
                     o->chunk_words = std::stoi(v);
+                } else if (k == "blocks_per_sm") {
+                    o->blocks_per_sm = std::stoi(v);
                 } else {
                     if (err) *err = "config: unknown key '" + k + "'";
                     return false;
@@ -285,7 +288,7 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
         prm.count = count;
     }
     if (i1 > i0) {
-        int const rc = launch_track(prm, opt.fast, opt.threads, stream);
+        int const rc = launch_track(prm, opt.fast, opt.threads, opt.blocks_per_sm, stream);
         if (rc != 0) {
             set_error(std::string("track kernel launch: ") + cudaGetErrorString((cudaError_t)rc));
             return -1;

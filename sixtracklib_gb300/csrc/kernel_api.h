@@ -46,7 +46,10 @@ struct TrackParams {
 
 // Launch one tracking kernel on `stream` (a cudaStream_t).  Returns the CUDA
 // error code of the launch (0 on success).
-int launch_track(const TrackParams &prm, bool fast, int threads, void *stream);
+// blocks_per_sm selects the register tier: 1 (up to 255 registers, no
+// spills) or 2 (at most 128 registers per thread, two CTAs per SM).
+int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_sm,
+                 void *stream);
 size_t track_smem_bytes(int stages, int chunk_words);
 
 // Stable selection of the particles with work left (compact.cu): fills

@@ -65,7 +65,6 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                             (opt.aperture_mode == 1 && L >= opt.aperture_min_length);
             aux = ap ? DRIFT_APERTURE : 0u;
             p = {d(0)};
-            if (op == OP_DRIFT) p.push_back(d2w(0.5 * L));
             break;
         }
         case ST_OBJECT_TYPE_MULTIPOLE: {

@@ -21,7 +21,6 @@ namespace stg {
 struct PState {
     double x, px, y, py, zeta, delta, psigma, rpp, rvv, chi, s;
     double beta0, q0, p0c, mass0, charge_ratio, gamma0, energy0;
-    double rvv_m1;  // rvv - 1 (exact for rvv in [1/2, 2]); the fast drift's zeta term
     int64_t pid, at_element, at_turn, state;
     bool lazy_s;    // s is +0 at this turn's start: s is read from the lattice's s table
 };
@@ -52,7 +51,6 @@ __device__ __forceinline__ void add_energy(PState &p, double de)
     p.zeta *= rvv / p.rvv;
     p.rvv = rvv;
     p.rpp = 1.0 / opd;
-    p.rvv_m1 = rvv - 1.0;
 }
 
 // NS(Particles_update_delta_value): particles.h:5459-5496
@@ -66,24 +64,25 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
     p.rvv = opd / (1.0 + ptau_beta0);
     p.rpp = 1.0 / opd;
     p.psigma = ptau_beta0 / (beta0 * beta0);
-    p.rvv_m1 = p.rvv - 1.0;
 }
 
 // ------------------------------------------------------------------- maps
-// be_drift/track.h:45-67.  FAST: zeta += L (rvv - 1) - (L/2)(xp^2 + yp^2), i.e.
-// the reference's L (rvv - (1 + (xp^2 + yp^2)/2)) regrouped into two fused
-// multiply-adds with rvv - 1 kept per particle.  s is only accumulated when
-// the turn did not start at s = +0 (otherwise it comes from the s table).
+// be_drift/track.h:45-67.  FAST keeps the reference's rounding of
+// 1 + (xp^2 + yp^2)/2 at the scale of 1.0 (u below): regrouping the zeta
+// update as L (rvv - 1) - (L/2)(xp^2 + yp^2) is more accurate but departs
+// from the reference by its own rounding noise, ~1e-16 m per drift.
+// s is only accumulated when the turn did not start at s = +0 (otherwise it
+// comes from the lattice's s table).
 template <bool FAST>
-__device__ __forceinline__ void drift(PState &p, double L, double half_L)
+__device__ __forceinline__ void drift(PState &p, double L)
 {
     double const xp = p.px * p.rpp;
     double const yp = p.py * p.rpp;
     if (FAST) {
-        double const t = fma(yp, yp, xp * xp);
+        double const u = fma(fma(yp, yp, xp * xp), 0.5, 1.0);
         p.x = fma(xp, L, p.x);
         p.y = fma(yp, L, p.y);
-        p.zeta = fma(-half_L, t, fma(L, p.rvv_m1, p.zeta));
+        p.zeta = fma(L, p.rvv - u, p.zeta);
     } else {
         double const dzeta = p.rvv - (1.0 + (xp * xp + yp * yp) * 0.5);
         p.x += xp * L;
@@ -233,7 +232,7 @@ __device__ __forceinline__ bool inside_rect_ellipse(const PState &p, const uint6
 }
 
 // be_rfmultipole/track.h:39-118
-__device__ __noinline__ void rf_multipole(PState &p, const uint64_t *rec, int order)
+__device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec, int order)
 {
     double const voltage = W(rec[1]), frequency = W(rec[2]), lag = W(rec[3]);
     const uint64_t *bal = rec + 4;
@@ -264,6 +263,7 @@ __device__ __noinline__ void rf_multipole(PState &p, const uint64_t *rec, int or
     p.px += -chi * dpx;
     p.py += chi * dpy;
     add_energy(p, cav_energy + rfm_energy);
+    return p;
 }
 
 // ----------------------------------------------------- Gaussian beam fields
@@ -401,7 +401,7 @@ __device__ __noinline__ void fields_gauss(double x, double y, double sigma_x, do
 }
 
 // be_beamfields/track.h:89-149
-__device__ __noinline__ void beam_beam_4d(PState &p, const uint64_t *rec)
+__device__ __noinline__ PState beam_beam_4d(PState p, const uint64_t *rec)
 {
     const uint64_t *d = rec + 1;
     double const charge = 1. * p.q0 * kQelemD;
@@ -415,6 +415,7 @@ __device__ __noinline__ void beam_beam_4d(PState &p, const uint64_t *rec)
                       (p0c * (beta + W(d[4])));
     p.px += (fk * ex - W(d[8]));
     p.py += (fk * ey - W(d[9]));
+    return p;
 }
 
 __device__ __forceinline__ double sgn(double a) { return (double)((a >= 0) - (a < 0)); }
@@ -504,7 +505,7 @@ __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr
 
 // be_beamfields/track.h:342-507 with NS(BeamBeam6D_boost / inv_boost)
 // (be_beamfields.h:2101-2230); rec = [hdr, 34 head words, slices...]
-__device__ __noinline__ void beam_beam_6d(PState &p, const uint64_t *rec, int n_slices)
+__device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n_slices)
 {
     const uint64_t *d = rec + 1;
     const uint64_t *np_ = d + 34;
@@ -612,10 +613,11 @@ __device__ __noinline__ void beam_beam_6d(PState &p, const uint64_t *rec, int n_
     p.py = py + W(d[24]) - W(d[30]);
     p.zeta = sg + W(d[25]) - W(d[31]);
     set_delta(p, dl + W(d[26]) - W(d[32]));
+    return p;
 }
 
 // be_beamfields/track.h:154-198
-__device__ __noinline__ void sc_coasting(PState &p, const uint64_t *rec)
+__device__ __noinline__ PState sc_coasting(PState p, const uint64_t *rec)
 {
     const uint64_t *c = rec + 1;
     double const charge = kCharge0SiD * p.q0;
@@ -628,10 +630,11 @@ __device__ __noinline__ void sc_coasting(PState &p, const uint64_t *rec)
     fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);
     p.px += fk * ex;
     p.py += fk * ey;
+    return p;
 }
 
 // be_beamfields/track.h:203-268 with NS(Math_q_gauss) (internal/math_qgauss.h:114-175)
-__device__ __noinline__ void sc_qgauss(PState &p, const uint64_t *rec)
+__device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
 {
     const uint64_t *c = rec + 1;
     double const charge = kCharge0SiD * p.q0;
@@ -660,6 +663,7 @@ __device__ __noinline__ void sc_qgauss(PState &p, const uint64_t *rec)
     fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);
     p.px += fk * ex;
     p.py += fk * ey;
+    return p;
 }
 
 }  // namespace stg

@@ -15,7 +15,7 @@ namespace stg {
 
 enum Op : uint32_t {
     OP_END = 0,             // end of chunk
-    OP_DRIFT = 1,           // [L, L/2]       aux bit0: global aperture check
+    OP_DRIFT = 1,           // [L]            aux bit0: global aperture check
     OP_DRIFT_EXACT = 2,     // [L]            aux bit0: global aperture check
     OP_MULTIPOLE = 3,       // [bal 0..2n+1]  aux = order n
     OP_MULTIPOLE_CURV = 4,  // [bal..., hxl, hyl, length]  aux = order n

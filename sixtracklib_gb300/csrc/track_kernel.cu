@@ -107,7 +107,6 @@ __device__ __forceinline__ void load_particle(PState &p, const uint64_t *cols, i
     p.at_turn = k[19 * n + i];
     p.state = k[20 * n + i];
     p.energy0 = sqrt(p.p0c * p.p0c + p.mass0 * p.mass0);
-    p.rvv_m1 = p.rvv - 1.0;
     p.lazy_s = false;
 }
 
@@ -191,7 +190,7 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
     uint32_t const aux = (uint32_t)(hdr >> 32);
     switch (op) {
     case OP_DRIFT:
-        drift<FAST>(p, W(rec[1]), W(rec[2]));
+        drift<FAST>(p, W(rec[1]));
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_MULTIPOLE:
@@ -228,19 +227,19 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         p.py += W(rec[2]) * p.y;
         return 0;
     case OP_RF_MULTIPOLE:
-        rf_multipole(p, rec, (int)aux);
+        p = rf_multipole(p, rec, (int)aux);
         return 0;
     case OP_BB4D:
-        beam_beam_4d(p, rec);
+        p = beam_beam_4d(p, rec);
         return 0;
     case OP_BB6D:
-        beam_beam_6d(p, rec, (int)aux);
+        p = beam_beam_6d(p, rec, (int)aux);
         return 0;
     case OP_SC_COASTING:
-        sc_coasting(p, rec);
+        p = sc_coasting(p, rec);
         return 0;
     case OP_SC_QGAUSS:
-        sc_qgauss(p, rec);
+        p = sc_qgauss(p, rec);
         return 0;
     case OP_MONITOR: {
         uint64_t *out = reinterpret_cast<uint64_t *>(rec[8]);
@@ -270,8 +269,8 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
 // Kernel. Block-uniform control flow: every thread walks every record of
 // every chunk of every turn the block needs; lanes whose particle is done
 // are predicated off inside apply().
-template <bool FAST>
-__global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
+template <bool FAST, int MIN_BLOCKS>
+__global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS) track_kernel(TrackParams prm)
 {
     extern __shared__ __align__(128) uint64_t smem[];
     int const stages = prm.stages;
@@ -471,8 +470,10 @@ __global__ void __launch_bounds__(kMaxThreads, 1) track_kernel(TrackParams prm)
     k[20 * n + i] = p.state;
 }
 
-template __global__ void track_kernel<false>(TrackParams);
-template __global__ void track_kernel<true>(TrackParams);
+template __global__ void track_kernel<false, 1>(TrackParams);
+template __global__ void track_kernel<true, 1>(TrackParams);
+template __global__ void track_kernel<false, 2>(TrackParams);
+template __global__ void track_kernel<true, 2>(TrackParams);
 
 }  // namespace stg
 
@@ -483,27 +484,31 @@ size_t track_smem_bytes(int stages, int chunk_words)
     return (size_t)(16 + (size_t)stages * chunk_words) * sizeof(uint64_t);
 }
 
-int launch_track(const TrackParams &prm, bool fast, int threads, void *stream)
+template <bool FAST, int MB>
+static int launch_one(const TrackParams &prm, unsigned blocks, int threads, size_t smem,
+                      cudaStream_t s)
+{
+    cudaError_t err = cudaFuncSetAttribute(track_kernel<FAST, MB>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return (int)err;
+    track_kernel<FAST, MB><<<blocks, threads, smem, s>>>(prm);
+    return (int)cudaGetLastError();
+}
+
+int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_sm, void *stream)
 {
     int64_t const count = prm.i1 - prm.i0;
     if (count <= 0) return 0;
-    if (threads <= 0 || threads > kMaxThreads || threads % 32 != 0) threads = 256;
+    if (threads <= 0 || threads > kMaxThreads || threads % 32 != 0) threads = kMaxThreads;
     int64_t const blocks = (count + threads - 1) / threads;
     size_t const smem = track_smem_bytes(prm.stages, prm.chunk_words);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t err;
-    if (fast) {
-        err = cudaFuncSetAttribute(track_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem);
-        if (err != cudaSuccess) return (int)err;
-        track_kernel<true><<<(unsigned)blocks, threads, smem, s>>>(prm);
-    } else {
-        err = cudaFuncSetAttribute(track_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem);
-        if (err != cudaSuccess) return (int)err;
-        track_kernel<false><<<(unsigned)blocks, threads, smem, s>>>(prm);
-    }
-    return (int)cudaGetLastError();
+    bool const two = blocks_per_sm >= 2;
+    if (fast)
+        return two ? launch_one<true, 2>(prm, (unsigned)blocks, threads, smem, s)
+                   : launch_one<true, 1>(prm, (unsigned)blocks, threads, smem, s);
+    return two ? launch_one<false, 2>(prm, (unsigned)blocks, threads, smem, s)
+               : launch_one<false, 1>(prm, (unsigned)blocks, threads, smem, s);
 }
 
 }  // namespace stg

@@ -213,14 +213,18 @@ def test_synthetic_ring_sample(torch_cuda, oracle, mode):
 
 @pytest.mark.parametrize("elliptic", [False, True])
 def test_beam_beam_space_charge_ring(torch_cuda, oracle, elliptic):
+    """FODO ring + BB6D (21 slices) + BB4D + 200 q-Gaussian space-charge
+    kicks: 1e-13 after one turn, 1e-10 after 20 (the beam-beam kicks amplify
+    last-bit differences of exp() between CUDA and the host libm)."""
     lat = lattices.bb_sc_ring(elliptic=elliptic).cbuffer.to_image()
     p = lattices.gaussian_particles(1024, seed=17, sx=2e-5, sy=2e-5)
-    exp = p.block.copy()
-    oracle.track_until(lat, exp, 20)
-    for mode in ("exact", "fast"):
-        st, got = run_device(torch_cuda, lat, p.block, until=20, mode=mode)
-        assert st == 0
-        assert_parity(got, exp, tol=1e-12)
+    for turns, tol in ((1, 1e-13), (20, 1e-10)):
+        exp = p.block.copy()
+        oracle.track_until(lat, exp, turns)
+        for mode in ("exact", "fast"):
+            st, got = run_device(torch_cuda, lat, p.block, until=turns, mode=mode)
+            assert st == 0
+            assert_parity(got, exp, tol=tol)
 
 
 # ------------------------------------------------------------ edge cases
