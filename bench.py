@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
-    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--threads", type=int, default=128)
+    ap.add_argument("--blocks-per-sm", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -174,7 +175,7 @@ def cpu_baseline(ring, parts, seconds, threads=None):
 
 
 # ------------------------------------------------------------------- e2e
-def e2e_measure(ring, parts, steps, warmup, mode, threads):
+def e2e_measure(ring, parts, steps, warmup, mode, threads, blocks_per_sm):
     """Through the C ABI with host buffers (TrackJob): push, track one turn,
     collect -- per step."""
     import ctypes as C
@@ -191,7 +192,8 @@ def e2e_measure(ring, parts, steps, warmup, mode, threads):
     eb = lib.st_Buffer_new_on_data(img_e.ctypes.data, img_e.nbytes)
     idx = (C.c_uint64 * 1)(0)
     job = lib.st_TrackJob_new_detailed(b"cuda", pb, 1, idx, eb, None, 0,
-                                       f"mode={mode} threads_per_block={threads}".encode())
+                                       f"mode={mode} threads_per_block={threads} "
+                                       f"blocks_per_sm={blocks_per_sm}".encode())
     if not job:
         raise RuntimeError(_native.last_error())
     n_elem = len(ring)
@@ -299,7 +301,9 @@ def run_ours(args):
     lib = _native.load()
     ring, parts = make_workload(args.particles)
     n_elem = len(ring)
-    trk = DeviceTracker(ring.cbuffer, config=f"mode={args.mode} threads_per_block={args.threads}")
+    cfg = (f"mode={args.mode} threads_per_block={args.threads} "
+           f"blocks_per_sm={args.blocks_per_sm}")
+    trk = DeviceTracker(ring.cbuffer, config=cfg)
     cols = torch.from_numpy(parts.block.copy().view(np.int64)).to(dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -373,7 +377,7 @@ def run_ours(args):
         "data": "synthetic (seeded lattice and particles)",
         "config": {"workload": WORKLOAD, "particles_per_gpu": args.particles,
                    "lattice_elements": n_elem, "turns_per_step": 1, "mode": args.mode,
-                   "threads_per_block": args.threads,
+                   "threads_per_block": args.threads, "blocks_per_sm": args.blocks_per_sm,
                    "l2": "inputs larger than L2: 168 MB particle columns per GPU",
                    "parallelism": f"particles sharded, {world} independent GPU(s)"},
         "gpu_launches": int(launches),
@@ -391,7 +395,7 @@ def run_ours(args):
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_measure(ring, parts, max(2, args.steps // 2), 1, args.mode,
-                                      args.threads)
+                                      args.threads, args.blocks_per_sm)
         except Exception as exc:  # report, do not hide
             line["e2e"] = {"error": str(exc)}
     print(json.dumps(line), flush=True)

@@ -35,14 +35,14 @@ namespace stg {
 // ------------------------------------------------------------- options
 struct Options {
     bool fast = false;
-    int threads = 256;
+    int threads = 128;
     int device = 0;
     int aperture_mode = 2;
     double aperture_min_length = 0.0;
     double x_limit = 1.0, y_limit = 1.0;
     int stages = kDefaultStages;
     int chunk_words = 1024;
-    int blocks_per_sm = 1;
+    int blocks_per_sm = 2;
 };
 
 static std::string trim(const std::string &s)
