@@ -443,6 +443,17 @@ st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *lat, void *d_col
 int32_t st_DeviceLattice_launch_until(st_DeviceLattice *lat, void *d_cols,
                                       int64_t num_particles, int64_t until_turn, void *stream);
 st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *lat);
+/* No counterpart in the reference.  Same as st_DeviceLattice_track_until,
+ * for callers that must not allocate device memory while they track (code
+ * inside another framework's allocator, fixed-budget real-time loops): the
+ * call uses no cudaMalloc / cudaFree; its scratch is a static device array
+ * sized for at most 1,048,576 particles (larger calls fail with -1).  The
+ * first call on a device resolves that array's address (make it before any
+ * stream capture); calls overlapping on one GPU share the array and race.
+ * Synchronises `stream` and returns the track status. */
+st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLattice *lat, void *d_cols,
+                                                        int64_t num_particles,
+                                                        int64_t until_turn, void *stream);
 /* Kernel-launch counter (for launch accounting in benchmarks). */
 uint64_t st_engine_kernel_launches(void);
 /* Compile-time properties of the engine build. */

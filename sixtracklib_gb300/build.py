@@ -28,6 +28,7 @@ CUDA_SOURCES = {
     "engine.cu": [],
     "probe.cu": [],
     "compact.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -1271,3 +1271,28 @@ uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *j)
 }
 
 }  // extern "C"
+
+// ------------------------------------------- launch view (for noalloc.cu)
+#include "lattice_view.h"
+
+namespace stg {
+
+bool device_lattice_view(const st_DeviceLattice *L, LatticeLaunchView *v)
+{
+    if (!L || !L->full || !L->dev || !v) return false;
+    v->stream = L->full->d;
+    v->s_table = L->full->s_table;
+    v->n_chunks = L->full->cs.info.num_chunks;
+    v->chunk_words = L->full->cs.info.chunk_words;
+    v->stages = L->opt.stages;
+    v->threads = L->opt.threads;
+    v->blocks_per_sm = L->opt.blocks_per_sm;
+    v->num_elements = L->full->cs.info.num_elements;
+    v->fast = L->opt.fast;
+    v->xlim_bits = aperture_bits(L->opt.x_limit);
+    v->ylim_bits = aperture_bits(L->opt.y_limit);
+    v->device = L->dev->id;
+    return true;
+}
+
+}  // namespace stg

@@ -1,0 +1,24 @@
+// lattice_view.h -- what a launch needs to know about an st_DeviceLattice,
+// for entry points outside engine.cu.
+#pragma once
+
+#include <cstdint>
+
+#include "sixtracklib_gb300.h"
+
+namespace stg {
+
+struct LatticeLaunchView {
+    const uint64_t *stream = nullptr;  // device: chunked element stream
+    const double *s_table = nullptr;   // device: s table
+    int32_t n_chunks = 0, chunk_words = 0, stages = 0;
+    int32_t threads = 0, blocks_per_sm = 1;
+    int64_t num_elements = 0;
+    bool fast = false;
+    uint64_t xlim_bits = 0, ylim_bits = 0;
+    int device = 0;
+};
+
+bool device_lattice_view(const st_DeviceLattice *lat, LatticeLaunchView *view);
+
+}  // namespace stg
