@@ -233,6 +233,27 @@ def e2e_measure(ring, parts, steps, warmup, mode, threads, blocks_per_sm):
             "d2h_bytes_per_step": nbytes, "ms_per_step": dt / steps * 1e3}
 
 
+def aggregate_over_ranks(pet, elapsed, device):
+    """Whole-job figures of a weak-scaling run: PET summed over ranks, time =
+    the slowest rank's (every rank tracks its own particles, no exchange)."""
+    import torch
+    import torch.distributed as dist
+
+    tt = torch.tensor([float(elapsed)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    pp = torch.tensor([float(pet)], device=device, dtype=torch.float64)
+    dist.all_reduce(pp)
+    return float(pp.item()), float(tt.item())
+
+
+def shard_range(n_total, rank, world):
+    """Contiguous particle range of `rank` when n_total particles are split
+    over `world` ranks (used when a fixed beam is divided, strong scaling)."""
+    base, extra = divmod(n_total, world)
+    start = rank * base + min(rank, extra)
+    return start, start + base + (1 if rank < extra else 0)
+
+
 # ------------------------------------------------------------------- main
 def run_reference(args):
     rank, world, local = dist_env()
@@ -343,16 +364,7 @@ def run_ours(args):
     af = torch.zeros_like(b4)
     af[17:] = after
     pet = pet_between(b4, af, n_elem)
-    pet_total, t_max = pet, elapsed
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        pp = torch.tensor([float(pet)], device=dev, dtype=torch.float64)
-        dist.all_reduce(pp)
-        t_max = float(tt.item())
-        pet_total = float(pp.item())
+    pet_total, t_max = aggregate_over_ranks(pet, elapsed, dev) if world > 1 else (pet, elapsed)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
