@@ -1,0 +1,278 @@
+"""Differentiable until-turn tracking (reverse mode) for PyTorch.
+
+The reference tracks but does not differentiate.  This module adds
+gradients of a loss on the final coordinates with respect to
+
+* the initial coordinates (x, px, y, py, zeta, delta) of every particle, and
+* chosen element parameters: multipole ``knl[k]`` / ``ksl[k]`` and cavity
+  ``voltage``,
+
+through :class:`TrackFunction`, a ``torch.autograd.Function`` whose forward
+is the engine's until-turn tracking kernel and whose backward is the
+engine's hand-written adjoint kernel (``st_DeviceLattice_adjoint_turn``), one
+launch per turn, last turn first.
+
+Memory: the forward stores the particle columns every ``checkpoint_every``
+turns; the backward recomputes the turn-boundary states of one segment at a
+time from its checkpoint (the tracking kernel is deterministic, so the
+recomputed states are the forward's states bit for bit) and reverses the
+segment's turns.  Peak extra memory is ``(checkpoint_every + 1 + turns /
+checkpoint_every)`` column blocks of ``168 * n`` bytes.
+
+Conventions: delta is the independent longitudinal coordinate; rpp, rvv and
+psigma follow it as NS(Particles_update_delta_value) defines them
+(particles.h:5459-5496).  Lost particles keep the coordinates they had when
+they were lost (the reference's convention); their gradient flows back from
+there.  Apertures contribute no derivative.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from math import factorial
+
+import numpy as np
+
+from . import _native
+from .beam_elements import Cavity, Elements, Multipole
+from .device import DeviceTracker, _check_cols, _stream_handle
+from .particles import COL
+
+COORDS = ("x", "px", "y", "py", "zeta", "delta")
+COORD_ROWS = tuple(COL[c] for c in COORDS)
+
+
+class DifferentiableLattice:
+    """A compiled lattice plus the list of its learnable parameters.
+
+    ``params`` is a sequence of ``(element_index, "knl", k)``,
+    ``(element_index, "ksl", k)`` or ``(element_index, "voltage")``.
+    """
+
+    def __init__(self, elements: Elements, params, config: str | None = "mode=exact"):
+        self.tracker = DeviceTracker(elements, config)
+        self._lib = _native.load()
+        objs = elements.get_elements()
+        kinds, elems, scales, init = [], [], [], []
+        for p in params:
+            e = int(p[0])
+            if not 0 <= e < len(objs):
+                raise IndexError(f"element index {e} out of range")
+            obj = objs[e]
+            name = p[1]
+            if name in ("knl", "ksl"):
+                if not isinstance(obj, Multipole):
+                    raise TypeError(f"element {e} is not a Multipole")
+                k = int(p[2])
+                if not 0 <= k <= int(obj.order):
+                    raise ValueError(f"element {e}: order {obj.order} has no {name}[{k}]")
+                kind = 2 * k + (name == "ksl")
+                scale = 1.0 / factorial(k)  # bal[2k] = knl[k] / k!
+                value = float(obj.bal[kind]) / scale
+            elif name == "voltage":
+                if not isinstance(obj, Cavity):
+                    raise TypeError(f"element {e} is not a Cavity")
+                kind, scale, value = -1, 1.0, float(obj.voltage)
+            else:
+                raise ValueError(f"unknown parameter {name!r}")
+            elems.append(e)
+            kinds.append(kind)
+            scales.append(scale)
+            init.append(value)
+        self.params = list(params)
+        self._elems = np.asarray(elems, dtype=np.int64)
+        self._kinds = np.asarray(kinds, dtype=np.int32)
+        self.scales = np.asarray(scales, dtype=np.float64)
+        self.initial_values = np.asarray(init, dtype=np.float64)
+        # per-element parameter table for the adjoint kernel
+        E = self.tracker.num_elements
+        order = np.argsort(self._elems, kind="stable")
+        counts = np.bincount(self._elems, minlength=E) if len(elems) else np.zeros(E, np.int64)
+        self._pbeg = np.zeros(E + 1, dtype=np.int32)
+        self._pbeg[1:] = np.cumsum(counts)
+        self._pkind = self._kinds[order].astype(np.int32)
+        self._pid = order.astype(np.int32)
+        self._dev_tables = {}
+
+    @property
+    def num_params(self) -> int:
+        return len(self._kinds)
+
+    def _tables(self, device):
+        import torch
+
+        key = str(device)
+        if key not in self._dev_tables:
+            mk = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+            self._dev_tables[key] = (mk(self._pbeg), mk(self._pkind), mk(self._pid))
+        return self._dev_tables[key]
+
+    def set_values(self, values) -> None:
+        """Write parameter values (knl / ksl / voltage units) into the
+        compiled lattice."""
+        v = np.asarray(values.detach().cpu().numpy() if hasattr(values, "detach") else values,
+                       dtype=np.float64).reshape(-1)
+        if v.shape[0] != self.num_params:
+            raise ValueError(f"expected {self.num_params} parameter values, got {v.shape[0]}")
+        if self.num_params == 0:
+            return
+        bal = np.ascontiguousarray(v * self.scales)
+        rc = self._lib.st_DeviceLattice_set_parameters(
+            self.tracker._ptr, self.num_params, self._elems.ctypes.data, self._kinds.ctypes.data,
+            bal.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("set_parameters: " + _native.last_error())
+
+    def adjoint_turn(self, start, end, lam, turn: int, grad=None) -> None:
+        """dL/d(coordinates at the start of `turn`) from dL/d(at its end),
+        in place in `lam` (6 x n); parameter contributions added to `grad`
+        (dL/d bal or voltage, per parameter), if given."""
+        n = _check_cols(start)
+        if _check_cols(end) != n or tuple(lam.shape) != (6, n) or not lam.is_contiguous():
+            raise ValueError("adjoint_turn: inconsistent shapes")
+        if grad is not None and self.num_params:
+            pbeg, pkind, pid = self._tables(start.device)
+            tabs = (pbeg.data_ptr(), pkind.data_ptr(), pid.data_ptr(), grad.data_ptr())
+        else:
+            tabs = (None, None, None, None)
+        rc = self._lib.st_DeviceLattice_adjoint_turn(
+            self.tracker._ptr, start.data_ptr(), end.data_ptr(), n, int(turn), lam.data_ptr(),
+            *tabs, _stream_handle(start))
+        if rc != 0:
+            raise RuntimeError("adjoint_turn: " + _native.last_error())
+
+    def track(self, coords, values, cols, until_turn: int, checkpoint_every: int = 100):
+        """Differentiable tracking: ``(final coordinates 6 x n, final state n)``."""
+        return TrackFunction.apply(coords, values, self, cols, int(until_turn),
+                                   int(checkpoint_every))
+
+
+def apply_values(elements: Elements, params, values) -> Elements:
+    """A copy of `elements` with the listed parameters set to `values`
+    (knl / ksl / voltage units): the lattice a training loop exports."""
+    values = np.asarray(values, dtype=np.float64).reshape(-1)
+    if len(values) != len(params):
+        raise ValueError("one value per parameter expected")
+    objs = elements.get_elements()
+    for p, v in zip(params, values):
+        obj = objs[int(p[0])]
+        if p[1] == "voltage":
+            obj.voltage = float(v)
+        else:
+            k = int(p[2])
+            obj.bal = np.array(obj.bal, dtype=np.float64)
+            obj.bal[2 * k + (p[1] == "ksl")] = float(v) / factorial(k)
+    out = Elements()
+    for obj in objs:
+        out.cbuffer.add_object(*obj._encode())
+    return out
+
+
+def coordinates(cols):
+    """The 6 x n coordinate rows (x, px, y, py, zeta, delta) of a column block."""
+    return cols.view(dtype=__import__("torch").float64)[list(COORD_ROWS)]
+
+
+def set_coordinates(cols, coords) -> None:
+    """Write x, px, y, py, zeta, delta into a column block and derive rpp,
+    rvv, psigma from delta (particles.h:5459-5496)."""
+    import torch
+
+    f = cols.view(dtype=torch.float64)
+    c = coords.detach().to(torch.float64)
+    for r, row in enumerate(COORD_ROWS):
+        f[row] = c[r]
+    beta0 = f[COL["beta0"]]
+    d = c[5]
+    db0 = d * beta0
+    ptau_beta0 = torch.sqrt(db0 * db0 + 2.0 * db0 * beta0 + 1.0) - 1.0
+    opd = 1.0 + d
+    f[COL["rvv"]] = opd / (1.0 + ptau_beta0)
+    f[COL["rpp"]] = 1.0 / opd
+    f[COL["psigma"]] = ptau_beta0 / (beta0 * beta0)
+
+
+def _start_turn(cols) -> int:
+    import torch
+
+    alive = cols[COL["state"]] == 1
+    if not bool(alive.any()):
+        return int(cols[COL["at_turn"]].max())
+    return int(torch.where(alive, cols[COL["at_turn"]], cols[COL["at_turn"]].max()).min())
+
+
+def _track_checked(lat: DifferentiableLattice, cols, until: int) -> None:
+    st = lat.tracker.track_until(cols, until)
+    if st != 0:
+        raise RuntimeError(f"tracking failed (status {st}): " + _native.last_error())
+
+
+class TrackFunction:
+    """``torch.autograd.Function``: (coords 6 x n, parameter values) ->
+    (final coords 6 x n, final state)."""
+
+    _fn = None
+
+    @classmethod
+    def apply(cls, *args):
+        if cls._fn is None:
+            cls._fn = _make_function()
+        return cls._fn.apply(*args)
+
+
+def _make_function():
+    import torch
+
+    class _Track(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, coords, values, lat, cols, until_turn, every):
+            if every < 1:
+                raise ValueError("checkpoint_every must be >= 1")
+            lat.set_values(values)
+            work = cols.clone()
+            set_coordinates(work, coords)
+            t0 = _start_turn(work)
+            ckpts = {t0: work.clone()}
+            t = t0
+            while t < until_turn:
+                t1 = min(t + every, until_turn)
+                _track_checked(lat, work, t1)
+                t = t1
+                if t < until_turn:
+                    ckpts[t] = work.clone()
+            ctx.lat, ctx.ckpts, ctx.t0, ctx.until, ctx.every = lat, ckpts, t0, until_turn, every
+            ctx.values = values.detach().clone() if torch.is_tensor(values) else values
+            ctx.coords_meta = (coords.dtype, coords.device)
+            out = coordinates(work).clone().to(coords.dtype)
+            state = work[COL["state"]].clone()
+            ctx.mark_non_differentiable(state)
+            return out, state
+
+        @staticmethod
+        def backward(ctx, g_out, g_state):
+            lat = ctx.lat
+            n = next(iter(ctx.ckpts.values())).shape[1]
+            dev = next(iter(ctx.ckpts.values())).device
+            if g_out is None:
+                lam = torch.zeros((6, n), dtype=torch.float64, device=dev)
+            else:
+                lam = g_out.detach().to(torch.float64).contiguous().clone()
+            grad = torch.zeros(lat.num_params, dtype=torch.float64, device=dev)
+            lat.set_values(ctx.values)
+            for ts in sorted(ctx.ckpts, reverse=True):
+                te = min(ts + ctx.every, ctx.until)
+                blocks = [ctx.ckpts[ts]]
+                cur = ctx.ckpts[ts].clone()
+                for t in range(ts, te):
+                    _track_checked(lat, cur, t + 1)
+                    blocks.append(cur.clone())
+                for t in range(te - 1, ts - 1, -1):
+                    lat.adjoint_turn(blocks[t - ts], blocks[t - ts + 1], lam, t, grad)
+                del blocks
+            dtype, _ = ctx.coords_meta
+            g_values = grad * torch.from_numpy(lat.scales).to(dev)
+            if torch.is_tensor(ctx.values):
+                g_values = g_values.to(ctx.values.dtype)
+            return lam.to(dtype), g_values, None, None, None, None
+
+    return _Track

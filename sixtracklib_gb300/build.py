@@ -29,6 +29,7 @@ CUDA_SOURCES = {
     "probe.cu": [],
     "compact.cu": [],
     "noalloc.cu": [],
+    "adjoint.cu": [],
 }
 
 

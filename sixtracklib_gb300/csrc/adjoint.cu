@@ -1,0 +1,409 @@
+// adjoint.cu -- reverse-mode derivative of one turn of tracking.
+//
+// For a loss L on the particles' final coordinates u = (x, px, y, py, zeta,
+// delta), the adjoint lambda = dL/du is carried backwards through the
+// lattice: lambda_in = J^T lambda_out for each map, J being the map's
+// Jacobian with rpp and rvv taken as the functions of delta that
+// NS(Particles_update_delta_value) defines (particles.h:5459-5496).
+// Derivatives with respect to element parameters (multipole coefficients
+// bal[k], cavity voltage) are accumulated over particles and turns.
+//
+// Every differentiable map here is explicitly invertible (drifts and
+// rotations trivially, thin kicks because they leave x and y unchanged, the
+// cavity because it preserves tau = zeta / (beta0 rvv)).  So one launch
+// reverses one turn without a tape: each thread starts from its particle's
+// end-of-turn state, and for each element, last to first, restores the
+// element's input from its output and applies the transposed Jacobian at
+// that input.  A particle lost in the turn starts from the element where it
+// stopped (at_element).  The reconstruction error is rounding-level per
+// turn; the caller re-anchors every turn from stored turn-boundary states.
+// All lanes of a warp walk the same element at the same time, so parameter
+// contributions are reduced with warp shuffles and added with one atomic
+// per warp.
+//
+// Apertures contribute no derivative (a loss is a discontinuity).  Lattices
+// with elements that have no adjoint here (RF multipole, beam-beam, space
+// charge, disabled maps) are refused before launch.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "common.h"
+#include "kernel_api.h"
+#include "lattice_view.h"
+#include "maps.cuh"
+
+namespace stg {
+
+namespace {
+
+constexpr int kAdjThreads = 128;
+
+struct AdjParams {
+    const uint64_t *stream;
+    const int64_t *elem_offset;
+    int64_t num_elements;
+    const uint64_t *end;     // 21 x n: states at the end of the turn
+    int64_t n;
+    const int64_t *idx;      // particles alive at the start of the turn
+    const int64_t *count;
+    double *lam;             // 6 x n (x px y py zeta delta): in end of turn, out start
+    const int32_t *pbeg;     // num_elements + 1 offsets into the parameter list (or null)
+    const int32_t *pkind;    // bal index (>= 0) or -1 for a cavity voltage
+    const int32_t *pid;      // gradient slot of the entry
+    double *grad;            // dL/d(bal or voltage) per gradient slot
+};
+
+struct Lam {
+    double x, px, y, py, z, d;
+};
+
+struct RState {
+    double x, px, y, py, zeta, delta, rpp, rvv;
+    double beta0, chi, q, energy0;
+};
+
+// Q(delta) = sqrt(delta^2 b0^2 + 2 delta b0^2 + 1) = 1 + ptau * beta0
+__device__ __forceinline__ double q_of_delta(double delta, double beta0)
+{
+    double const db0 = delta * beta0;
+    return sqrt(db0 * db0 + 2.0 * db0 * beta0 + 1.0);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void add_grad(const AdjParams &a, int32_t j, double g)
+{
+    g = warp_sum(g);
+    if ((threadIdx.x & 31) == 0 && g != 0.0) atomicAdd(&a.grad[a.pid[j]], g);
+}
+
+// P(z) = sum_k (bal[2k] + i bal[2k+1]) z^k and P'(z), z = x + i y, by Horner.
+__device__ __forceinline__ void horner2(const uint64_t *bal, int n, double x, double y,
+                                        double &pr, double &pi, double &dr, double &di)
+{
+    pr = W(bal[2 * n]);
+    pi = W(bal[2 * n + 1]);
+    dr = 0.0;
+    di = 0.0;
+    for (int k = n - 1; k >= 0; --k) {
+        double const ndr = fma(dr, x, fma(-di, y, pr));
+        double const ndi = fma(dr, y, fma(di, x, pi));
+        double const npr = fma(pr, x, fma(-pi, y, W(bal[2 * k])));
+        double const npi = fma(pr, y, fma(pi, x, W(bal[2 * k + 1])));
+        dr = ndr;
+        di = ndi;
+        pr = npr;
+        pi = npi;
+    }
+}
+
+// Restore the input of one element from its output (state s) and apply
+// lambda <- J^T lambda at that input.  `on` is false for lanes that do not
+// take part (they still join the warp reductions).
+__device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *rec,
+                                             const AdjParams &a, int64_t e, bool on)
+{
+    uint64_t const hdr = rec[0];
+    uint32_t const op = (uint32_t)(hdr & 0xFF);
+    uint32_t const aux = (uint32_t)(hdr >> 32);
+    switch (op) {
+    case OP_DRIFT: {  // be_drift/track.h:45-67
+        if (!on) break;
+        double const L = W(rec[1]);
+        double const rpp = s.rpp, px = s.px, py = s.py;
+        double const xp = px * rpp, yp = py * rpp;
+        s.x -= xp * L;
+        s.y -= yp * L;
+        s.zeta -= L * (s.rvv - (1.0 + (xp * xp + yp * yp) * 0.5));
+        double const Q = q_of_delta(s.delta, s.beta0);
+        double const drvv = (1.0 - s.beta0 * s.beta0) / (Q * Q * Q);
+        double const drpp = -rpp * rpp;
+        double const lx = l.x, ly = l.y, lz = l.z;
+        l.px += L * rpp * (lx - lz * xp);
+        l.py += L * rpp * (ly - lz * yp);
+        l.d += L * (drpp * (lx * px + ly * py) + lz * (drvv - (xp * px + yp * py) * drpp));
+        break;
+    }
+    case OP_DRIFT_EXACT: {  // be_drift/track.h:71-97
+        if (!on) break;
+        double const L = W(rec[1]);
+        double const px = s.px, py = s.py;
+        double const opd = 1.0 + s.delta;
+        double const D2 = opd * opd - (px * px + py * py);
+        double const D = sqrt(D2);
+        double const lpzi = L / D;
+        s.x -= px * lpzi;
+        s.y -= py * lpzi;
+        s.zeta -= s.rvv * L - opd * lpzi;
+        double const D3 = D2 * D;
+        double const a_px = L * px / D3, a_py = L * py / D3, a_d = -L * opd / D3;
+        double const Q = q_of_delta(s.delta, s.beta0);
+        double const drvv = (1.0 - s.beta0 * s.beta0) / (Q * Q * Q);
+        double const lx = l.x, ly = l.y, lz = l.z;
+        l.px += lx * (lpzi + px * a_px) + ly * (py * a_px) - lz * opd * a_px;
+        l.py += lx * (px * a_py) + ly * (lpzi + py * a_py) - lz * opd * a_py;
+        l.d += lx * (px * a_d) + ly * (py * a_d) + lz * (L * drvv - lpzi - opd * a_d);
+        break;
+    }
+    case OP_MULTIPOLE:
+    case OP_MULTIPOLE_CURV: {  // be_multipole/track.h:38-112
+        int const n = (int)aux;
+        const uint64_t *bal = rec + 1;
+        bool const curv = op == OP_MULTIPOLE_CURV;
+        double const chi = s.chi, x = s.x, y = s.y;
+        double const hxl = curv ? W(bal[2 * n + 2]) : 0.0;
+        double const hyl = curv ? W(bal[2 * n + 3]) : 0.0;
+        double const length = curv ? W(bal[2 * n + 4]) : 0.0;
+        double const lpx = l.px, lpy = l.py;
+        if (on) {
+            double pr, pi, dr, di;
+            horner2(bal, n, x, y, pr, pi, dr, di);
+            double dpx = -chi * pr, dpy = chi * pi;
+            if (curv) {
+                s.zeta -= chi * (y * hyl - x * hxl);
+                dpx += hxl + hxl * s.delta;
+                dpy -= hyl + hyl * s.delta;
+                if (length > 0.0) {
+                    dpx -= chi * W(bal[0]) * x * hxl / length;
+                    dpy += chi * W(bal[1]) * y * hyl / length;
+                }
+            }
+            s.px -= dpx;
+            s.py -= dpy;
+            l.x += chi * (-lpx * dr + lpy * di);
+            l.y += chi * (lpx * di + lpy * dr);
+            if (curv) {
+                l.x -= l.z * chi * hxl;
+                l.y += l.z * chi * hyl;
+                l.d += lpx * hxl - lpy * hyl;
+                if (length > 0.0) {
+                    l.x -= lpx * chi * W(bal[0]) * hxl / length;
+                    l.y += lpy * chi * W(bal[1]) * hyl / length;
+                }
+            }
+        }
+        if (a.pbeg) {
+            // d(dpx, dpy)/d bal[2k] = chi (-Re z^k, Im z^k); / d bal[2k+1] = chi (Im z^k, Re z^k)
+            for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j) {
+                int const k2 = a.pkind[j];
+                double g = 0.0;
+                if (on && k2 >= 0) {
+                    double zr = 1.0, zi = 0.0;
+                    for (int k = 0; k < k2 / 2; ++k) {
+                        double const t = zr * x - zi * y;
+                        zi = zr * y + zi * x;
+                        zr = t;
+                    }
+                    g = (k2 & 1) ? chi * (lpx * zi + lpy * zr) : chi * (-lpx * zr + lpy * zi);
+                    if (length > 0.0 && k2 == 0) g -= lpx * chi * hxl * x / length;
+                    if (length > 0.0 && k2 == 1) g += lpy * chi * hyl * y / length;
+                }
+                add_grad(a, j, g);
+            }
+        }
+        break;
+    }
+    case OP_CAVITY: {  // be_cavity/track.h:39-67 + particles.h:5255-5297
+        double gV = 0.0;
+        if (on) {
+            double const beta0 = s.beta0, b2 = beta0 * beta0;
+            double const V = W(rec[1]), kf = W(rec[2]), lag = W(rec[3]);
+            // outputs; tau = zeta / (beta0 rvv) is unchanged by the map
+            double const zeta_o = s.zeta, rvv_o = s.rvv, delta_o = s.delta;
+            double const phase = lag - kf * (zeta_o / (beta0 * rvv_o));
+            double sph, cph;
+            sincos(phase, &sph, &cph);
+            double const dEn = s.q * V * sph / s.energy0;
+            double const Qo = q_of_delta(delta_o, beta0);
+            double const P = b2 * delta_o * (delta_o + 2.0) / (Qo + 1.0);  // Qo - 1
+            double const opdn = 1.0 + delta_o;
+            // input: Q_in - 1 = P - dE / E0
+            double const qm1 = P - dEn;
+            double const Qi = 1.0 + qm1;
+            double const r = qm1 * (qm1 + 2.0) / b2;  // (1 + delta_in)^2 - 1
+            double const opd = sqrt(r + 1.0);
+            double const delta = r / (opd + 1.0);
+            double const rvv = opd / Qi;
+            double const zeta = zeta_o * rvv / rvv_o;
+            s.delta = delta;
+            s.rvv = rvv;
+            s.rpp = 1.0 / opd;
+            s.zeta = zeta;
+            // transposed Jacobian
+            double const drvv = (1.0 - b2) / (Qi * Qi * Qi);
+            double const dEc = s.q * V * cph / s.energy0;
+            double const dP_dzeta = -dEc * kf / (beta0 * rvv);
+            double const dP_ddelta = dEc * kf * zeta / (beta0 * rvv * rvv) * drvv + b2 * opd / Qi;
+            double const dopd_dP = (1.0 + P) / (b2 * opdn);
+            double const drvvn_dP = dopd_dP / (1.0 + P) - opdn / ((1.0 + P) * (1.0 + P));
+            double const lP = l.d * dopd_dP + l.z * (zeta / rvv) * drvvn_dP;
+            double const lz = l.z * (rvv_o / rvv) + lP * dP_dzeta;
+            double const ld = -l.z * (zeta * rvv_o / (rvv * rvv)) * drvv + lP * dP_ddelta;
+            gV = lP * s.q * sph / s.energy0;
+            l.z = lz;
+            l.d = ld;
+        }
+        if (a.pbeg) {
+            for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j)
+                add_grad(a, j, (on && a.pkind[j] < 0) ? gV : 0.0);
+        }
+        break;
+    }
+    case OP_XYSHIFT:  // be_xyshift/track.h:38-55
+        if (!on) break;
+        s.x -= W(rec[1]);
+        s.y -= W(rec[2]);
+        break;
+    case OP_SROTATION: {  // be_srotation/track.h:38-69
+        if (!on) break;
+        double const cz = W(rec[1]), sz = W(rec[2]);
+        double const x = s.x, y = s.y, px = s.px, py = s.py;
+        s.x = cz * x - sz * y;
+        s.y = sz * x + cz * y;
+        s.px = cz * px - sz * py;
+        s.py = sz * px + cz * py;
+        double const lx = l.x, ly = l.y, lpx = l.px, lpy = l.py;
+        l.x = cz * lx - sz * ly;
+        l.y = sz * lx + cz * ly;
+        l.px = cz * lpx - sz * lpy;
+        l.py = sz * lpx + cz * lpy;
+        break;
+    }
+    case OP_DIPEDGE:  // be_dipedge/track.h:37-51
+        if (!on) break;
+        s.px -= W(rec[1]) * s.x;
+        s.py -= W(rec[2]) * s.y;
+        l.x += W(rec[1]) * l.px;
+        l.y += W(rec[2]) * l.py;
+        break;
+    default:  // apertures, monitors, no-ops: identity
+        break;
+    }
+}
+
+__global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
+{
+    int64_t const t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t const cnt = *a.count;
+    bool const part = t < cnt;
+    int64_t const n = a.n;
+    int64_t const i = part ? a.idx[t] : 0;
+    RState s{};
+    Lam l{0, 0, 0, 0, 0, 0};
+    int64_t last = -1;  // last element the particle went through in this turn
+    if (part) {
+        const double *d = reinterpret_cast<const double *>(a.end);
+        const int64_t *k = reinterpret_cast<const int64_t *>(a.end);
+        double const p0c = d[4 * n + i], mass0 = d[1 * n + i];
+        s.beta0 = d[2 * n + i];
+        s.x = d[6 * n + i];
+        s.y = d[7 * n + i];
+        s.px = d[8 * n + i];
+        s.py = d[9 * n + i];
+        s.zeta = d[10 * n + i];
+        s.delta = d[12 * n + i];
+        s.rpp = d[13 * n + i];
+        s.rvv = d[14 * n + i];
+        s.chi = d[15 * n + i];
+        s.q = d[0 * n + i] * d[16 * n + i];
+        s.energy0 = sqrt(p0c * p0c + mass0 * mass0);
+        int64_t const ae = k[18 * n + i];
+        last = (k[20 * n + i] == 1) ? a.num_elements - 1
+                                    : (ae < a.num_elements ? ae : a.num_elements - 1);
+        l.x = a.lam[0 * n + i];
+        l.px = a.lam[1 * n + i];
+        l.y = a.lam[2 * n + i];
+        l.py = a.lam[3 * n + i];
+        l.z = a.lam[4 * n + i];
+        l.d = a.lam[5 * n + i];
+    }
+    long long wl = last;
+    for (int o = 16; o > 0; o >>= 1) {
+        long long const v = __shfl_xor_sync(0xFFFFFFFFu, wl, o);
+        wl = v > wl ? v : wl;
+    }
+    for (int64_t e = (int64_t)wl; e >= 0; --e)
+        reverse_elem(s, l, a.stream + a.elem_offset[e], a, e, part && e <= last);
+    if (part) {
+        a.lam[0 * n + i] = l.x;
+        a.lam[1 * n + i] = l.px;
+        a.lam[2 * n + i] = l.y;
+        a.lam[3 * n + i] = l.py;
+        a.lam[4 * n + i] = l.z;
+        a.lam[5 * n + i] = l.d;
+    }
+}
+
+}  // namespace
+
+}  // namespace stg
+
+using namespace stg;
+
+extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
+    st_DeviceLattice *lat, const void *d_start, const void *d_end, int64_t n, int64_t turn,
+    double *d_lam, const int32_t *d_param_begin, const int32_t *d_param_kind,
+    const int32_t *d_param_id, double *d_grad, void *stream)
+{
+    clear_error();
+    LatticeLaunchView v;
+    if (!device_lattice_view(lat, &v)) {
+        set_error("adjoint: invalid lattice");
+        return -1;
+    }
+    uint32_t const no_adjoint = (1u << OP_RF_MULTIPOLE) | (1u << OP_BB4D) | (1u << OP_BB6D) |
+                                (1u << OP_SC_COASTING) | (1u << OP_SC_QGAUSS) |
+                                (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
+    if (v.op_mask & no_adjoint) {
+        set_error("adjoint: the lattice contains elements without an adjoint "
+                  "(RF multipole, beam-beam, space charge or a disabled map)");
+        return -1;
+    }
+    if (n <= 0 || v.num_elements == 0) return 0;
+    if (!d_start || !d_end || !d_lam ||
+        (d_param_begin && (!d_param_kind || !d_param_id || !d_grad))) {
+        set_error("adjoint: missing device buffer");
+        return -1;
+    }
+    if (cudaSetDevice(v.device) != cudaSuccess) {
+        set_error("adjoint: cudaSetDevice failed");
+        return -1;
+    }
+    uint64_t *scratch = device_scratch(v.device, select_scratch_words(n));
+    if (!scratch) return -1;
+    int64_t *idx = nullptr, *count = nullptr;
+    // alive at the start of the turn: state 1 and at_turn < turn + 1
+    int rc = launch_select(static_cast<const uint64_t *>(d_start), n, 0, n, MODE_UNTIL, turn + 1,
+                           scratch, &idx, &count, stream);
+    if (rc != 0) {
+        set_error(std::string("adjoint selection: ") + cudaGetErrorString((cudaError_t)rc));
+        return -1;
+    }
+    AdjParams a{};
+    a.stream = v.stream;
+    a.elem_offset = v.elem_offset;
+    a.num_elements = v.num_elements;
+    a.end = static_cast<const uint64_t *>(d_end);
+    a.n = n;
+    a.idx = idx;
+    a.count = count;
+    a.lam = d_lam;
+    a.pbeg = d_param_begin;
+    a.pkind = d_param_kind;
+    a.pid = d_param_id;
+    a.grad = d_grad;
+    unsigned const blocks = (unsigned)((n + kAdjThreads - 1) / kAdjThreads);
+    adjoint_turn_kernel<<<blocks, kAdjThreads, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    rc = (int)cudaGetLastError();
+    if (rc != 0) {
+        set_error(std::string("adjoint launch: ") + cudaGetErrorString((cudaError_t)rc));
+        return -1;
+    }
+    count_launches(4);
+    return 0;
+}

@@ -194,8 +194,9 @@ static Device *get_device(int id)
 // ------------------------------------------------------- device stream
 struct DevStream {
     CompiledStream cs;
-    uint64_t *d = nullptr;        // chunked stream, then the s table
+    uint64_t *d = nullptr;        // chunked stream, the s table, the element offsets
     const double *s_table = nullptr;
+    const int64_t *elem_offset = nullptr;
     int device = -1;
     DevStream() = default;
     DevStream(const DevStream &) = delete;
@@ -220,8 +221,12 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     }
     size_t const bytes = s->cs.words.size() * 8;
     size_t const sbytes = s->cs.s_table.size() * 8;
+    size_t const obytes = s->cs.elem_offset.size() * 8;
     if (!cuda_ok(cudaSetDevice(dev->id), "cudaSetDevice") ||
-        !cuda_ok(cudaMalloc(&s->d, bytes + sbytes), "cudaMalloc(lattice)") ||
+        !cuda_ok(cudaMalloc(&s->d, bytes + sbytes + obytes + 8), "cudaMalloc(lattice)") ||
+        !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + bytes + sbytes,
+                            s->cs.elem_offset.data(), obytes, cudaMemcpyHostToDevice),
+                 "cudaMemcpy(element offsets)") ||
         !cuda_ok(cudaMemcpy(s->d, s->cs.words.data(), bytes, cudaMemcpyHostToDevice),
                  "cudaMemcpy(lattice)") ||
         !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + bytes, s->cs.s_table.data(), sbytes,
@@ -229,6 +234,8 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
                  "cudaMemcpy(s table)"))
         return nullptr;
     s->s_table = reinterpret_cast<const double *>(reinterpret_cast<char *>(s->d) + bytes);
+    s->elem_offset =
+        reinterpret_cast<const int64_t *>(reinterpret_cast<char *>(s->d) + bytes + sbytes);
     s->device = dev->id;
     return s;
 }
@@ -557,6 +564,72 @@ int64_t st_DeviceLattice_num_elements(const st_DeviceLattice *L)
 int64_t st_DeviceLattice_num_chunks(const st_DeviceLattice *L)
 {
     return L ? L->full->cs.info.num_chunks : 0;
+}
+
+st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *L, int64_t num,
+                                                  const int64_t *element, const int32_t *kind,
+                                                  const double *value)
+{
+    clear_error();
+    if (!L || num < 0 || (num > 0 && (!element || !kind || !value))) {
+        set_error("set_parameters: invalid arguments");
+        return -1;
+    }
+    ImageView img;
+    std::string err;
+    if (!img.open(L->image.data(), L->image.size() * 8, &err)) {
+        set_error(err);
+        return -1;
+    }
+    DevStream &ds = *L->full;
+    // validate everything before writing anything
+    std::vector<std::pair<uint64_t, uint64_t>> where((size_t)num);  // (stream word, image word)
+    for (int64_t j = 0; j < num; ++j) {
+        int64_t const e = element[j];
+        if (e < 0 || e >= ds.cs.info.num_elements) {
+            set_error("set_parameters: element index out of range");
+            return -1;
+        }
+        uint64_t const off = (uint64_t)ds.cs.elem_offset[(size_t)e];
+        uint64_t const hdr = ds.cs.words[off];
+        uint32_t const op = (uint32_t)(hdr & 0xFF);
+        uint32_t const order = (uint32_t)(hdr >> 32);
+        if (kind[j] >= 0) {
+            const uint64_t *bal = img.deref((uint64_t)e, 4);
+            if ((op != OP_MULTIPOLE && op != OP_MULTIPOLE_CURV) || !bal ||
+                (uint32_t)kind[j] >= 2 * order + 2) {
+                set_error("set_parameters: element " + std::to_string(e) +
+                          " has no multipole coefficient bal[" + std::to_string(kind[j]) + "]");
+                return -1;
+            }
+            where[(size_t)j] = {off + 1 + (uint64_t)kind[j],
+                                (uint64_t)(bal - img.img) + (uint64_t)kind[j]};
+        } else if (kind[j] == -1) {
+            if (op != OP_CAVITY) {
+                set_error("set_parameters: element " + std::to_string(e) + " is not a cavity");
+                return -1;
+            }
+            where[(size_t)j] = {off + 1, img.begin_word((uint64_t)e)};
+        } else {
+            set_error("set_parameters: unknown parameter kind");
+            return -1;
+        }
+    }
+    if (!cuda_ok(cudaSetDevice(L->dev->id), "cudaSetDevice") ||
+        !cuda_ok(cudaDeviceSynchronize(), "cudaDeviceSynchronize"))
+        return -1;
+    for (int64_t j = 0; j < num; ++j) {
+        uint64_t bits;
+        std::memcpy(&bits, &value[j], 8);
+        ds.cs.words[where[(size_t)j].first] = bits;
+        L->image[where[(size_t)j].second] = bits;
+    }
+    if (!cuda_ok(cudaMemcpy(ds.d, ds.cs.words.data(), ds.cs.words.size() * 8,
+                            cudaMemcpyHostToDevice),
+                 "cudaMemcpy(lattice)"))
+        return -1;
+    L->lines.clear();  // line streams are rebuilt from the updated image
+    return 0;
 }
 
 st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols, int64_t n,
@@ -1292,7 +1365,27 @@ bool device_lattice_view(const st_DeviceLattice *L, LatticeLaunchView *v)
     v->xlim_bits = aperture_bits(L->opt.x_limit);
     v->ylim_bits = aperture_bits(L->opt.y_limit);
     v->device = L->dev->id;
+    v->elem_offset = L->full->elem_offset;
+    v->op_mask = L->full->cs.info.op_mask;
     return true;
 }
+
+// Selection scratch of `device`, grown to at least `words` (engine-owned).
+uint64_t *device_scratch(int device, int64_t words)
+{
+    Device *dev = get_device(device);
+    if (!dev) return nullptr;
+    if (words > dev->scratch_words) {
+        if (dev->scratch) cudaFree(dev->scratch);
+        dev->scratch = nullptr;
+        dev->scratch_words = 0;
+        if (!cuda_ok(cudaMalloc(&dev->scratch, (size_t)words * 8), "cudaMalloc(scratch)"))
+            return nullptr;
+        dev->scratch_words = words;
+    }
+    return dev->scratch;
+}
+
+void count_launches(uint64_t n) { g_launches.fetch_add(n); }
 
 }  // namespace stg

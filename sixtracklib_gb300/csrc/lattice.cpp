@@ -235,9 +235,12 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
         ++nchunks;
         used = 0;
     };
+    out->elem_offset.clear();
+    out->elem_offset.reserve(em.rec_len.size());
     for (uint64_t r = 0; r < em.rec_len.size(); ++r) {
         uint64_t const n = em.rec_len[r];
         if (used + n + 1 > cw) close_chunk();
+        out->elem_offset.push_back((int64_t)out->words.size());
         out->words.insert(out->words.end(), em.recs.begin() + pos, em.recs.begin() + pos + n);
         used += n;
         pos += n;

@@ -30,6 +30,8 @@ struct CompiledStream {
     // the drift lengths summed in lattice order, in double, exactly as the
     // tracking loop accumulates them (num_elements + 1 entries).
     std::vector<double> s_table;
+    // word offset of each element's record in `words` (num_elements entries)
+    std::vector<int64_t> elem_offset;
 };
 
 // Compile elements [begin, end) of the image.  Returns false (and sets the

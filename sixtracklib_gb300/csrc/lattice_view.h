@@ -17,8 +17,12 @@ struct LatticeLaunchView {
     bool fast = false;
     uint64_t xlim_bits = 0, ylim_bits = 0;
     int device = 0;
+    const int64_t *elem_offset = nullptr;  // device: record offset per element
+    uint32_t op_mask = 0;                  // opcodes present in the lattice
 };
 
 bool device_lattice_view(const st_DeviceLattice *lat, LatticeLaunchView *view);
+uint64_t *device_scratch(int device, int64_t words);
+void count_launches(uint64_t n);
 
 }  // namespace stg

@@ -232,7 +232,7 @@ __device__ __forceinline__ bool inside_rect_ellipse(const PState &p, const uint6
 }
 
 // be_rfmultipole/track.h:39-118
-__device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec, int order)
+static __device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec, int order)
 {
     double const voltage = W(rec[1]), frequency = W(rec[2]), lag = W(rec[3]);
     const uint64_t *bal = rec + 4;
@@ -271,7 +271,7 @@ __device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec, int o
 // C335), as used by be_beamfields/faddeeva_cern.h:45-120.  The backward
 // recursion and the series are fused into one loop (the series consumes
 // R[n-1] as soon as the recursion yields it), so no arrays are needed.
-__device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
+static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
 {
     double const a_const = 1.12837916709551;
     double const xlim = 5.33, ylim = 4.29;
@@ -327,7 +327,7 @@ __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, dou
 }
 
 // gauss_fields.h:56-208 (NS(get_Ex_Ey_Gx_Gy_gauss), centred: Delta = 0)
-__device__ __noinline__ void fields_gauss(double x, double y, double sigma_x, double sigma_y,
+static __device__ __noinline__ void fields_gauss(double x, double y, double sigma_x, double sigma_y,
                                           double min_sigma_diff, int skip_gs, double *ex_p,
                                           double *ey_p, double *gx_p, double *gy_p)
 {
@@ -401,7 +401,7 @@ __device__ __noinline__ void fields_gauss(double x, double y, double sigma_x, do
 }
 
 // be_beamfields/track.h:89-149
-__device__ __noinline__ PState beam_beam_4d(PState p, const uint64_t *rec)
+static __device__ __noinline__ PState beam_beam_4d(PState p, const uint64_t *rec)
 {
     const uint64_t *d = rec + 1;
     double const charge = 1. * p.q0 * kQelemD;
@@ -421,7 +421,7 @@ __device__ __noinline__ PState beam_beam_4d(PState p, const uint64_t *rec)
 __device__ __forceinline__ double sgn(double a) { return (double)((a >= 0) - (a < 0)); }
 
 // be_beamfields/be_beamfields.h:2232-2385 (NS(BeamBeam6D_propagate_Sigma_matrix))
-__device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr, double *out)
+static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr, double *out)
 {
     double const S11_0 = W(sg[0]), S12_0 = W(sg[1]), S13_0 = W(sg[2]), S14_0 = W(sg[3]),
                  S22_0 = W(sg[4]), S23_0 = W(sg[5]), S24_0 = W(sg[6]), S33_0 = W(sg[7]),
@@ -505,7 +505,7 @@ __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr
 
 // be_beamfields/track.h:342-507 with NS(BeamBeam6D_boost / inv_boost)
 // (be_beamfields.h:2101-2230); rec = [hdr, 34 head words, slices...]
-__device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n_slices)
+static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n_slices)
 {
     const uint64_t *d = rec + 1;
     const uint64_t *np_ = d + 34;
@@ -617,7 +617,7 @@ __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n
 }
 
 // be_beamfields/track.h:154-198
-__device__ __noinline__ PState sc_coasting(PState p, const uint64_t *rec)
+static __device__ __noinline__ PState sc_coasting(PState p, const uint64_t *rec)
 {
     const uint64_t *c = rec + 1;
     double const charge = kCharge0SiD * p.q0;
@@ -634,7 +634,7 @@ __device__ __noinline__ PState sc_coasting(PState p, const uint64_t *rec)
 }
 
 // be_beamfields/track.h:203-268 with NS(Math_q_gauss) (internal/math_qgauss.h:114-175)
-__device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
+static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
 {
     const uint64_t *c = rec + 1;
     double const charge = kCharge0SiD * p.q0;

@@ -47,6 +47,32 @@ def fodo_ring(n_cells=64, with_cavity=True, with_aperture=True) -> Elements:
     return e
 
 
+def learnable_fodo_ring(seed=4, n_cells=64, n_sextupoles=16, k2l_sigma=0.1):
+    """The FODO ring with learnable strengths: the 64 focusing quadrupoles'
+    knl[1] and, on 16 of them (evenly spaced), a sextupole component knl[2]
+    ~ N(0, 0.1).  Returns ``(elements, params)`` with ``params`` in the form
+    :class:`sixtracklib_gb300.autodiff.DifferentiableLattice` takes: 64
+    ``(element, "knl", 1)`` then 16 ``(element, "knl", 2)``."""
+    rng = np.random.default_rng(seed)
+    e = Elements()
+    sext_cells = set(np.linspace(0, n_cells, n_sextupoles, endpoint=False).astype(int).tolist())
+    quads, sexts = [], []
+    for c in range(n_cells):
+        e.Drift(length=2.0)
+        if c in sext_cells:
+            sexts.append(len(e))
+            e.Multipole(knl=[0.0, +0.05, float(rng.normal(0.0, k2l_sigma))])
+        else:
+            e.Multipole(knl=[0.0, +0.05])
+        quads.append(len(e) - 1)
+        e.Drift(length=2.0)
+        e.Multipole(knl=[0.0, -0.05])
+    e.Cavity(voltage=6e6, frequency=400e6, lag=180.0)
+    e.LimitRect(min_x=-0.02, max_x=0.02, min_y=-0.02, max_y=0.02)
+    params = [(q, "knl", 1) for q in quads] + [(s, "knl", 2) for s in sexts]
+    return e, params
+
+
 def synthetic_ring(seed=20240601, n_cells=4000, n_extra_drift=1000,
                    n_shift=1000, n_rot=1000, n_cav=16, n_ell=984) -> Elements:
     """The 20,000-element synthetic ring.
