@@ -466,27 +466,30 @@ st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLattice *lat, vo
 st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *lat, int64_t num,
                                                   const int64_t *element, const int32_t *kind,
                                                   const double *value);
-/* No reference counterpart.  Reverse-mode derivative of turn `turn` of
- * until-turn tracking.  d_start / d_end: 21 x n column blocks holding the
- * particles at the start and at the end of that turn (the results of
- * st_DeviceLattice_track_until to `turn` and to `turn + 1`).  d_lam: 6 x n
- * doubles (rows x, px, y, py, zeta, delta) holding dL/d(end coordinates) on
- * entry and dL/d(start coordinates) on return, for the particles alive at the
- * start of the turn (other columns are left unchanged).  Parameter
- * derivatives: d_param_begin[e] .. d_param_begin[e + 1] - 1 index the
- * entries of element e in d_param_kind (bal index, or -1 for a cavity
- * voltage) and d_param_id (slot of d_grad), num_elements + 1 offsets; the
- * turn's contribution is added to d_grad.  Pass d_param_begin = NULL for
- * coordinate derivatives only.  Lattices with RF multipoles, beam-beam or
- * space-charge elements are refused (-1).  Asynchronous on `stream`; device
- * pointers except `lat`. */
-st_track_status_t st_DeviceLattice_adjoint_turn(st_DeviceLattice *lat, const void *d_start,
-                                                const void *d_end, int64_t num_particles,
-                                                int64_t turn, double *d_lam,
-                                                const int32_t *d_param_begin,
-                                                const int32_t *d_param_kind,
-                                                const int32_t *d_param_id, double *d_grad,
-                                                void *stream);
+/* No reference counterpart.  Reverse-mode derivative of turns
+ * [turn_begin, turn_end) of until-turn tracking.  d_start / d_end: 21 x n
+ * column blocks holding the particles at turn_begin and at turn_end (the
+ * results of st_DeviceLattice_track_until to those turns).  d_lam: 6 x n
+ * doubles (rows x, px, y, py, zeta, delta) holding dL/d(coordinates at
+ * turn_end) on entry and dL/d(coordinates at turn_begin) on return, for the
+ * particles alive at turn_begin (a particle lost inside the range has its
+ * row taken as dL/d(coordinates where it was lost)); other columns are left
+ * unchanged.  Intermediate turns are reconstructed by inverting the maps, so
+ * the accuracy is best for short ranges (one turn: exact re-anchoring).
+ * Parameter derivatives: d_param_begin[e] .. d_param_begin[e + 1] - 1 index
+ * the entries of element e in d_param_kind (bal index, or -1 for a cavity
+ * voltage) and d_param_id (slot of d_grad, every id < num_slots);
+ * num_elements + 1 offsets; the range's contribution is added to d_grad.
+ * Pass d_param_begin = NULL for coordinate derivatives only.  Lattices with
+ * RF multipoles, beam-beam or space-charge elements are refused (-1).
+ * Asynchronous on `stream`; device pointers except `lat`. */
+st_track_status_t st_DeviceLattice_adjoint_turns(st_DeviceLattice *lat, const void *d_start,
+                                                 const void *d_end, int64_t num_particles,
+                                                 int64_t turn_begin, int64_t turn_end,
+                                                 double *d_lam, const int32_t *d_param_begin,
+                                                 const int32_t *d_param_kind,
+                                                 const int32_t *d_param_id, int32_t num_slots,
+                                                 double *d_grad, void *stream);
 /* Kernel-launch counter (for launch accounting in benchmarks). */
 uint64_t st_engine_kernel_launches(void);
 /* Compile-time properties of the engine build. */

@@ -78,7 +78,8 @@ _SIGNATURES = {
     "st_DeviceLattice_launch_until": ([vp, vp, i64, i64, vp], i32),
     "st_DeviceLattice_last_status": ([vp], i32),
     "st_DeviceLattice_set_parameters": ([vp, i64, vp, vp, vp], i32),
-    "st_DeviceLattice_adjoint_turn": ([vp, vp, vp, i64, i64, vp, vp, vp, vp, vp, vp], i32),
+    "st_DeviceLattice_adjoint_turns": ([vp, vp, vp, i64, i64, i64, vp, vp, vp, vp, i32, vp, vp],
+                                       i32),
     "st_engine_kernel_launches": ([], u64),
     "st_engine_build_info": ([], cstr),
     "st_engine_measure_fp64_peak": ([C.c_int], C.c_double),

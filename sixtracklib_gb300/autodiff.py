@@ -9,15 +9,17 @@ gradients of a loss on the final coordinates with respect to
 
 through :class:`TrackFunction`, a ``torch.autograd.Function`` whose forward
 is the engine's until-turn tracking kernel and whose backward is the
-engine's hand-written adjoint kernel (``st_DeviceLattice_adjoint_turn``), one
-launch per turn, last turn first.
+engine's hand-written adjoint kernel (``st_DeviceLattice_adjoint_turns``),
+last checkpoint segment first.
 
 Memory: the forward stores the particle columns every ``checkpoint_every``
-turns; the backward recomputes the turn-boundary states of one segment at a
-time from its checkpoint (the tracking kernel is deterministic, so the
-recomputed states are the forward's states bit for bit) and reverses the
-segment's turns.  Peak extra memory is ``(checkpoint_every + 1 + turns /
-checkpoint_every)`` column blocks of ``168 * n`` bytes.
+turns (``turns / checkpoint_every + 1`` column blocks of ``168 * n`` bytes).
+The backward works one segment at a time, either reversing it in one launch
+from the states at its two ends (``reconstruct="inverse"``: the maps are
+inverted element by element) or recomputing its turn-boundary states from
+the checkpoint first (``reconstruct="recompute"``: ``checkpoint_every + 1``
+more blocks; the tracking kernel is deterministic, so the recomputed states
+are the forward's states bit for bit).
 
 Conventions: delta is the independent longitudinal coordinate; rpp, rvv and
 psigma follow it as NS(Particles_update_delta_value) defines them
@@ -123,28 +125,41 @@ class DifferentiableLattice:
         if rc != 0:
             raise RuntimeError("set_parameters: " + _native.last_error())
 
-    def adjoint_turn(self, start, end, lam, turn: int, grad=None) -> None:
-        """dL/d(coordinates at the start of `turn`) from dL/d(at its end),
-        in place in `lam` (6 x n); parameter contributions added to `grad`
-        (dL/d bal or voltage, per parameter), if given."""
+    def adjoint_turns(self, start, end, lam, turn_begin: int, turn_end: int, grad=None) -> None:
+        """dL/d(coordinates at turn_begin) from dL/d(coordinates at
+        turn_end), in place in `lam` (6 x n); parameter contributions added
+        to `grad` (dL/d bal or voltage, per parameter), if given.  `start`
+        and `end` are the column blocks at the two turns."""
         n = _check_cols(start)
         if _check_cols(end) != n or tuple(lam.shape) != (6, n) or not lam.is_contiguous():
-            raise ValueError("adjoint_turn: inconsistent shapes")
+            raise ValueError("adjoint_turns: inconsistent shapes")
         if grad is not None and self.num_params:
             pbeg, pkind, pid = self._tables(start.device)
-            tabs = (pbeg.data_ptr(), pkind.data_ptr(), pid.data_ptr(), grad.data_ptr())
+            tabs = (pbeg.data_ptr(), pkind.data_ptr(), pid.data_ptr(), self.num_params,
+                    grad.data_ptr())
         else:
-            tabs = (None, None, None, None)
-        rc = self._lib.st_DeviceLattice_adjoint_turn(
-            self.tracker._ptr, start.data_ptr(), end.data_ptr(), n, int(turn), lam.data_ptr(),
-            *tabs, _stream_handle(start))
+            tabs = (None, None, None, 0, None)
+        rc = self._lib.st_DeviceLattice_adjoint_turns(
+            self.tracker._ptr, start.data_ptr(), end.data_ptr(), n, int(turn_begin),
+            int(turn_end), lam.data_ptr(), *tabs, _stream_handle(start))
         if rc != 0:
-            raise RuntimeError("adjoint_turn: " + _native.last_error())
+            raise RuntimeError("adjoint: " + _native.last_error())
 
-    def track(self, coords, values, cols, until_turn: int, checkpoint_every: int = 100):
-        """Differentiable tracking: ``(final coordinates 6 x n, final state n)``."""
+    def track(self, coords, values, cols, until_turn: int, checkpoint_every: int = 100,
+              reconstruct: str = "inverse"):
+        """Differentiable tracking: ``(final coordinates 6 x n, final state n)``.
+
+        ``reconstruct`` selects how the backward pass obtains the states
+        inside a checkpoint segment: ``"inverse"`` reverses the whole segment
+        in one launch, reconstructing each element's input by inverting the
+        map (no recomputation; the reconstruction is re-anchored at every
+        checkpoint); ``"recompute"`` re-tracks the segment from its
+        checkpoint storing every turn boundary, then reverses one turn per
+        launch (re-anchored every turn, ~1 forward pass more work)."""
+        if reconstruct not in ("inverse", "recompute"):
+            raise ValueError("reconstruct must be 'inverse' or 'recompute'")
         return TrackFunction.apply(coords, values, self, cols, int(until_turn),
-                                   int(checkpoint_every))
+                                   int(checkpoint_every), reconstruct)
 
 
 def apply_values(elements: Elements, params, values) -> Elements:
@@ -225,7 +240,7 @@ def _make_function():
 
     class _Track(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, coords, values, lat, cols, until_turn, every):
+        def forward(ctx, coords, values, lat, cols, until_turn, every, reconstruct):
             if every < 1:
                 raise ValueError("checkpoint_every must be >= 1")
             lat.set_values(values)
@@ -240,9 +255,10 @@ def _make_function():
                 t = t1
                 if t < until_turn:
                     ckpts[t] = work.clone()
-            ctx.lat, ctx.ckpts, ctx.t0, ctx.until, ctx.every = lat, ckpts, t0, until_turn, every
+            ckpts[max(t, t0)] = work
+            ctx.lat, ctx.ckpts, ctx.every, ctx.reconstruct = lat, ckpts, every, reconstruct
             ctx.values = values.detach().clone() if torch.is_tensor(values) else values
-            ctx.coords_meta = (coords.dtype, coords.device)
+            ctx.coords_dtype = coords.dtype
             out = coordinates(work).clone().to(coords.dtype)
             state = work[COL["state"]].clone()
             ctx.mark_non_differentiable(state)
@@ -251,28 +267,36 @@ def _make_function():
         @staticmethod
         def backward(ctx, g_out, g_state):
             lat = ctx.lat
-            n = next(iter(ctx.ckpts.values())).shape[1]
-            dev = next(iter(ctx.ckpts.values())).device
+            turns = sorted(ctx.ckpts)
+            first = ctx.ckpts[turns[0]]
+            n, dev = first.shape[1], first.device
             if g_out is None:
                 lam = torch.zeros((6, n), dtype=torch.float64, device=dev)
             else:
                 lam = g_out.detach().to(torch.float64).contiguous().clone()
             grad = torch.zeros(lat.num_params, dtype=torch.float64, device=dev)
             lat.set_values(ctx.values)
-            for ts in sorted(ctx.ckpts, reverse=True):
-                te = min(ts + ctx.every, ctx.until)
-                blocks = [ctx.ckpts[ts]]
-                cur = ctx.ckpts[ts].clone()
+            blocks = None
+            for ts, te in reversed(list(zip(turns[:-1], turns[1:]))):
+                if ctx.reconstruct == "inverse":
+                    lat.adjoint_turns(ctx.ckpts[ts], ctx.ckpts[te], lam, ts, te, grad)
+                    continue
+                # turn-boundary states of the segment, launched back to back
+                if blocks is None or blocks.shape[0] < te - ts + 1:
+                    blocks = torch.empty((te - ts + 1,) + tuple(first.shape), dtype=first.dtype,
+                                         device=dev)
+                blocks[0].copy_(ctx.ckpts[ts])
                 for t in range(ts, te):
-                    _track_checked(lat, cur, t + 1)
-                    blocks.append(cur.clone())
+                    blocks[t - ts + 1].copy_(blocks[t - ts])
+                    lat.tracker.launch_until(blocks[t - ts + 1], t + 1)
+                st = lat.tracker.last_status()
+                if st != 0:
+                    raise RuntimeError(f"tracking failed (status {st}): " + _native.last_error())
                 for t in range(te - 1, ts - 1, -1):
-                    lat.adjoint_turn(blocks[t - ts], blocks[t - ts + 1], lam, t, grad)
-                del blocks
-            dtype, _ = ctx.coords_meta
+                    lat.adjoint_turns(blocks[t - ts], blocks[t - ts + 1], lam, t, t + 1, grad)
             g_values = grad * torch.from_numpy(lat.scales).to(dev)
             if torch.is_tensor(ctx.values):
                 g_values = g_values.to(ctx.values.dtype)
-            return lam.to(dtype), g_values, None, None, None, None
+            return lam.to(ctx.coords_dtype), g_values, None, None, None, None, None
 
     return _Track

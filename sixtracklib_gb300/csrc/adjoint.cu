@@ -1,4 +1,4 @@
-// adjoint.cu -- reverse-mode derivative of one turn of tracking.
+// adjoint.cu -- reverse-mode derivative of until-turn tracking.
 //
 // For a loss L on the particles' final coordinates u = (x, px, y, py, zeta,
 // delta), the adjoint lambda = dL/du is carried backwards through the
@@ -10,16 +10,21 @@
 //
 // Every differentiable map here is explicitly invertible (drifts and
 // rotations trivially, thin kicks because they leave x and y unchanged, the
-// cavity because it preserves tau = zeta / (beta0 rvv)).  So one launch
-// reverses one turn without a tape: each thread starts from its particle's
-// end-of-turn state, and for each element, last to first, restores the
-// element's input from its output and applies the transposed Jacobian at
-// that input.  A particle lost in the turn starts from the element where it
-// stopped (at_element).  The reconstruction error is rounding-level per
-// turn; the caller re-anchors every turn from stored turn-boundary states.
+// cavity because it preserves tau = zeta / (beta0 rvv)).  So the reverse
+// sweep needs no tape: each thread holds one particle's state and adjoint in
+// registers and, for each element, last to first, restores the element's
+// input from its output and applies the transposed Jacobian at that input.
+// One launch reverses a range of turns [turn_begin, turn_end) from the
+// states stored at both ends: a particle starts from its state at
+// turn_end, or, if it was lost inside the range, from the element where it
+// stopped (its at_turn / at_element).  The reconstruction error grows by
+// rounding each element; callers bound it by re-anchoring at stored turn
+// boundaries (every turn when the caller recomputes the per-turn states,
+// every checkpoint otherwise).
+//
 // All lanes of a warp walk the same element at the same time, so parameter
-// contributions are reduced with warp shuffles and added with one atomic
-// per warp.
+// contributions are reduced with warp shuffles, summed per CTA in shared
+// memory and added to the global gradient once per CTA and launch.
 //
 // Apertures contribute no derivative (a loss is a discontinuity).  Lattices
 // with elements that have no adjoint here (RF multipole, beam-beam, space
@@ -38,20 +43,30 @@ namespace stg {
 namespace {
 
 constexpr int kAdjThreads = 128;
+// Parameter sums: per-thread columns in shared memory while they fit
+// (no reduction on the FP64 pipe until the end of the launch), else per-CTA
+// slots fed by warp reductions, else global atomics.
+constexpr int kMaxColumnSlots = 96;   // 96 x 128 threads x 8 B = 96 KiB
+constexpr int kMaxSmemSlots = 4096;   // 32 KiB
+enum AccMode : int32_t { ACC_GLOBAL = 0, ACC_CTA = 1, ACC_COLUMNS = 2 };
 
 struct AdjParams {
     const uint64_t *stream;
     const int64_t *elem_offset;
     int64_t num_elements;
-    const uint64_t *end;     // 21 x n: states at the end of the turn
+    const uint64_t *start;   // 21 x n: states at turn_begin
+    const uint64_t *end;     // 21 x n: states at turn_end
     int64_t n;
-    const int64_t *idx;      // particles alive at the start of the turn
+    int64_t turn_begin, turn_end;
+    const int64_t *idx;      // particles alive at turn_begin with work before turn_end
     const int64_t *count;
     double *lam;             // 6 x n (x px y py zeta delta): in end of turn, out start
     const int32_t *pbeg;     // num_elements + 1 offsets into the parameter list (or null)
     const int32_t *pkind;    // bal index (>= 0) or -1 for a cavity voltage
     const int32_t *pid;      // gradient slot of the entry
     double *grad;            // dL/d(bal or voltage) per gradient slot
+    int32_t slots;           // number of gradient slots
+    int32_t acc;             // AccMode
 };
 
 struct Lam {
@@ -60,6 +75,10 @@ struct Lam {
 
 struct RState {
     double x, px, y, py, zeta, delta, rpp, rvv;
+    // functions of delta, constant between cavities
+    double drvv;   // d rvv / d delta
+    double drpp;   // d rpp / d delta = -rpp^2
+    double rvvm1;  // rvv - 1
     double beta0, chi, q, energy0;
 };
 
@@ -76,10 +95,35 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-__device__ __forceinline__ void add_grad(const AdjParams &a, int32_t j, double g)
+__device__ __forceinline__ double drvv_of(double delta, double beta0)
 {
-    g = warp_sum(g);
-    if ((threadIdx.x & 31) == 0 && g != 0.0) atomicAdd(&a.grad[a.pid[j]], g);
+    double const Q = q_of_delta(delta, beta0);
+    return (1.0 - beta0 * beta0) / (Q * Q * Q);
+}
+
+__device__ __forceinline__ void set_delta_terms(RState &s)
+{
+    s.drvv = drvv_of(s.delta, s.beta0);
+    s.drpp = -s.rpp * s.rpp;
+    s.rvvm1 = s.rvv - 1.0;
+}
+
+extern __shared__ double s_grad[];
+
+// `on` lanes contribute g; all lanes of the warp call this together.
+__device__ __forceinline__ void add_grad(const AdjParams &a, int32_t j, double g, bool on)
+{
+    if (a.acc == ACC_COLUMNS) {
+        if (on) s_grad[a.pid[j] * kAdjThreads + threadIdx.x] += g;
+        return;
+    }
+    g = warp_sum(on ? g : 0.0);
+    if ((threadIdx.x & 31) == 0 && g != 0.0) {
+        if (a.acc == ACC_CTA)
+            atomicAdd(&s_grad[a.pid[j]], g);
+        else
+            atomicAdd(&a.grad[a.pid[j]], g);
+    }
 }
 
 // P(z) = sum_k (bal[2k] + i bal[2k+1]) z^k and P'(z), z = x + i y, by Horner.
@@ -90,7 +134,15 @@ __device__ __forceinline__ void horner2(const uint64_t *bal, int n, double x, do
     pi = W(bal[2 * n + 1]);
     dr = 0.0;
     di = 0.0;
-    for (int k = n - 1; k >= 0; --k) {
+    if (n > 0) {  // first step: P' = a_n, P = a_n z + a_(n-1)
+        dr = pr;
+        di = pi;
+        double const npr = fma(pr, x, fma(-pi, y, W(bal[2 * n - 2])));
+        double const npi = fma(pr, y, fma(pi, x, W(bal[2 * n - 1])));
+        pr = npr;
+        pi = npi;
+    }
+    for (int k = n - 2; k >= 0; --k) {
         double const ndr = fma(dr, x, fma(-di, y, pr));
         double const ndi = fma(dr, y, fma(di, x, pi));
         double const npr = fma(pr, x, fma(-pi, y, W(bal[2 * k])));
@@ -114,19 +166,24 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
     switch (op) {
     case OP_DRIFT: {  // be_drift/track.h:45-67
         if (!on) break;
+        // input from output: x -= L rpp px, zeta -= L (rvv - 1 - (xp^2 + yp^2) / 2)
         double const L = W(rec[1]);
         double const rpp = s.rpp, px = s.px, py = s.py;
-        double const xp = px * rpp, yp = py * rpp;
-        s.x -= xp * L;
-        s.y -= yp * L;
-        s.zeta -= L * (s.rvv - (1.0 + (xp * xp + yp * yp) * 0.5));
-        double const Q = q_of_delta(s.delta, s.beta0);
-        double const drvv = (1.0 - s.beta0 * s.beta0) / (Q * Q * Q);
-        double const drpp = -rpp * rpp;
+        double const a_ = L * rpp;
+        s.x = fma(-a_, px, s.x);
+        s.y = fma(-a_, py, s.y);
+        double const p2 = fma(py, py, px * px);
+        double const s2 = rpp * p2;          // xp px + yp py
+        double const h = rpp * s2;           // xp^2 + yp^2
+        s.zeta = fma(L, fma(0.5, h, -s.rvvm1), s.zeta);
+        // lambda: d(out)/d(px, py, delta) with rpp(delta), rvv(delta)
         double const lx = l.x, ly = l.y, lz = l.z;
-        l.px += L * rpp * (lx - lz * xp);
-        l.py += L * rpp * (ly - lz * yp);
-        l.d += L * (drpp * (lx * px + ly * py) + lz * (drvv - (xp * px + yp * py) * drpp));
+        double const lzr = lz * rpp;
+        l.px = fma(a_, fma(-lzr, px, lx), l.px);
+        l.py = fma(a_, fma(-lzr, py, ly), l.py);
+        double const s1 = fma(ly, py, lx * px);
+        double const w_ = fma(lz, s.drvv, s.drpp * fma(-lz, s2, s1));
+        l.d = fma(L, w_, l.d);
         break;
     }
     case OP_DRIFT_EXACT: {  // be_drift/track.h:71-97
@@ -142,8 +199,7 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         s.zeta -= s.rvv * L - opd * lpzi;
         double const D3 = D2 * D;
         double const a_px = L * px / D3, a_py = L * py / D3, a_d = -L * opd / D3;
-        double const Q = q_of_delta(s.delta, s.beta0);
-        double const drvv = (1.0 - s.beta0 * s.beta0) / (Q * Q * Q);
+        double const drvv = s.drvv;
         double const lx = l.x, ly = l.y, lz = l.z;
         l.px += lx * (lpzi + px * a_px) + ly * (py * a_px) - lz * opd * a_px;
         l.py += lx * (px * a_py) + ly * (lpzi + py * a_py) - lz * opd * a_py;
@@ -189,21 +245,27 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         }
         if (a.pbeg) {
             // d(dpx, dpy)/d bal[2k] = chi (-Re z^k, Im z^k); / d bal[2k+1] = chi (Im z^k, Re z^k)
+            double const cx = chi * lpx, cy = chi * lpy;
             for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j) {
                 int const k2 = a.pkind[j];
                 double g = 0.0;
                 if (on && k2 >= 0) {
+                    int const kk = k2 >> 1;
                     double zr = 1.0, zi = 0.0;
-                    for (int k = 0; k < k2 / 2; ++k) {
-                        double const t = zr * x - zi * y;
-                        zi = zr * y + zi * x;
-                        zr = t;
+                    if (kk > 0) {
+                        zr = x;
+                        zi = y;
+                        for (int k = 1; k < kk; ++k) {
+                            double const t = fma(zr, x, -zi * y);
+                            zi = fma(zr, y, zi * x);
+                            zr = t;
+                        }
                     }
-                    g = (k2 & 1) ? chi * (lpx * zi + lpy * zr) : chi * (-lpx * zr + lpy * zi);
-                    if (length > 0.0 && k2 == 0) g -= lpx * chi * hxl * x / length;
-                    if (length > 0.0 && k2 == 1) g += lpy * chi * hyl * y / length;
+                    g = (k2 & 1) ? fma(cx, zi, cy * zr) : fma(-cx, zr, cy * zi);
+                    if (length > 0.0 && k2 == 0) g -= cx * hxl * x / length;
+                    if (length > 0.0 && k2 == 1) g += cy * hyl * y / length;
                 }
-                add_grad(a, j, g);
+                add_grad(a, j, g, on);
             }
         }
         break;
@@ -236,6 +298,9 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
             s.zeta = zeta;
             // transposed Jacobian
             double const drvv = (1.0 - b2) / (Qi * Qi * Qi);
+            s.drvv = drvv;
+            s.drpp = -s.rpp * s.rpp;
+            s.rvvm1 = rvv - 1.0;
             double const dEc = s.q * V * cph / s.energy0;
             double const dP_dzeta = -dEc * kf / (beta0 * rvv);
             double const dP_ddelta = dEc * kf * zeta / (beta0 * rvv * rvv) * drvv + b2 * opd / Qi;
@@ -250,7 +315,7 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         }
         if (a.pbeg) {
             for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j)
-                add_grad(a, j, (on && a.pkind[j] < 0) ? gV : 0.0);
+                add_grad(a, j, a.pkind[j] < 0 ? gV : 0.0, on);
         }
         break;
     }
@@ -286,19 +351,36 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
     }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
+__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams a)
 {
+    int const acc_words = a.acc == ACC_COLUMNS ? a.slots * kAdjThreads
+                          : (a.acc == ACC_CTA ? a.slots : 0);
+    for (int j = threadIdx.x; j < acc_words; j += blockDim.x) s_grad[j] = 0.0;
+    __syncthreads();
     int64_t const t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t const cnt = *a.count;
     bool const part = t < cnt;
     int64_t const n = a.n;
     int64_t const i = part ? a.idx[t] : 0;
+    int64_t const E = a.num_elements;
     RState s{};
     Lam l{0, 0, 0, 0, 0, 0};
-    int64_t last = -1;  // last element the particle went through in this turn
+    // turns [t_first, t_last] of this particle lie in the range; in turn
+    // t_last it went through elements 0..e_last
+    int64_t t_first = a.turn_end, t_last = a.turn_begin - 1, e_last = -1;
     if (part) {
+        const int64_t *ks = reinterpret_cast<const int64_t *>(a.start);
         const double *d = reinterpret_cast<const double *>(a.end);
         const int64_t *k = reinterpret_cast<const int64_t *>(a.end);
+        t_first = ks[19 * n + i] > a.turn_begin ? ks[19 * n + i] : a.turn_begin;
+        if (k[20 * n + i] == 1) {
+            t_last = a.turn_end - 1;
+            e_last = E - 1;
+        } else {
+            int64_t const at = k[19 * n + i], ae = k[18 * n + i];
+            t_last = at < a.turn_end ? at : a.turn_end - 1;
+            e_last = ae < E ? ae : E - 1;
+        }
         double const p0c = d[4 * n + i], mass0 = d[1 * n + i];
         s.beta0 = d[2 * n + i];
         s.x = d[6 * n + i];
@@ -312,9 +394,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
         s.chi = d[15 * n + i];
         s.q = d[0 * n + i] * d[16 * n + i];
         s.energy0 = sqrt(p0c * p0c + mass0 * mass0);
-        int64_t const ae = k[18 * n + i];
-        last = (k[20 * n + i] == 1) ? a.num_elements - 1
-                                    : (ae < a.num_elements ? ae : a.num_elements - 1);
+        set_delta_terms(s);
         l.x = a.lam[0 * n + i];
         l.px = a.lam[1 * n + i];
         l.y = a.lam[2 * n + i];
@@ -322,13 +402,18 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
         l.z = a.lam[4 * n + i];
         l.d = a.lam[5 * n + i];
     }
-    long long wl = last;
-    for (int o = 16; o > 0; o >>= 1) {
-        long long const v = __shfl_xor_sync(0xFFFFFFFFu, wl, o);
-        wl = v > wl ? v : wl;
+    for (int64_t turn = a.turn_end - 1; turn >= a.turn_begin; --turn) {
+        bool const act = part && turn >= t_first && turn <= t_last;
+        if (!__any_sync(0xFFFFFFFFu, act)) continue;
+        long long const mine = act ? (turn == t_last ? e_last : E - 1) : -1;
+        long long wl = mine;
+        for (int o = 16; o > 0; o >>= 1) {
+            long long const v = __shfl_xor_sync(0xFFFFFFFFu, wl, o);
+            wl = v > wl ? v : wl;
+        }
+        for (int64_t e = (int64_t)wl; e >= 0; --e)
+            reverse_elem(s, l, a.stream + a.elem_offset[e], a, e, act && e <= mine);
     }
-    for (int64_t e = (int64_t)wl; e >= 0; --e)
-        reverse_elem(s, l, a.stream + a.elem_offset[e], a, e, part && e <= last);
     if (part) {
         a.lam[0 * n + i] = l.x;
         a.lam[1 * n + i] = l.px;
@@ -336,6 +421,17 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
         a.lam[3 * n + i] = l.py;
         a.lam[4 * n + i] = l.z;
         a.lam[5 * n + i] = l.d;
+    }
+    __syncthreads();
+    if (a.acc == ACC_COLUMNS) {
+        for (int j = threadIdx.x; j < a.slots; j += blockDim.x) {
+            double sum = 0.0;
+            for (int c = 0; c < kAdjThreads; ++c) sum += s_grad[j * kAdjThreads + c];
+            if (sum != 0.0) atomicAdd(&a.grad[j], sum);
+        }
+    } else if (a.acc == ACC_CTA) {
+        for (int j = threadIdx.x; j < a.slots; j += blockDim.x)
+            if (s_grad[j] != 0.0) atomicAdd(&a.grad[j], s_grad[j]);
     }
 }
 
@@ -345,10 +441,11 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_turn_kernel(AdjParams a)
 
 using namespace stg;
 
-extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
-    st_DeviceLattice *lat, const void *d_start, const void *d_end, int64_t n, int64_t turn,
-    double *d_lam, const int32_t *d_param_begin, const int32_t *d_param_kind,
-    const int32_t *d_param_id, double *d_grad, void *stream)
+extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
+    st_DeviceLattice *lat, const void *d_start, const void *d_end, int64_t n,
+    int64_t turn_begin, int64_t turn_end, double *d_lam, const int32_t *d_param_begin,
+    const int32_t *d_param_kind, const int32_t *d_param_id, int32_t num_slots, double *d_grad,
+    void *stream)
 {
     clear_error();
     LatticeLaunchView v;
@@ -364,9 +461,13 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
                   "(RF multipole, beam-beam, space charge or a disabled map)");
         return -1;
     }
-    if (n <= 0 || v.num_elements == 0) return 0;
+    if (turn_end < turn_begin) {
+        set_error("adjoint: turn_end < turn_begin");
+        return -1;
+    }
+    if (n <= 0 || v.num_elements == 0 || turn_end == turn_begin) return 0;
     if (!d_start || !d_end || !d_lam ||
-        (d_param_begin && (!d_param_kind || !d_param_id || !d_grad))) {
+        (d_param_begin && (!d_param_kind || !d_param_id || !d_grad || num_slots <= 0))) {
         set_error("adjoint: missing device buffer");
         return -1;
     }
@@ -377,8 +478,8 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
     uint64_t *scratch = device_scratch(v.device, select_scratch_words(n));
     if (!scratch) return -1;
     int64_t *idx = nullptr, *count = nullptr;
-    // alive at the start of the turn: state 1 and at_turn < turn + 1
-    int rc = launch_select(static_cast<const uint64_t *>(d_start), n, 0, n, MODE_UNTIL, turn + 1,
+    // alive at turn_begin with turns left before turn_end
+    int rc = launch_select(static_cast<const uint64_t *>(d_start), n, 0, n, MODE_UNTIL, turn_end,
                            scratch, &idx, &count, stream);
     if (rc != 0) {
         set_error(std::string("adjoint selection: ") + cudaGetErrorString((cudaError_t)rc));
@@ -388,8 +489,11 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
     a.stream = v.stream;
     a.elem_offset = v.elem_offset;
     a.num_elements = v.num_elements;
+    a.start = static_cast<const uint64_t *>(d_start);
     a.end = static_cast<const uint64_t *>(d_end);
     a.n = n;
+    a.turn_begin = turn_begin;
+    a.turn_end = turn_end;
     a.idx = idx;
     a.count = count;
     a.lam = d_lam;
@@ -397,8 +501,25 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turn(
     a.pkind = d_param_kind;
     a.pid = d_param_id;
     a.grad = d_grad;
+    a.slots = d_param_begin ? num_slots : 0;
+    a.acc = (a.slots > 0 && a.slots <= kMaxColumnSlots) ? ACC_COLUMNS
+            : (a.slots > 0 && a.slots <= kMaxSmemSlots ? ACC_CTA : ACC_GLOBAL);
+    size_t const smem = a.acc == ACC_COLUMNS ? (size_t)a.slots * kAdjThreads * sizeof(double)
+                        : (a.acc == ACC_CTA ? (size_t)a.slots * sizeof(double) : 0);
+    if (smem > 48 * 1024) {
+        static bool attr_set[64] = {};
+        if (v.device >= 0 && v.device < 64 && !attr_set[v.device]) {
+            if (cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)((size_t)kMaxColumnSlots * kAdjThreads * 8)) !=
+                cudaSuccess) {
+                set_error("adjoint: cannot raise the shared-memory limit");
+                return -1;
+            }
+            attr_set[v.device] = true;
+        }
+    }
     unsigned const blocks = (unsigned)((n + kAdjThreads - 1) / kAdjThreads);
-    adjoint_turn_kernel<<<blocks, kAdjThreads, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    adjoint_kernel<<<blocks, kAdjThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
     rc = (int)cudaGetLastError();
     if (rc != 0) {
         set_error(std::string("adjoint launch: ") + cudaGetErrorString((cudaError_t)rc));

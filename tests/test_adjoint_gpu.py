@@ -61,7 +61,7 @@ def _dual_grads(e, params, blk, T, w):
     return g_coords, g_params, vals, st
 
 
-def _gpu_grads(e, params, blk, T, w, config="mode=exact", every=7):
+def _gpu_grads(e, params, blk, T, w, config="mode=exact", every=7, reconstruct="inverse"):
     torch = _torch()
     from sixtracklib_gb300.autodiff import DifferentiableLattice, coordinates
 
@@ -70,7 +70,8 @@ def _gpu_grads(e, params, blk, T, w, config="mode=exact", every=7):
     coords = coordinates(cols).clone().requires_grad_(True)
     values = torch.tensor(lat.initial_values, dtype=torch.float64, device="cuda",
                           requires_grad=True)
-    out, state = lat.track(coords, values, cols, T, checkpoint_every=every)
+    out, state = lat.track(coords, values, cols, T, checkpoint_every=every,
+                           reconstruct=reconstruct)
     loss = (torch.from_numpy(w).cuda() * out).sum()
     loss.backward()
     return (coords.grad.cpu().numpy(), values.grad.cpu().numpy(),
@@ -81,8 +82,9 @@ def _rel_rows(a, b):
     return np.max(np.abs(a - b), axis=-1) / np.max(np.abs(b), axis=-1)
 
 
+@pytest.mark.parametrize("reconstruct", ["inverse", "recompute"])
 @pytest.mark.parametrize("case", ["fodo", "misc"])
-def test_adjoint_matches_dual_numbers(case):
+def test_adjoint_matches_dual_numbers(case, reconstruct):
     if case == "fodo":
         e, params = lattices.learnable_fodo_ring()
         T, n = 30, 600
@@ -92,7 +94,7 @@ def test_adjoint_matches_dual_numbers(case):
     blk = _beam(n, seed=21)
     w = np.random.default_rng(2).normal(size=(6, n)) / SIGMA[:, None]
     gc_d, gp_d, vals_d, st_d = _dual_grads(e, params, blk, T, w)
-    gc, gp, vals, st = _gpu_grads(e, params, blk, T, w)
+    gc, gp, vals, st = _gpu_grads(e, params, blk, T, w, reconstruct=reconstruct)
     assert np.array_equal(st, st_d)
     assert 0 < (st == 0).sum() < n
     np.testing.assert_allclose(vals, vals_d, rtol=1e-12, atol=1e-18)
@@ -116,11 +118,19 @@ def test_checkpoint_interval_does_not_change_gradients():
     T, n = 12, 256
     blk = _beam(n, seed=8)
     w = np.random.default_rng(4).normal(size=(6, n)) / SIGMA[:, None]
-    results = [_gpu_grads(e, params, blk, T, w, every=k) for k in (1, 5, 12, 100)]
-    for gc, gp, vals, st in results[1:]:
-        assert np.array_equal(gc, results[0][0])  # same kernels, same order
-        np.testing.assert_allclose(gp, results[0][1], rtol=1e-12)  # atomics: order varies
-        assert np.array_equal(vals, results[0][2])
+    # recomputed turn states: the same kernels in the same order
+    res = [_gpu_grads(e, params, blk, T, w, every=k, reconstruct="recompute")
+           for k in (1, 5, 12, 100)]
+    for gc, gp, vals, st in res[1:]:
+        assert np.array_equal(gc, res[0][0])
+        np.testing.assert_allclose(gp, res[0][1], rtol=1e-12)  # atomics: order varies
+        assert np.array_equal(vals, res[0][2])
+    # reconstructed states: re-anchored at different turns, rounding-level changes
+    for k in (1, 5, 12, 100):
+        gc, gp, vals, st = _gpu_grads(e, params, blk, T, w, every=k)
+        assert np.array_equal(vals, res[0][2])
+        assert np.all(_rel_rows(gc, res[0][0]) < 1e-11)
+        assert np.max(np.abs(gp - res[0][1])) < 1e-10 * np.max(np.abs(res[0][1]))
 
 
 def test_adjoint_vs_central_finite_differences():
