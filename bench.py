@@ -15,6 +15,12 @@ particle passes counts once (lost particles stop counting where they are lost).
               launch / launch time, against the DFMA peak measured in-process;
   cpu_baseline  the CPU oracle (C restatement of the reference loop, OpenMP
               over particles) on a bounded sample of the same workload.
+  adjoint     the differentiable-tracking workload: the FODO ring with 64
+              quadrupole and 16 sextupole strengths as parameters, 65,536
+              Gaussian protons, 1,000 turns, a checkpoint every 100 turns;
+              loss = mean over surviving particles of x^2 + y^2 plus a
+              penalty on the lost fraction; forward and backward timed with
+              CUDA events; ratio = backward / plain tracking of the same turns.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -50,6 +56,7 @@ def parse():
     ap.add_argument("--blocks-per-sm", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -233,6 +240,61 @@ def e2e_measure(ring, parts, steps, warmup, mode, threads, blocks_per_sm):
             "d2h_bytes_per_step": nbytes, "ms_per_step": dt / steps * 1e3}
 
 
+def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
+    """Forward and backward of differentiable tracking (see module doc)."""
+    import torch
+
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.autodiff import DifferentiableLattice, coordinates
+
+    ring, params = lattices.learnable_fodo_ring()
+    lat = DifferentiableLattice(ring, params, f"mode={mode}")
+    cols = torch.from_numpy(lattices.gaussian_particles(n, seed=1).block.copy()
+                            .view(np.int64)).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    out = {"workload": f"learnable FODO ring ({len(ring)} elements, {len(params)} strengths), "
+                       f"{n} particles, {turns} turns, checkpoint every {every}",
+           "mode": mode, "particles": n, "turns": turns, "checkpoint_every": every,
+           "parameters": len(params)}
+    for rep in range(2):  # warm-up, then timed
+        c = cols.clone()
+        torch.cuda.synchronize(dev)
+        a, b = ev(), ev()
+        a.record(stream)
+        lat.tracker.launch_until(c, turns)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        out["plain_forward_ms"] = a.elapsed_time(b)
+    for rec in ("inverse", "recompute"):
+        for rep in range(2):
+            coords = coordinates(cols).clone().requires_grad_(True)
+            values = torch.tensor(lat.initial_values, dtype=torch.float64, device=dev,
+                                  requires_grad=True)
+            torch.cuda.synchronize(dev)
+            a, b, c2 = ev(), ev(), ev()
+            a.record(stream)
+            fin, state = lat.track(coords, values, cols, turns, checkpoint_every=every,
+                                   reconstruct=rec)
+            alive = state == 1
+            loss = (((fin[0] ** 2 + fin[2] ** 2) * alive).sum() / alive.sum().clamp(min=1)
+                    + 1e-3 * (~alive).sum() / n)
+            b.record(stream)
+            loss.backward()
+            c2.record(stream)
+            torch.cuda.synchronize(dev)
+        key = "" if rec == "inverse" else "recompute_"
+        out[key + "forward_ms"] = a.elapsed_time(b)
+        out[key + "backward_ms"] = b.elapsed_time(c2)
+        out[key + "ratio"] = out[key + "backward_ms"] / out["plain_forward_ms"]
+        out[key + "grad_norm"] = float(values.grad.norm())
+    out["reconstruct"] = "inverse (recompute_* keys: per-turn states recomputed)"
+    return out
+
+
 def aggregate_over_ranks(pet, elapsed, device):
     """Whole-job figures of a weak-scaling run: PET summed over ranks, time =
     the slowest rank's (every rank tracks its own particles, no exchange)."""
@@ -404,6 +466,11 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ring, parts, args.cpu_seconds)
+    if not args.no_adjoint:
+        try:
+            line["adjoint"] = adjoint_measure(dev, args.mode)
+        except Exception as exc:  # report, do not hide
+            line["adjoint"] = {"error": str(exc)}
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_measure(ring, parts, max(2, args.steps // 2), 1, args.mode,

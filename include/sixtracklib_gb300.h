@@ -490,6 +490,48 @@ st_track_status_t st_DeviceLattice_adjoint_turns(st_DeviceLattice *lat, const vo
                                                  const int32_t *d_param_kind,
                                                  const int32_t *d_param_id, int32_t num_slots,
                                                  double *d_grad, void *stream);
+/* ------------------------------------------------------------ batching */
+/* No reference counterpart (the reference tracks one lattice per job).  A
+ * batch tracks many lattice variants, each with its own device-resident
+ * particle block, with one persistent kernel: tiles of particles of all
+ * variants, longest lattice first, are taken by the CTAs from a global
+ * counter.  Results are bit-identical to st_DeviceLattice_track_until on each
+ * variant alone.  All lattices must be on one device with one arithmetic mode
+ * (the "mode" of their configuration).  config: threads_per_block,
+ * blocks_per_sm (1 or 2), stages (2..8), turns_per_launch; all optional. */
+typedef struct st_BatchTracker st_BatchTracker;
+st_BatchTracker *st_BatchTracker_new(st_DeviceLattice *const *lattices, int32_t num_variants,
+                                     const char *config);
+void st_BatchTracker_delete(st_BatchTracker *batch);
+/* One 21 x n column block per variant (device pointers; n may be 0).  The
+ * lattices and blocks must outlive the batch's use of them. */
+int32_t st_BatchTracker_set_particles(st_BatchTracker *batch, void *const *d_cols,
+                                      const int64_t *num_particles);
+/* Track every variant's particles until `until_turn`, in launches of
+ * turns_per_launch turns starting at from_turn (particles already past a
+ * launch's turn are left alone); synchronises `stream`, returns the status. */
+st_track_status_t st_BatchTracker_track_until(st_BatchTracker *batch, int64_t from_turn,
+                                              int64_t until_turn, void *stream);
+/* Capture the launches that advance every variant by turns_per_replay turns
+ * into a CUDA graph.  Each replay starts at the batch's turn counter (set by
+ * st_BatchTracker_set_turn, asynchronous on `stream`) and advances it. */
+int32_t st_BatchTracker_capture(st_BatchTracker *batch, int64_t turns_per_replay);
+int32_t st_BatchTracker_set_turn(st_BatchTracker *batch, int64_t turn, void *stream);
+int32_t st_BatchTracker_replay(st_BatchTracker *batch, void *stream);
+/* Synchronise `stream` and return the OR of the statuses since the last
+ * replay or track_until. */
+st_track_status_t st_BatchTracker_status(st_BatchTracker *batch, void *stream);
+int32_t st_BatchTracker_get_shape(const st_BatchTracker *batch, int32_t *threads_per_block,
+                                  int32_t *blocks_per_sm, int32_t *stages,
+                                  int32_t *turns_per_launch);
+/* Autotuner: times launch shapes (threads per block, register tier,
+ * shared-memory stages, turns per launch; coordinate descent, two passes)
+ * on a copy of the first sample_fraction of every variant's particles for
+ * trial_turns turns and keeps the fastest.  The batch's particles are not
+ * modified; a captured graph is dropped.  *best_ms: the winning trial. */
+int32_t st_BatchTracker_autotune(st_BatchTracker *batch, double sample_fraction,
+                                 int64_t trial_turns, double *best_ms);
+
 /* Kernel-launch counter (for launch accounting in benchmarks). */
 uint64_t st_engine_kernel_launches(void);
 /* Compile-time properties of the engine build. */

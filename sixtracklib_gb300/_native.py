@@ -80,6 +80,16 @@ _SIGNATURES = {
     "st_DeviceLattice_set_parameters": ([vp, i64, vp, vp, vp], i32),
     "st_DeviceLattice_adjoint_turns": ([vp, vp, vp, i64, i64, i64, vp, vp, vp, vp, i32, vp, vp],
                                        i32),
+    "st_BatchTracker_new": ([vp, i32, cstr], vp),
+    "st_BatchTracker_delete": ([vp], None),
+    "st_BatchTracker_set_particles": ([vp, vp, vp], i32),
+    "st_BatchTracker_track_until": ([vp, i64, i64, vp], i32),
+    "st_BatchTracker_capture": ([vp, i64], i32),
+    "st_BatchTracker_set_turn": ([vp, i64, vp], i32),
+    "st_BatchTracker_replay": ([vp, vp], i32),
+    "st_BatchTracker_status": ([vp, vp], i32),
+    "st_BatchTracker_get_shape": ([vp, vp, vp, vp, vp], i32),
+    "st_BatchTracker_autotune": ([vp, C.c_double, i64, vp], i32),
     "st_engine_kernel_launches": ([], u64),
     "st_engine_build_info": ([], cstr),
     "st_engine_measure_fp64_peak": ([C.c_int], C.c_double),

@@ -30,6 +30,7 @@ CUDA_SOURCES = {
     "compact.cu": [],
     "noalloc.cu": [],
     "adjoint.cu": [],
+    "batch.cu": [],
 }
 
 

@@ -52,6 +52,32 @@ int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_
                  void *stream);
 size_t track_smem_bytes(int stages, int chunk_words);
 
+// Batched tracking (track_kernel.cu): a work item is a tile of particles of
+// one lattice variant, starting at particle `first`.
+struct BatchItem {
+    int32_t variant;
+    int32_t pad_;
+    int64_t first;
+};
+
+struct BatchLaunch {
+    const TrackParams *variants;  // device: one per variant (mode MODE_UNTIL)
+    const BatchItem *items;       // device: longest first
+    int32_t num_items;
+    int32_t *counter;             // device: zero before the launch
+    const int64_t *base_turn;     // device: until_turn = *base_turn + turn_offset
+    int64_t turn_offset;
+    bool fast;
+    int threads, blocks_per_sm;
+    unsigned grid;
+    size_t smem;
+};
+
+// Set the kernel's shared-memory limit to `smem` and report how many CTAs
+// of `threads` fit on one SM.  Returns the CUDA error code.
+int batch_ctas_per_sm(bool fast, int threads, int blocks_per_sm, size_t smem, int *per_sm);
+int launch_batch(const BatchLaunch &b, void *stream);
+
 // Stable selection of the particles with work left (compact.cu): fills
 // idx / count inside `scratch` (select_scratch_words(i1 - i0) words).
 int64_t select_scratch_words(int64_t count);

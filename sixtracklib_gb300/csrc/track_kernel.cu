@@ -266,20 +266,27 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
 
 }  // namespace
 
-// Kernel. Block-uniform control flow: every thread walks every record of
-// every chunk of every turn the block needs; lanes whose particle is done
-// are predicated off inside apply().
-template <bool FAST, int MIN_BLOCKS>
-__global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS) track_kernel(TrackParams prm)
+__device__ __forceinline__ void mbar_inval(uint64_t *bar)
 {
-    extern __shared__ __align__(128) uint64_t smem[];
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// One CTA's share of a tracking call: particle t of the launch (an index
+// into prm.idx, or prm.i0 + t).  Block-uniform control flow: every thread
+// walks every record of every chunk of every turn the block needs; lanes
+// whose particle is done are predicated off inside apply().  `smem` holds
+// 16 words of mbarriers followed by prm.stages chunk buffers.  Returns with
+// every copy it issued complete; the caller invalidates the barriers before
+// the shared memory is used again.
+template <bool FAST>
+__device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, uint64_t *smem)
+{
     int const stages = prm.stages;
     int const cw = prm.chunk_words;
     uint64_t *bars = smem;                 // `stages` mbarriers (8 B each, padded to 16 words)
     uint64_t *bufs = smem + 16;            // stages * cw words
     __shared__ long long s_tmin;
 
-    int64_t const t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t i;
     bool valid;
     if (prm.idx) {  // compacted launch: only the particles with work left
@@ -470,10 +477,57 @@ __global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS) track_kernel(TrackPar
     k[20 * n + i] = p.state;
 }
 
+template <bool FAST, int MIN_BLOCKS>
+__global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS) track_kernel(TrackParams prm)
+{
+    extern __shared__ __align__(128) uint64_t smem[];
+    track_block<FAST>(prm, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, smem);
+}
+
+// Persistent batched kernel: each CTA takes work items (a tile of
+// blockDim.x particles of one lattice variant) from a global counter until
+// none is left, and tracks the tile until turn *base_turn + turn_offset with
+// that variant's lattice.  Items are ordered longest first by the host.
+template <bool FAST, int MIN_BLOCKS>
+__global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS)
+    batch_kernel(const TrackParams *variants, const BatchItem *items, int32_t num_items,
+                 int32_t *counter, const int64_t *base_turn, int64_t turn_offset)
+{
+    extern __shared__ __align__(128) uint64_t smem[];
+    __shared__ int32_t s_item;
+    int64_t const until = *base_turn + turn_offset;
+    while (true) {
+        __syncthreads();  // previous item done (barriers invalidated, s_item read)
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        int32_t const it = s_item;
+        if (it >= num_items) break;
+        BatchItem const w = items[it];
+        TrackParams prm = variants[w.variant];
+        prm.until_turn = until;
+        prm.idx = nullptr;
+        prm.count = nullptr;
+        prm.i0 = w.first;
+        prm.i1 = (w.first + blockDim.x < prm.n) ? w.first + blockDim.x : prm.n;
+        track_block<FAST>(prm, threadIdx.x, smem);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int b = 0; b < prm.stages; ++b) mbar_inval(&smem[b]);
+    }
+}
+
 template __global__ void track_kernel<false, 1>(TrackParams);
 template __global__ void track_kernel<true, 1>(TrackParams);
 template __global__ void track_kernel<false, 2>(TrackParams);
 template __global__ void track_kernel<true, 2>(TrackParams);
+template __global__ void batch_kernel<false, 1>(const TrackParams *, const BatchItem *, int32_t,
+                                                int32_t *, const int64_t *, int64_t);
+template __global__ void batch_kernel<true, 1>(const TrackParams *, const BatchItem *, int32_t,
+                                               int32_t *, const int64_t *, int64_t);
+template __global__ void batch_kernel<false, 2>(const TrackParams *, const BatchItem *, int32_t,
+                                                int32_t *, const int64_t *, int64_t);
+template __global__ void batch_kernel<true, 2>(const TrackParams *, const BatchItem *, int32_t,
+                                               int32_t *, const int64_t *, int64_t);
 
 }  // namespace stg
 
@@ -509,6 +563,48 @@ int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_
                    : launch_one<true, 1>(prm, (unsigned)blocks, threads, smem, s);
     return two ? launch_one<false, 2>(prm, (unsigned)blocks, threads, smem, s)
                : launch_one<false, 1>(prm, (unsigned)blocks, threads, smem, s);
+}
+
+template <bool FAST, int MB>
+static cudaError_t batch_occupancy(int threads, size_t smem, int *per_sm)
+{
+    cudaError_t err = cudaFuncSetAttribute(batch_kernel<FAST, MB>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<FAST, MB>, threads,
+                                                         smem);
+}
+
+int batch_ctas_per_sm(bool fast, int threads, int blocks_per_sm, size_t smem, int *per_sm)
+{
+    bool const two = blocks_per_sm >= 2;
+    cudaError_t err = fast ? (two ? batch_occupancy<true, 2>(threads, smem, per_sm)
+                                  : batch_occupancy<true, 1>(threads, smem, per_sm))
+                           : (two ? batch_occupancy<false, 2>(threads, smem, per_sm)
+                                  : batch_occupancy<false, 1>(threads, smem, per_sm));
+    return (int)err;
+}
+
+int launch_batch(const BatchLaunch &b, void *stream)
+{
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    bool const two = b.blocks_per_sm >= 2;
+#define STG_BATCH(F, M)                                                                         \
+    batch_kernel<F, M><<<b.grid, b.threads, b.smem, s>>>(b.variants, b.items, b.num_items,      \
+                                                         b.counter, b.base_turn, b.turn_offset)
+    if (b.fast) {
+        if (two)
+            STG_BATCH(true, 2);
+        else
+            STG_BATCH(true, 1);
+    } else {
+        if (two)
+            STG_BATCH(false, 2);
+        else
+            STG_BATCH(false, 1);
+    }
+#undef STG_BATCH
+    return (int)cudaGetLastError();
 }
 
 }  // namespace stg

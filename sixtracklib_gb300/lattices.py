@@ -130,6 +130,30 @@ def synthetic_ring(seed=20240601, n_cells=4000, n_extra_drift=1000,
     return e
 
 
+def variant_ring(seed: int, n_elements: int) -> Elements:
+    """A ring built like :func:`synthetic_ring`, scaled to about
+    ``n_elements`` elements (cells, split drifts, shifts, rotations,
+    apertures and cavities in the same proportions), with its own seeded
+    quadrupole ramp and multipole errors."""
+    f = max(n_elements, 100) / 20000.0
+    n_cells = max(4, int(round(4000 * f)))
+    n_extra = min(int(round(1000 * f)), n_cells)  # at most one split per cell pair
+    return synthetic_ring(seed=seed, n_cells=n_cells, n_extra_drift=n_extra,
+                          n_shift=int(round(1000 * f)), n_rot=int(round(1000 * f)),
+                          n_cav=max(1, int(round(16 * f))), n_ell=int(round(984 * f)))
+
+
+def batch_specs(n_variants=256, seed=2025, elements=(500, 20000), particles=(1024, 262144)):
+    """The batched-tracking workload: per variant ``(lattice seed, element
+    count ~ U(elements), particle count ~ log-uniform(particles), particle
+    seed)``."""
+    rng = np.random.default_rng(seed)
+    e = rng.uniform(elements[0], elements[1], n_variants).astype(int)
+    n = np.exp(rng.uniform(np.log(particles[0]), np.log(particles[1]), n_variants)).astype(int)
+    return [(int(seed * 1000 + v), int(e[v]), int(n[v]), int(seed * 7919 + v))
+            for v in range(n_variants)]
+
+
 def bb_sc_ring(seed=7, n_bb6d=4, n_bb4d=4, n_sc=200, n_slices=21,
                sigma_x=16.7e-6, sigma_y=16.7e-6, sigma_z=0.0755,
                bunch_charge=1.15e11, elliptic=False) -> Elements:
