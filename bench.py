@@ -15,6 +15,12 @@ particle passes counts once (lost particles stop counting where they are lost).
               launch / launch time, against the DFMA peak measured in-process;
   cpu_baseline  the CPU oracle (C restatement of the reference loop, OpenMP
               over particles) on a bounded sample of the same workload.
+  batched     256 lattice variants (rings built like the synthetic ring, element
+              count ~ U(500, 20000), particle count ~ log-uniform(1024, 262144),
+              Gaussian 6D): one captured CUDA graph of the persistent batch
+              kernel (autotuned launch shape) against one plain tracking launch
+              per variant, both over the same 2 turns after 2 warm-up turns;
+              results compared bit for bit.
   adjoint     the differentiable-tracking workload: the FODO ring with 64
               quadrupole and 16 sextupole strengths as parameters, 65,536
               Gaussian protons, 1,000 turns, a checkpoint every 100 turns;
@@ -57,6 +63,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-variants", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -240,6 +248,95 @@ def e2e_measure(ring, parts, steps, warmup, mode, threads, blocks_per_sm):
             "d2h_bytes_per_step": nbytes, "ms_per_step": dt / steps * 1e3}
 
 
+def _build_variant(spec):
+    from sixtracklib_gb300 import lattices
+
+    seed, n_elem, _, _ = spec
+    return lattices.variant_ring(seed, n_elem).cbuffer.to_image()
+
+
+def build_variants(n_variants):
+    """Lattice images of the batched workload, built in a spawned pool (the
+    pure-Python lattice construction is the slow part)."""
+    import multiprocessing as mp
+
+    from sixtracklib_gb300 import lattices
+
+    specs = lattices.batch_specs(n_variants=n_variants)
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        images = pool.map(_build_variant, specs)
+    return specs, images
+
+
+def batched_measure(dev, mode, specs, images, turns=2):
+    import torch
+
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.batch import BatchTracker
+    from sixtracklib_gb300.device import DeviceTracker
+
+    stream = torch.cuda.current_stream(dev)
+    trk = [DeviceTracker(img, config=f"mode={mode}") for img in images]
+    cols = [torch.from_numpy(lattices.gaussian_particles(n, seed=ps).block.copy()
+                             .view(np.int64)).to(dev) for _, _, n, ps in specs]
+    n_elem = [t.num_elements for t in trk]
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def pet(before, after):
+        return sum(pet_between(b, a, e) for b, a, e in zip(before, after, n_elem))
+
+    # plain: one tracking launch per variant, one variant after the other
+    plain = [c.clone() for c in cols]
+    for t, c in zip(trk, plain):
+        t.launch_until(c, turns)
+    torch.cuda.synchronize(dev)
+    before = [c.clone() for c in plain]
+    a, b = ev(), ev()
+    a.record(stream)
+    for t, c in zip(trk, plain):
+        t.launch_until(c, 2 * turns)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    t_plain = a.elapsed_time(b) / 1e3
+    pet_plain = pet(before, plain)
+
+    work = [c.clone() for c in cols]
+    bt = BatchTracker(trk)
+    bt.set_particles(work)
+    t0 = time.time()
+    tune_ms = bt.autotune(sample_fraction=1 / 64, trial_turns=2)
+    tune_s = time.time() - t0
+    bt.capture(turns)
+    bt.set_turn(0)
+    bt.replay()  # warm-up replay: turns 0..turns
+    assert bt.status() == 0, "batch status"
+    before = [c.clone() for c in work]
+    bt.set_turn(turns)
+    torch.cuda.synchronize(dev)
+    a, b = ev(), ev()
+    a.record(stream)
+    bt.replay()
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    t_batch = a.elapsed_time(b) / 1e3
+    assert bt.status() == 0, "batch status"
+    pet_batch = pet(before, work)
+    identical = all(torch.equal(x, y) for x, y in zip(work, plain))
+    return {
+        "workload": f"{len(specs)} lattice variants, element count ~ U(500, 20000), particle "
+                    f"count ~ log-uniform(1024, 262144), Gaussian 6D, FP64 {mode}",
+        "particles": int(sum(c.shape[1] for c in cols)),
+        "elements": int(sum(n_elem)), "turns_timed": turns,
+        "plain_per_lattice": {"seconds": t_plain, "value": pet_plain / t_plain,
+                              "launches": "one tracking call per variant"},
+        "batched_graph": {"seconds": t_batch, "value": pet_batch / t_batch,
+                          "shape": bt.shape, "autotune_s": tune_s, "autotune_trial_ms": tune_ms},
+        "unit": METRIC, "speedup": t_plain / t_batch, "bit_identical": bool(identical),
+    }
+
+
 def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
     """Forward and backward of differentiable tracking (see module doc)."""
     import torch
@@ -366,9 +463,12 @@ def run_reference(args):
 
 
 def run_ours(args):
+    rank, world, local = dist_env()
+    variants = None
+    if not args.no_batched and rank == 0:
+        variants = build_variants(args.batch_variants)  # before any CUDA call
     import torch
 
-    rank, world, local = dist_env()
     if world > 1:
         import torch.distributed as dist
 
@@ -466,6 +566,11 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(ring, parts, args.cpu_seconds)
+    if variants is not None:
+        try:
+            line["batched"] = batched_measure(dev, args.mode, *variants)
+        except Exception as exc:  # report, do not hide
+            line["batched"] = {"error": str(exc)}
     if not args.no_adjoint:
         try:
             line["adjoint"] = adjoint_measure(dev, args.mode)
