@@ -959,6 +959,86 @@ static int m_sc_qgauss(prec *p, const double *c)
     return ST_OK;
 }
 
+/* NS(LineDensityProfileData_interpolate_value), be_beamfields.h:3385-3408,
+ * with NS(Math_interpol_y_equ) (internal/math_interpol.h:901-920): linear
+ * (:649-665, y[i] + (z - (z0 + dz i)) yp[i]) and cubic (:789-816) evaluation.
+ * d: the LineDensityProfileData object {method, capacity, values_addr,
+ * derivatives_addr, z0, dz, num_values} (be_beamfields.h:887-897). */
+static double ldp_word(const lattice_t *L, const uint64_t *d, int which, int64_t i)
+{
+    /* the readable window: from the first array's start to the end of the
+     * second; inside the image or at a host address (the reference's CPU
+     * semantics); reads outside it give 0 */
+    uint64_t const va = d[2], da = d[3], cap = d[1];
+    uint64_t const lo = va < da ? va : da;
+    uint64_t const hi = (va > da ? va : da) + cap * 8u;
+    uint64_t const a = d[2 + which] + (uint64_t)i * 8u;
+    uint64_t const size = ((const uint64_t *)L->img)[1];
+    double v = 0.0;
+    if (i < 0 || a < lo || a + 8u > hi) return 0.0;
+    if (lo >= L->base && hi <= L->base + size)
+        memcpy(&v, lat_at(L, a), 8);
+    else
+        memcpy(&v, (const void *)(uintptr_t)a, 8);
+    return v;
+}
+
+static double ldp_interpolate(const lattice_t *L, const uint64_t *d, double z)
+{
+    uint64_t const method = d[0];
+    double z0, dz;
+    memcpy(&z0, &d[4], 8);
+    memcpy(&dz, &d[5], 8);
+    int64_t const nv = (int64_t)d[6];
+    double result = 0.0;
+    if ((z <= z0 + dz * nv) && (z >= z0)) {
+        int64_t const idx = (int64_t)((z - z0) / dz);
+        if (method == 0) {
+            result = ldp_word(L, d, 0, idx) + (z - (z0 + dz * idx)) * ldp_word(L, d, 1, idx);
+        } else if (method == 1) {
+            double const t2 = (z0 + dz * (idx + 1) - z) / dz;
+            double const t1 = (z - (z0 + dz * idx)) / dz;
+            double y = ldp_word(L, d, 0, idx + 1) * t1 + ldp_word(L, d, 0, idx) * t2;
+            y -= ldp_word(L, d, 1, idx) * dz * dz * (t2 - t2 * t2 * t2) / 6.0;
+            y -= ldp_word(L, d, 1, idx + 1) * dz * dz * (t1 - t1 * t1 * t1) / 6.0;
+            result = y;
+        }
+    }
+    return result;
+}
+
+/* be_beamfields/track.h:273-337; struct be_beamfields.h:1281-1293:
+ * {number_of_particles, sigma_x, sigma_y, length, x_co, y_co,
+ *  interpol_data_addr, line_density_prof_fallback, min_sigma_diff, enabled} */
+static int m_sc_interpol(const lattice_t *L, prec *p, const uint64_t *w)
+{
+    const double *c = (const double *)w;
+    double ex, ey, gx, gy;
+    double const charge = O_CHARGE0_SI * p->q0;
+    double const beta0 = p->beta0;
+    double const beta = beta0 * p->rvv;
+    double const pc0 = p->p0c * O_CHARGE0_SI;
+    double fk = p->chi * p->charge_ratio * c[3] * c[0] * charge * charge *
+                (1.0 - beta0 * beta);
+    uint64_t const addr = w[6];
+    uint64_t const size = ((const uint64_t *)L->img)[1];
+    const uint64_t *d = NULL;
+    if (addr != 0 && addr >= L->base && addr + 56u <= L->base + size)
+        d = (const uint64_t *)lat_at(L, addr);
+    else if (addr != 0)
+        d = (const uint64_t *)(uintptr_t)addr; /* host address, as the reference */
+    if (d != NULL && d[0] != 255u && (int64_t)d[6] > 0) {
+        fk *= ldp_interpolate(L, d, p->zeta);
+    } else {
+        fk *= c[7];
+    }
+    fk /= (pc0 * beta);
+    orc_fields_gauss(p->x - c[4], p->y - c[5], c[1], c[2], c[8], 1, &ex, &ey, &gx, &gy);
+    p->px += fk * ex;
+    p->py += fk * ey;
+    return ST_OK;
+}
+
 /* ---------------------------------------------------------- monitors */
 typedef struct {
     const orc_monitor_outputs *mon;
@@ -1079,6 +1159,9 @@ static int dispatch(const lattice_t *L, prec *p, int64_t obj,
         break;
     case T_SC_QGAUSS:
         ret = m_sc_qgauss(p, obj_reals(L, obj));
+        break;
+    case T_SC_INTERPOL:
+        ret = m_sc_interpol(L, p, obj_words(L, obj));
         break;
     default:
         p->state = 0;

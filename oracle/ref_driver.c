@@ -61,9 +61,21 @@ static int open_lattice(ref_lattice *L, const uint8_t *img,
     L->mem = (unsigned char *)aligned_alloc(64, (size + 63) & ~(uint64_t)63);
     if (!L->mem) return -1;
     memcpy(L->mem, img, size);
+    uint64_t const old_base = ((const uint64_t *)img)[0];
     if (NS(ManagedBuffer_remap)(L->mem, 8u) != 0) return -1;
     L->begin = NS(ManagedBuffer_get_const_objects_index_begin)(L->mem, 8u);
     L->end = NS(ManagedBuffer_get_const_objects_index_end)(L->mem, 8u);
+    /* the interpolated space-charge element holds a plain address (no
+     * dataptr; the reference's TrackJob assigns it): when it points into
+     * this image, move it with the image, as the caller would */
+    uint64_t const new_base = (uint64_t)(uintptr_t)L->mem;
+    for (NS(Object) const *it = L->begin; it != L->end; ++it) {
+        if (NS(Object_get_type_id)(it) != NS(OBJECT_TYPE_SC_INTERPOLATED_PROF)) continue;
+        NS(SCInterpolatedProfile) *sc =
+            (NS(SCInterpolatedProfile) *)(uintptr_t)NS(Object_get_begin_addr)(it);
+        if (sc->interpol_data_addr >= old_base && sc->interpol_data_addr < old_base + size)
+            sc->interpol_data_addr = sc->interpol_data_addr - old_base + new_base;
+    }
     L->mon_out = NULL;
     if (mon && mon->num > 0) {
         L->mon_out = (NS(ParticlesGenericAddr) *)calloc(

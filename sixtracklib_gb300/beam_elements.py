@@ -400,6 +400,129 @@ def q_gauss_cq(q):
     return cq
 
 
+def interpolation_derivatives(values, dz, method):
+    """Derivative table of a line-density profile as the reference prepares
+    it (NS(Math_interpol_prepare_equ), internal/math_interpol.h:604-645):
+    linear -- forward slopes ``(y[i+1] - y[i]) / dz`` (last entry 0,
+    :322-367); cubic -- second derivatives of the natural cubic spline
+    (tridiagonal solve of :369-600 with natural boundaries)."""
+    y = np.asarray(values, dtype=np.float64)
+    n = y.size
+    out = np.zeros(n)
+    if method == 0:
+        if n > 1:
+            out[:-1] = (y[1:] - y[:-1]) / dz
+        return out
+    if method != 1:
+        return out
+    if n <= 3:
+        raise ValueError("cubic interpolation needs more than 3 values")
+    h = np.full(n, float(dz))
+    g = np.zeros(n)
+    d = np.zeros(n)
+    l_ = np.zeros(n)
+    dy = np.zeros(n)
+    for i in range(1, n - 1):
+        g[i] = (h[i - 1] + h[i]) * 2.0
+        t = (y[i + 1] - y[i]) / h[i]
+        t -= (y[i] - y[i - 1]) / h[i - 1]
+        dy[i] = t * 6.0
+    d[0] = g[1]
+    out[0] = dy[1]
+    for i in range(1, n - 2):
+        l_[i] = h[i] / d[i - 1]
+        d[i] = g[i + 1] - l_[i] * h[i]
+        out[i] = dy[i + 1] - out[i - 1] * l_[i]
+    i = n - 3
+    out[i + 1] = out[i] / d[i]
+    for i in range(n - 4, -1, -1):
+        out[i + 1] = (out[i] - h[i + 1] * out[i + 2]) / d[i]
+    out[0] = 0.0
+    out[n - 1] = 0.0
+    return out
+
+
+class LineDensityProfileData(_Element):
+    """Tabulated longitudinal line density (be_beamfields.h:887-897): values
+    on the grid ``z0 + k dz`` and the derivative table for ``method`` 0
+    (linear) or 1 (cubic); 255 disables interpolation.  The arrays have
+    ``capacity`` entries, of which ``num_values`` are used."""
+
+    _typeid = TYPE_LINE_DENSITY_PROF_DATA
+    _fields = (
+        ("method", "u"),
+        ("capacity", "i"),
+        ("values", ("p", "capacity")),
+        ("derivatives", ("p", "capacity")),
+        ("z0", "f"),
+        ("dz", "f"),
+        ("num_values", "i"),
+    )
+    METHODS = {"linear": 0, "cubic": 1, "none": 255}
+    _default_dz = 1.0
+
+    def __init__(self, values=None, z0=0.0, dz=1.0, method="linear", capacity=None,
+                 derivatives=None, cbuffer=None, **kw):
+        m = self.METHODS[method] if isinstance(method, str) else int(method)
+        v = np.asarray(values if values is not None else [], dtype=np.float64)
+        nv = v.size
+        cap = max(int(capacity or 0), nv)
+        vals = np.zeros(cap)
+        vals[:nv] = v
+        if derivatives is None:
+            der = np.zeros(cap)
+            der[:nv] = interpolation_derivatives(v, dz, m) if nv else []
+        else:
+            der = np.zeros(cap)
+            der[: len(derivatives)] = derivatives
+        kw.pop("num_values", None)
+        super().__init__(cbuffer=cbuffer, method=m, capacity=cap, values=vals,
+                         derivatives=der, z0=float(z0), dz=float(dz), num_values=nv, **kw)
+
+
+class SCInterpolatedProfile(_Element):
+    """Space-charge kick with a tabulated line density (be_beamfields.h:
+    1281-1293).  ``line_density``: index of a :class:`LineDensityProfileData`
+    object in the same buffer; its absolute address is written into
+    ``interpol_data_addr`` whenever the buffer is serialised.  Without one
+    (or with method 255 or no values) ``line_density_prof_fallback`` is the
+    density, as in the reference."""
+
+    _typeid = TYPE_SC_INTERPOLATED_PROF
+    _fields = (
+        ("number_of_particles", "f"),
+        ("sigma_x", "f"),
+        ("sigma_y", "f"),
+        ("length", "f"),
+        ("x_co", "f"),
+        ("y_co", "f"),
+        ("interpol_data_addr", "u"),
+        ("line_density_prof_fallback", "f"),
+        ("min_sigma_diff", "f"),
+        ("enabled", "u"),
+    )
+    _default_sigma_x = 1.0
+    _default_sigma_y = 1.0
+    _default_line_density_prof_fallback = 1.0
+    _default_min_sigma_diff = 1e-10
+    _default_enabled = 1
+
+    def __init__(self, line_density=None, cbuffer=None, **kw):
+        self.line_density = None if line_density is None else int(line_density)
+        super().__init__(cbuffer=cbuffer, **kw)
+
+    def _encode(self):
+        typeid, words, arrays = super()._encode()
+        links = [] if self.line_density is None else [(6, self.line_density)]
+        return typeid, words, arrays, links
+
+    @classmethod
+    def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
+        self = super()._from_cobject(obj, cbuffer, index)
+        self.line_density = obj.links[0][1] if obj.links else None
+        return self
+
+
 # Aliases used by the reference's naming of the space-charge kicks.
 SpaceChargeCoasting = SCCoasting
 SpaceChargeQGaussianProfile = SCQGaussProfile
@@ -422,6 +545,8 @@ ELEMENT_TYPES = {
     TYPE_BEAM_BEAM_6D: BeamBeam6D,
     TYPE_SC_COASTING: SCCoasting,
     TYPE_SC_QGAUSSIAN_PROF: SCQGaussProfile,
+    TYPE_SC_INTERPOLATED_PROF: SCInterpolatedProfile,
+    TYPE_LINE_DENSITY_PROF_DATA: LineDensityProfileData,
 }
 
 

@@ -31,6 +31,7 @@ import numpy as np
 SLOT = 8
 HEADER_WORDS = 8
 DEFAULT_BASE = 4096
+TYPE_SC_INTERPOLATED_PROF = 257
 
 
 @dataclass
@@ -42,6 +43,10 @@ class CObject:
     typeid: int
     words: np.ndarray
     ptr_fields: list = field(default_factory=list)
+    # (field index, object index): plain address fields that hold the
+    # absolute address of another object of the same buffer (not dataptrs:
+    # the reference leaves them to its TrackJob's address assignment)
+    links: list = field(default_factory=list)
 
     @property
     def nbytes(self) -> int:
@@ -68,13 +73,15 @@ class CBuffer:
         self._image_cache = None
 
     # ------------------------------------------------------------ building
-    def add_object(self, typeid: int, struct_words, arrays=()) -> int:
+    def add_object(self, typeid: int, struct_words, arrays=(), links=()) -> int:
         """Append an object.
 
         ``struct_words``: the fixed struct as u64 words; pointer fields may
         hold anything.  ``arrays``: ``[(field_index, values)]`` -- each array
         is appended after the struct (8-byte aligned) and the pointer field at
-        ``field_index`` is made to reference it.  Returns the object index.
+        ``field_index`` is made to reference it.  ``links``: ``[(field_index,
+        object_index)]`` -- the field receives that object's absolute address
+        in every image.  Returns the object index.
         """
         sw = _as_words(struct_words)
         parts = [sw]
@@ -87,12 +94,14 @@ class CBuffer:
             parts.append(vw)
             off += vw.size
         words = np.concatenate(parts) if len(parts) > 1 else sw.copy()
-        self.objects.append(CObject(int(typeid), words, ptrs))
+        self.objects.append(CObject(int(typeid), words, ptrs,
+                                    [(int(f), int(t)) for f, t in links]))
         self._image_cache = None
         return len(self.objects) - 1
 
     def add_raw(self, obj: CObject) -> int:
-        self.objects.append(CObject(obj.typeid, obj.words.copy(), list(obj.ptr_fields)))
+        self.objects.append(CObject(obj.typeid, obj.words.copy(), list(obj.ptr_fields),
+                                    list(obj.links)))
         self._image_cache = None
         return len(self.objects) - 1
 
@@ -142,6 +151,7 @@ class CBuffer:
         img[dp_w + 1] = ndp
         img[gb_w] = 2 * SLOT
         img[gb_w + 1] = 0
+        starts = np.cumsum([0] + [o.words.size for o in self.objects]) + (slots_w + 2)
         pos = slots_w + 2
         k = 0
         for i, o in enumerate(self.objects):
@@ -151,6 +161,8 @@ class CBuffer:
                 seg[f] = base + (pos + int(o.words[f])) * SLOT
                 img[dp_w + 2 + k] = base + (pos + f) * SLOT
                 k += 1
+            for f, t in o.links:
+                seg[f] = base + int(starts[t]) * SLOT
             img[pos : pos + n] = seg
             e = objs_w + 2 + 3 * i
             img[e] = base + pos * SLOT
@@ -218,6 +230,15 @@ class CBuffer:
                     ptrs.append(f)
                 j += 1
             out.objects.append(CObject(t, words, ptrs))
+        # interpolated space charge (type 257): field 6 addresses the line
+        # density object of the same buffer when it is linked
+        begin_index = {b: i for i, (b, _, _) in enumerate(starts)}
+        base_w = {base + b * SLOT: i for b, i in begin_index.items()}
+        for o in out.objects:
+            if o.typeid == TYPE_SC_INTERPOLATED_PROF and o.words.size > 6:
+                tgt = base_w.get(int(o.words[6]))
+                if tgt is not None:
+                    o.links.append((6, tgt))
         return out
 
 

@@ -455,6 +455,7 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
     }
     uint32_t const no_adjoint = (1u << OP_RF_MULTIPOLE) | (1u << OP_BB4D) | (1u << OP_BB6D) |
                                 (1u << OP_SC_COASTING) | (1u << OP_SC_QGAUSS) |
+                                (1u << OP_SC_INTERP) |
                                 (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
     if (v.op_mask & no_adjoint) {
         set_error("adjoint: the lattice contains elements without an adjoint "

@@ -165,6 +165,17 @@ bool relayout(st_Buffer *b, const stg::ImageView *src, uint64_t slots_cap,
             mem[dptr_w + 2 + nd] = base + nfw * 8;
             ++nd;
         }
+        // interpolated space charge: field 6 is a plain address (not a
+        // dataptr); when it names an object of this buffer, move it along
+        for (uint64_t i = 0; i < src->num_objects; ++i) {
+            if (src->type_of(i) != ST_OBJECT_TYPE_SC_INTERPOLATED_PROF || old_n[i] < 7) continue;
+            uint64_t const tw = src->word_of(src->img[old_begin[i] + 6]);
+            for (uint64_t t = 0; t < src->num_objects && tw != UINT64_MAX; ++t)
+                if (old_begin[t] == tw) {
+                    mem[new_begin[i] + 6] = base + new_begin[t] * 8;
+                    break;
+                }
+        }
         mem[objs_w + 1] = src->num_objects;
     } else {
         mem[objs_w + 1] = 0;

@@ -723,10 +723,16 @@ struct st_TrackJob {
     int64_t min_pid = 0, max_pid = 0, min_elem = 0, max_elem = 0, min_turn = 0, max_turn = 0;
     uint16_t collect_flags = 0x05;  // particles | output (track/definitions.h)
     bool default_rolling = true;
+    // the particle buffer's memory, page-locked for direct DMA (or null)
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
 
     ~st_TrackJob() { release(); }
     void release()
     {
+        if (pinned) cudaHostUnregister(pinned);
+        pinned = nullptr;
+        pinned_bytes = 0;
         if (d_cols) cudaFree(d_cols);
         if (d_out) cudaFree(d_out);
         d_cols = nullptr;
@@ -750,8 +756,63 @@ st_Particles *pset(st_TrackJob *j, size_t k)
     return st_Particles_buffer_get_particles(j->pbuf, j->psets[k]);
 }
 
+// Page-lock the caller's particle buffer for the job's lifetime so that
+// push / collect are direct DMA copies of the columns (no staging copy on
+// the host).  The buffer is caller-owned and outlives the job (the
+// reference's ownership rule); when it cannot be registered (already
+// registered by another job, or unsupported) the staged copy is used.
+void pin_particles(st_TrackJob *j)
+{
+    unsigned char *base = st_Buffer_get_data_begin(j->pbuf);
+    size_t const bytes = (size_t)st_Buffer_get_capacity(j->pbuf);
+    if (!base || bytes == 0) return;
+    if (cudaHostRegister(base, bytes, cudaHostRegisterDefault) == cudaSuccess) {
+        j->pinned = base;
+        j->pinned_bytes = bytes;
+    } else {
+        (void)cudaGetLastError();  // not fatal: staged copies
+    }
+}
+
+// Column c of particle set k (host pointer) when the whole column lies in
+// the page-locked range, else null.
+void *pinned_column(st_TrackJob *j, size_t k, int c)
+{
+    if (!j->pinned || st_Buffer_get_data_begin(j->pbuf) != j->pinned) return nullptr;
+    st_Particles *p = pset(j, k);
+    void *col = c < 17 ? (void *)real_cols(p)[c] : (void *)int_cols(p)[c - 17];
+    uintptr_t const a = (uintptr_t)col, b = (uintptr_t)j->pinned;
+    size_t const bytes = (size_t)j->pset_cnt[k] * 8;
+    if (a < b || a + bytes > b + j->pinned_bytes) return nullptr;
+    return col;
+}
+
+// Direct column copies between the page-locked buffer and the device block.
+bool copy_pinned(st_TrackJob *j, bool to_device)
+{
+    if (!j->pinned) return false;
+    for (size_t k = 0; k < j->psets.size(); ++k)
+        for (int c = 0; c < 21; ++c)
+            if (!pinned_column(j, k, c)) return false;
+    cudaStream_t s = j->dev->stream;
+    for (size_t k = 0; k < j->psets.size(); ++k) {
+        size_t const bytes = (size_t)j->pset_cnt[k] * 8;
+        if (bytes == 0) continue;
+        for (int c = 0; c < 21; ++c) {
+            uint64_t *dcol = j->d_cols + (size_t)c * j->n_total + j->pset_off[k];
+            void *hcol = pinned_column(j, k, c);
+            cudaError_t const e =
+                to_device ? cudaMemcpyAsync(dcol, hcol, bytes, cudaMemcpyHostToDevice, s)
+                          : cudaMemcpyAsync(hcol, dcol, bytes, cudaMemcpyDeviceToHost, s);
+            if (!cuda_ok(e, "cudaMemcpyAsync(particles)")) return false;
+        }
+    }
+    return cuda_ok(cudaStreamSynchronize(s), "particle copy");
+}
+
 bool upload_particles(st_TrackJob *j)
 {
+    if (j->pinned && copy_pinned(j, true)) return true;
     std::vector<uint64_t> blk((size_t)j->n_total * 21);
     for (size_t k = 0; k < j->psets.size(); ++k) {
         st_Particles *p = pset(j, k);
@@ -768,6 +829,7 @@ bool upload_particles(st_TrackJob *j)
 
 bool download_particles(st_TrackJob *j)
 {
+    if (j->pinned && copy_pinned(j, false)) return true;
     std::vector<uint64_t> blk((size_t)j->n_total * 21);
     if (!cuda_ok(cudaMemcpy(blk.data(), j->d_cols, blk.size() * 8, cudaMemcpyDeviceToHost),
                  "cudaMemcpy(particles)"))
@@ -951,6 +1013,7 @@ bool setup_job(st_TrackJob *j, st_Buffer *pb, st_buffer_size_t nsets, const st_b
         off += (size_t)b.second * 21;
         j->outs.push_back(o);
     }
+    pin_particles(j);
     if (!upload_particles(j) || !transfer_outputs(j, true)) return false;
     return compile_job_lattice(j);
 }

@@ -184,6 +184,59 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             op = OP_SC_QGAUSS;
             p.assign(w, w + 11);
             break;
+        case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {
+            // be_beamfields/track.h:273-337.  interpol_data_addr (field 6)
+            // is a plain address of a NS(LineDensityProfileData): inside
+            // this buffer, or else a host address, which the reference's CPU
+            // tracking dereferences as it is (the data is copied into the
+            // compiled record here); 0 selects the fallback density.
+            if (!need(10)) return bad(err, i, "truncated interpolated space charge");
+            op = OP_SC_INTERP;
+            // N, sigma_x, sigma_y, length, x_co, y_co, fallback, min_sigma_diff
+            p = {w[0], w[1], w[2], w[3], w[4], w[5], w[7], w[8]};
+            uint64_t method = 255, nv = 0, z0 = 0, dz = 0, voff = 0, doff = 0;
+            std::vector<uint64_t> data;
+            if (w[6] != 0) {
+                uint64_t const dw = img.word_of(w[6]);
+                bool const inside = dw != UINT64_MAX && dw + 7 <= img.size_words;
+                const uint64_t *ld =
+                    inside ? img.img + dw : reinterpret_cast<const uint64_t *>((uintptr_t)w[6]);
+                int64_t const cap = (int64_t)ld[1];
+                if (ld[0] != 255u && (int64_t)ld[6] > 0) {
+                    if (cap <= 0 || cap > (int64_t)1 << 20 || ld[2] == 0 || ld[3] == 0)
+                        return bad(err, i, "line-density data without arrays");
+                    // the window the interpolation reads: from the first
+                    // array's start to the end of the second (the
+                    // reference's y[idx + 1] in the last interval reads the
+                    // first derivative); reads outside it give 0
+                    uint64_t const va = ld[2], da = ld[3];
+                    uint64_t const lo = std::min(va, da);
+                    uint64_t const hi = std::max(va, da) + (uint64_t)cap * 8u;
+                    if ((hi - lo) / 8u > ((uint64_t)1 << 21))
+                        return bad(err, i, "line-density arrays too far apart");
+                    if (inside) {
+                        uint64_t const lw = img.word_of(lo);
+                        uint64_t const hw = img.word_of(hi - 8u);
+                        if (lw == UINT64_MAX || hw == UINT64_MAX)
+                            return bad(err, i, "line-density arrays outside the lattice buffer");
+                        data.assign(img.img + lw, img.img + hw + 1);
+                    } else {
+                        const uint64_t *src = reinterpret_cast<const uint64_t *>((uintptr_t)lo);
+                        data.assign(src, src + (hi - lo) / 8u);
+                    }
+                    voff = (va - lo) / 8u;
+                    doff = (da - lo) / 8u;
+                    method = ld[0];
+                    nv = ld[6];
+                    z0 = ld[4];
+                    dz = ld[5];
+                }
+            }
+            aux = (method != 255u && nv > 0) ? 1u : 0u;
+            p.insert(p.end(), {method, nv, z0, dz, voff, doff, (uint64_t)data.size()});
+            p.insert(p.end(), data.begin(), data.end());
+            break;
+        }
         case ST_OBJECT_TYPE_BEAM_MONITOR: {
             if (!need(8)) return bad(err, i, "truncated beam monitor");
             op = OP_MONITOR;

@@ -666,4 +666,60 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
     return p;
 }
 
+// NS(LineDensityProfileData_interpolate_value), be_beamfields.h:3385-3408,
+// with NS(Math_interpol_y_equ), internal/math_interpol.h:649-665 (linear)
+// and :789-816 (cubic).  c: the record's parameters; the tables are one
+// window of memory holding both arrays (values at word c[12], derivatives
+// at c[13], c[14] words), copied in at compile time; a read outside the
+// window gives 0.
+__device__ __forceinline__ double ldp_word(const uint64_t *c, uint64_t off, int64_t i)
+{
+    uint64_t const k = off + (uint64_t)i;
+    return (i >= 0 && k < c[14]) ? W(c[15 + k]) : 0.0;
+}
+
+__device__ __forceinline__ double ldp_interpolate(const uint64_t *c, double z)
+{
+    uint64_t const method = c[8];
+    int64_t const nv = (int64_t)c[9];
+    double const z0 = W(c[10]), dz = W(c[11]);
+    double result = 0.0;
+    if ((z <= z0 + dz * (double)nv) && (z >= z0)) {
+        int64_t const idx = (int64_t)((z - z0) / dz);
+        if (method == 0) {
+            result = ldp_word(c, c[12], idx) + (z - (z0 + dz * (double)idx)) * ldp_word(c, c[13], idx);
+        } else if (method == 1) {
+            double const t2 = (z0 + dz * (double)(idx + 1) - z) / dz;
+            double const t1 = (z - (z0 + dz * (double)idx)) / dz;
+            double y = ldp_word(c, c[12], idx + 1) * t1 + ldp_word(c, c[12], idx) * t2;
+            y -= ldp_word(c, c[13], idx) * dz * dz * (t2 - t2 * t2 * t2) / 6.0;
+            y -= ldp_word(c, c[13], idx + 1) * dz * dz * (t1 - t1 * t1 * t1) / 6.0;
+            result = y;
+        }
+    }
+    return result;
+}
+
+// be_beamfields/track.h:273-337
+static __device__ __noinline__ PState sc_interpolated(PState p, const uint64_t *rec, uint32_t aux)
+{
+    const uint64_t *c = rec + 1;
+    double const charge = kCharge0SiD * p.q0;
+    double const beta0 = p.beta0;
+    double const beta = beta0 * p.rvv;
+    double const pc0 = p.p0c * kCharge0SiD;
+    double fk = p.chi * p.charge_ratio * W(c[3]) * W(c[0]) * charge * charge *
+                (1.0 - beta0 * beta);
+    if (aux & 1u)
+        fk *= ldp_interpolate(c, p.zeta);
+    else
+        fk *= W(c[6]);
+    fk /= (pc0 * beta);
+    double ex, ey, gx, gy;
+    fields_gauss(p.x - W(c[4]), p.y - W(c[5]), W(c[1]), W(c[2]), W(c[7]), 1, &ex, &ey, &gx, &gy);
+    p.px += fk * ex;
+    p.py += fk * ey;
+    return p;
+}
+
 }  // namespace stg

@@ -36,6 +36,10 @@ enum Op : uint32_t {
     OP_NOP = 18,            // success, no effect (disabled beam-beam)
     OP_FAIL = 19,           // failure (map compiled out, e.g. TriCub)
     OP_FAIL_LOST = 20,      // failure and particle lost (unknown type id)
+    OP_SC_INTERP = 21,      // [N, sigma_x, sigma_y, length, x_co, y_co, fallback,
+                            //  min_sigma_diff, method, num_values, z0, dz,
+                            //  values@, derivatives@, nwords, data[nwords]]
+                            // aux bit0: interpolate (else the fallback density)
     OP_COUNT
 };
 

@@ -241,6 +241,9 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
     case OP_SC_QGAUSS:
         p = sc_qgauss(p, rec);
         return 0;
+    case OP_SC_INTERP:
+        p = sc_interpolated(p, rec, aux);
+        return 0;
     case OP_MONITOR: {
         uint64_t *out = reinterpret_cast<uint64_t *>(rec[8]);
         if (out == nullptr) return 0;

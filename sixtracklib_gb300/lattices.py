@@ -12,6 +12,12 @@ synthetic (no public dataset is involved) and fully determined by the seed:
   N(0,1e-4) rad, 16 cavities, 984 LimitEllipse (a=0.015, b=0.01);
 * :func:`bb_sc_ring` -- the FODO ring plus 4 BeamBeam6D (21 slices), 4
   BeamBeam4D and 200 q-Gaussian space-charge kicks;
+* :func:`sc_interpolated_ring` -- the FODO ring plus interpolated
+  space-charge kicks on tabulated line densities;
+* :func:`learnable_fodo_ring` -- the FODO ring with 64 quadrupole and 16
+  sextupole strengths marked as learnable (differentiable tracking);
+* :func:`variant_ring` / :func:`batch_specs` -- rings built like the
+  synthetic ring at any size, and the 256-variant batched workload;
 * particle sets: Gaussian 6D and the polar amplitude grid.
 """
 
@@ -128,6 +134,34 @@ def synthetic_ring(seed=20240601, n_cells=4000, n_extra_drift=1000,
                 else:
                     e.LimitEllipse(a=0.015, b=0.01)
     return e
+
+
+def sc_interpolated_ring(n_kicks=8, seed=3):
+    """The FODO ring plus interpolated space-charge kicks: tabulated
+    Gaussian line densities (linear and cubic interpolation, one table with
+    interpolation switched off) and kicks without a table (fallback
+    density).  Returns ``(elements, tables)``; ``tables`` (a
+    :class:`~sixtracklib_gb300.sc_line_density.LineDensityBuffer`) owns the
+    tables the kicks address and must stay alive while the lattice is
+    compiled or tracked on the CPU."""
+    from .sc_line_density import LineDensityBuffer
+
+    rng = np.random.default_rng(seed)
+    tables = LineDensityBuffer()
+    z = np.linspace(-0.3, 0.3, 41)
+    prof = np.exp(-0.5 * (z / 0.1) ** 2) * 1e12
+    idx = [tables.add(prof, z0=-0.3, dz=float(z[1] - z[0]), method="linear", capacity=48),
+           tables.add(prof * 1.1, z0=-0.3, dz=float(z[1] - z[0]), method="cubic"),
+           tables.add(prof, z0=-0.3, dz=float(z[1] - z[0]), method="none")]
+    e = fodo_ring()
+    for k in range(n_kicks):
+        which = k % 4
+        addr = tables.address(idx[which]) if which < 3 else 0
+        e.SCInterpolatedProfile(number_of_particles=1e11, length=0.5,
+                                sigma_x=1e-3, sigma_y=float(rng.choice([1e-3, 1.2e-3])),
+                                interpol_data_addr=addr, line_density_prof_fallback=5e11,
+                                min_sigma_diff=1e-10)
+    return e, tables
 
 
 def variant_ring(seed: int, n_elements: int) -> Elements:

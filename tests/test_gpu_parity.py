@@ -227,6 +227,22 @@ def test_beam_beam_space_charge_ring(torch_cuda, oracle, elliptic):
             assert_parity(got, exp, tol=tol)
 
 
+def test_interpolated_space_charge(torch_cuda, oracle):
+    """SCInterpolatedProfile (linear / cubic / disabled tables and the
+    fallback density): 1e-13 after one turn, 1e-10 after 20."""
+    e, tables = lattices.sc_interpolated_ring()
+    lat = e.cbuffer.to_image()
+    p = lattices.gaussian_particles(1024, seed=23, sz=0.12)
+    for turns, tol in ((1, 1e-13), (20, 1e-10)):
+        exp = p.block.copy()
+        assert oracle.track_until(lat, exp, turns) == 0
+        for mode in ("exact", "fast"):
+            st, got = run_device(torch_cuda, lat, p.block, until=turns, mode=mode)
+            assert st == 0
+            assert_parity(got, exp, tol=tol)
+    del tables
+
+
 # ------------------------------------------------------------ edge cases
 def test_edge_cases(torch_cuda, oracle):
     e = Elements()

@@ -141,3 +141,36 @@ def test_tracking_without_gpu_fails_loudly(lib):
     assert st == -1
     assert "GPU" in _native.last_error() or "CUDA" in _native.last_error()
     assert np.array_equal(blk, q.block)
+
+
+def test_line_density_link_survives_buffer_adoption():
+    """A SCInterpolatedProfile linked to a LineDensityProfileData of the same
+    buffer keeps pointing at it when the engine adopts the image at a new
+    address (the field is a plain address, not a dataptr)."""
+    import ctypes as C
+
+    import numpy as np
+
+    from sixtracklib_gb300 import CBuffer, _native
+    from sixtracklib_gb300.beam_elements import Elements
+
+    e = Elements()
+    e.Drift(length=1.0)
+    ld = len(e)
+    e.LineDensityProfileData(values=np.linspace(1, 2, 8), z0=-1.0, dz=0.25, method="cubic")
+    e.SCInterpolatedProfile(number_of_particles=1e10, length=1.0, line_density=ld)
+    img = e.cbuffer.to_image()
+    back = CBuffer.from_image(img)
+    assert back.objects[2].links == [(6, ld)]
+    lib = _native.load()
+    buf = lib.st_Buffer_new_on_data(img.ctypes.data, img.nbytes)
+    assert buf
+    try:
+        objs = [C.cast(lib.st_Buffer_get_const_object(buf, i), C.POINTER(C.c_uint64))
+                for i in range(3)]
+        ld_addr = int(objs[1][0])
+        sc = C.cast(C.c_void_p(int(objs[2][0])), C.POINTER(C.c_uint64))
+        assert int(sc[6]) == ld_addr != int(img[0])
+    finally:
+        lib.st_Buffer_delete(buf)
+

@@ -205,3 +205,20 @@ def test_cerrf_matches_reference(oracle, ref_oracle):
     for args in [(1e-6, 2e-6, 3e-6, 3e-6, 1e-10, 0), (1e-6, -2e-6, 3e-6, 4e-6, 1e-10, 0),
                  (0.0, 0.0, 3e-6, 3e-6, 1e-10, 1), (1e-7, 2e-7, 3e-6, 2e-6, 1e-10, 0)]:
         assert oracle.fields_gauss(*args) == ref_oracle.fields_gauss(*args)
+
+
+def test_oracle_matches_reference_interpolated_space_charge(oracle, ref_oracle):
+    """SCInterpolatedProfile with linear, cubic and disabled line-density
+    tables (host addresses, as the reference's CPU tracking reads them) and
+    the fallback density; zeta spread beyond the tables' range."""
+    e, tables = lattices.sc_interpolated_ring()
+    lat = e.cbuffer.to_image()
+    p = lattices.gaussian_particles(300, seed=2, sz=0.12)
+    for turns in (1, 6):
+        a, b = p.block.copy(), p.block.copy()
+        assert oracle.track_until(lat, a, turns) == ref_oracle.track_until(lat, b, turns) == 0
+        assert np.array_equal(a, b)
+    dpx = a.view(np.float64)[8] - p.block.view(np.float64)[8]
+    assert np.abs(dpx).max() > 0
+    del tables
+
