@@ -67,6 +67,16 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
 }
 
 // ------------------------------------------------------------------- maps
+// s += L for a particle whose s is accumulated (not read from the s table).
+// `s_live` is block-uniform: false once every particle of the block reads s
+// from the table (every turn after the first).  The add is a volatile PTX
+// instruction so that it cannot be speculated out of the branch (the plain
+// C form is issued for every lane and its result selected).
+__device__ __forceinline__ void add_s(PState &p, double L, bool s_live)
+{
+    if (s_live && !p.lazy_s) asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(p.s) : "d"(L));
+}
+
 // be_drift/track.h:45-67.  FAST keeps the reference's rounding of
 // 1 + (xp^2 + yp^2)/2 at the scale of 1.0 (u below): regrouping the zeta
 // update as L (rvv - 1) - (L/2)(xp^2 + yp^2) is more accurate but departs
@@ -74,7 +84,7 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
 // s is only accumulated when the turn did not start at s = +0 (otherwise it
 // comes from the lattice's s table).
 template <bool FAST>
-__device__ __forceinline__ void drift(PState &p, double L)
+__device__ __forceinline__ void drift(PState &p, double L, bool s_live = true)
 {
     double const xp = p.px * p.rpp;
     double const yp = p.py * p.rpp;
@@ -89,29 +99,37 @@ __device__ __forceinline__ void drift(PState &p, double L)
         p.y += yp * L;
         p.zeta += L * dzeta;
     }
-    if (!p.lazy_s) p.s += L;
+    add_s(p, L, s_live);
 }
 
 // be_drift/track.h:71-97
-__device__ __forceinline__ void drift_exact(PState &p, double L)
+__device__ __forceinline__ void drift_exact(PState &p, double L, bool s_live = true)
 {
     double const opd = p.delta + 1.0;
     double const lpzi = L / sqrt(opd * opd - (p.px * p.px + p.py * p.py));
     double const dzeta = p.rvv * L - opd * lpzi;
     p.x += p.px * lpzi;
     p.y += p.py * lpzi;
-    if (!p.lazy_s) p.s += L;
+    add_s(p, L, s_live);
     p.zeta += dzeta;
 }
 
 // Global aperture (be_limit/track.h:54-88) on the integer pipe:
-// |x| < limit  <=>  bits(|x|) < bits(limit), NaN and inf fail as in the
-// reference's float compare.
+// |x| < limit  <=>  bits(|x|) < bits(limit) for a limit >= +0; NaN and inf
+// fail as in the reference's float compare.  The compare is spelled on the
+// two 32-bit halves: a 64-bit mask of the sign bit is recognised as fabs()
+// and costs an FP64 instruction per coordinate.
+__device__ __forceinline__ bool abs_below(double v, uint64_t lim)
+{
+    uint32_t const hi = (uint32_t)__double2hiint(v) & 0x7FFFFFFFu;
+    uint32_t const lo = (uint32_t)__double2loint(v);
+    uint32_t const lhi = (uint32_t)(lim >> 32), llo = (uint32_t)lim;
+    return (hi < lhi) | ((hi == lhi) & (lo < llo));
+}
+
 __device__ __forceinline__ bool inside_global(const PState &p, uint64_t xlim, uint64_t ylim)
 {
-    uint64_t const ax = (uint64_t)__double_as_longlong(p.x) & 0x7FFFFFFFFFFFFFFFull;
-    uint64_t const ay = (uint64_t)__double_as_longlong(p.y) & 0x7FFFFFFFFFFFFFFFull;
-    return (ax < xlim) & (ay < ylim);
+    return abs_below(p.x, xlim) & abs_below(p.y, ylim);
 }
 
 // be_multipole/track.h:38-112 (bal[2k] = knl[k]/k!, bal[2k+1] = ksl[k]/k!)

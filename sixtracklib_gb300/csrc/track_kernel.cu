@@ -184,13 +184,13 @@ __device__ __forceinline__ int64_t ebe_index(const EbeDevConfig &c, int64_t pid,
 template <bool FAST>
 __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hdr,
                                      const TrackParams &prm, int64_t cur_elem, int64_t cur_turn,
-                                     int64_t ord)
+                                     int64_t ord, bool s_live)
 {
     uint32_t const op = (uint32_t)(hdr & 0xFF);
     uint32_t const aux = (uint32_t)(hdr >> 32);
     switch (op) {
     case OP_DRIFT:
-        drift<FAST>(p, W(rec[1]));
+        drift<FAST>(p, W(rec[1]), s_live);
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_MULTIPOLE:
@@ -213,7 +213,7 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         multipole<FAST, true>(p, rec, (int)aux);
         return 0;
     case OP_DRIFT_EXACT:
-        drift_exact(p, W(rec[1]));
+        drift_exact(p, W(rec[1]), s_live);
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_LIMIT_RECT:
@@ -356,6 +356,8 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
 
     while (any && !timed_out) {
         bool part = (prm.mode == MODE_LINE) ? active : (active && (p.at_turn == turn));
+        // some particle of the block accumulates s in this pass (block-uniform)
+        bool const s_live = __syncthreads_or(part && !p.lazy_s);
         int64_t ord = 0;  // element ordinal within the turn / line
         int64_t ae = start_elem;
         for (int c = 0; c < nch; ++c) {
@@ -383,7 +385,7 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
                                          p.lazy_s ? prm.s_table[ord] : p.s);
                     }
                     int const rc =
-                        apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn, ord);
+                        apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn, ord, s_live);
                     if (rc != 0 || p.state != 1) {
                         status |= rc;
                         part = false;

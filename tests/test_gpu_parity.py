@@ -68,6 +68,9 @@ def assert_parity(got, exp, tol, bit_exact=False):
         assert dev <= tol, f"max deviation {dev:.3e} > {tol:.1e}"
 
 
+_CACHE = {}
+
+
 def load(name):
     return np.load(os.path.join(GOLDEN, name))
 
@@ -209,6 +212,27 @@ def test_synthetic_ring_sample(torch_cuda, oracle, mode):
     st, got = run_device(torch_cuda, lat, p.block, until=5, mode=mode)
     assert st == 0
     assert_parity(got, exp, tol=1e-12)
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast"])
+def test_synthetic_ring_1000_turns(torch_cuda, oracle, mode):
+    """The 20,000-element ring over 1000 turns on a strided sample of the
+    benchmark's polar grid (amplitudes 0-20 sigma, so particles are lost on
+    the way): loss flags, at_element and at_turn identical, coordinates
+    within 1e-10."""
+    if "synthetic_1000" not in _CACHE:  # the oracle run (~15 s) serves both modes
+        lat = lattices.synthetic_ring().cbuffer.to_image()
+        full = lattices.polar_grid_particles(1_000_000, seed=99)
+        blk = np.ascontiguousarray(full.block[:, ::4096])
+        exp = blk.copy()
+        assert oracle.track_until(lat, exp, 1000) == 0
+        _CACHE["synthetic_1000"] = (lat, blk, exp)
+    lat, blk, exp = _CACHE["synthetic_1000"]
+    st, got = run_device(torch_cuda, lat, blk, until=1000, mode=mode)
+    assert st == 0
+    lost = int((exp.view(np.int64)[20] == 0).sum())
+    assert 0 < lost < blk.shape[1]
+    assert_parity(got, exp, tol=1e-10)
 
 
 @pytest.mark.parametrize("elliptic", [False, True])
