@@ -75,10 +75,13 @@ struct Lam {
 
 struct RState {
     double x, px, y, py, zeta, delta, rpp, rvv;
-    // functions of delta, constant between cavities
-    double drvv;   // d rvv / d delta
-    double drpp;   // d rpp / d delta = -rpp^2
-    double rvvm1;  // rvv - 1
+    // functions of delta (and of lambda_zeta), constant between cavities
+    double drvv;    // d rvv / d delta
+    double drpp;    // d rpp / d delta = -rpp^2
+    double rvvm1;   // rvv - 1
+    double hr2;     // rpp^2 / 2
+    double lzr;     // lambda_zeta * rpp
+    double lzdrvv;  // lambda_zeta * d rvv / d delta
     double beta0, chi, q, energy0;
 };
 
@@ -101,11 +104,16 @@ __device__ __forceinline__ double drvv_of(double delta, double beta0)
     return (1.0 - beta0 * beta0) / (Q * Q * Q);
 }
 
-__device__ __forceinline__ void set_delta_terms(RState &s)
+// Refresh the cached terms after delta or lambda_zeta changed (start of the
+// walk, cavities); drifts and kicks leave both unchanged.
+__device__ __forceinline__ void set_delta_terms(RState &s, double lz)
 {
     s.drvv = drvv_of(s.delta, s.beta0);
     s.drpp = -s.rpp * s.rpp;
     s.rvvm1 = s.rvv - 1.0;
+    s.hr2 = 0.5 * s.rpp * s.rpp;
+    s.lzr = lz * s.rpp;
+    s.lzdrvv = lz * s.drvv;
 }
 
 extern __shared__ double s_grad[];
@@ -154,6 +162,69 @@ __device__ __forceinline__ void horner2(const uint64_t *bal, int n, double x, do
     }
 }
 
+// Multipole (be_multipole/track.h:38-112), with the curvature terms only in
+// the CURV instantiation: a runtime branch around them is if-converted, and
+// predicated-off FP64 instructions still occupy the FP64 pipe.
+template <bool CURV>
+__device__ __forceinline__ void reverse_multipole(RState &s, Lam &l, const uint64_t *bal, int n,
+                                                  const AdjParams &a, int64_t e, bool on)
+{
+    double const chi = s.chi, x = s.x, y = s.y;
+    // curvature words 2n+2.. : hxl, hyl, length, hxl / length, hyl / length
+    // (the ratios are 0 without length)
+    double const hxl = CURV ? W(bal[2 * n + 2]) : 0.0;
+    double const hyl = CURV ? W(bal[2 * n + 3]) : 0.0;
+    double const hxl_l = CURV ? W(bal[2 * n + 5]) : 0.0;
+    double const hyl_l = CURV ? W(bal[2 * n + 6]) : 0.0;
+    double const lpx = l.px, lpy = l.py;
+    if (on) {
+        double pr, pi, dr, di;
+        horner2(bal, n, x, y, pr, pi, dr, di);
+        // input from output: the kick (-chi Re P, chi Im P) taken back
+        s.px = fma(chi, pr, s.px);
+        s.py = fma(-chi, pi, s.py);
+        if (CURV) {
+            s.zeta -= chi * (y * hyl - x * hxl);
+            s.px -= hxl + hxl * s.delta - chi * W(bal[0]) * x * hxl_l;
+            s.py -= -(hyl + hyl * s.delta) + chi * W(bal[1]) * y * hyl_l;
+        }
+        double const clx = chi * lpx, cly = chi * lpy;
+        l.x = fma(-clx, dr, fma(cly, di, l.x));
+        l.y = fma(clx, di, fma(cly, dr, l.y));
+        if (CURV) {
+            l.x -= l.z * chi * hxl + clx * W(bal[0]) * hxl_l;
+            l.y += l.z * chi * hyl + cly * W(bal[1]) * hyl_l;
+            l.d += lpx * hxl - lpy * hyl;
+        }
+    }
+    int32_t const j0 = a.pbeg ? a.pbeg[e] : 0, j1 = a.pbeg ? a.pbeg[e + 1] : 0;
+    if (j0 < j1) {  // warp-uniform
+        // d(dpx, dpy)/d bal[2k] = chi (-Re z^k, Im z^k); / d bal[2k+1] = chi (Im z^k, Re z^k)
+        double const cx = chi * lpx, cy = chi * lpy;
+        for (int32_t j = j0; j < j1; ++j) {
+            int const k2 = a.pkind[j];
+            double g = 0.0;
+            if (on && k2 >= 0) {
+                int const kk = k2 >> 1;
+                double zr = 1.0, zi = 0.0;
+                if (kk > 0) {
+                    zr = x;
+                    zi = y;
+                    for (int k = 1; k < kk; ++k) {
+                        double const t = fma(zr, x, -zi * y);
+                        zi = fma(zr, y, zi * x);
+                        zr = t;
+                    }
+                }
+                g = (k2 & 1) ? fma(cx, zi, cy * zr) : fma(-cx, zr, cy * zi);
+                if (CURV && k2 == 0) g -= cx * x * hxl_l;
+                if (CURV && k2 == 1) g += cy * y * hyl_l;
+            }
+            add_grad(a, j, g, on);
+        }
+    }
+}
+
 // Restore the input of one element from its output (state s) and apply
 // lambda <- J^T lambda at that input.  `on` is false for lanes that do not
 // take part (they still join the warp reductions).
@@ -166,24 +237,22 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
     switch (op) {
     case OP_DRIFT: {  // be_drift/track.h:45-67
         if (!on) break;
-        // input from output: x -= L rpp px, zeta -= L (rvv - 1 - (xp^2 + yp^2) / 2)
+        // input from output: x -= L rpp px, zeta -= L (rvv - 1 - rpp^2 (px^2 + py^2) / 2)
         double const L = W(rec[1]);
-        double const rpp = s.rpp, px = s.px, py = s.py;
-        double const a_ = L * rpp;
+        double const px = s.px, py = s.py;
+        double const a_ = L * s.rpp;
         s.x = fma(-a_, px, s.x);
         s.y = fma(-a_, py, s.y);
         double const p2 = fma(py, py, px * px);
-        double const s2 = rpp * p2;          // xp px + yp py
-        double const h = rpp * s2;           // xp^2 + yp^2
-        s.zeta = fma(L, fma(0.5, h, -s.rvvm1), s.zeta);
-        // lambda: d(out)/d(px, py, delta) with rpp(delta), rvv(delta)
-        double const lx = l.x, ly = l.y, lz = l.z;
-        double const lzr = lz * rpp;
-        l.px = fma(a_, fma(-lzr, px, lx), l.px);
-        l.py = fma(a_, fma(-lzr, py, ly), l.py);
+        s.zeta = fma(L, fma(s.hr2, p2, -s.rvvm1), s.zeta);
+        // lambda: d(out)/d(px, py, delta) with rpp(delta), rvv(delta):
+        //   l.px += L rpp (lx - lz rpp px), l.py likewise,
+        //   l.d += L (drpp (lx px + ly py - lz rpp (px^2 + py^2)) + lz drvv)
+        double const lx = l.x, ly = l.y;
+        l.px = fma(a_, fma(-s.lzr, px, lx), l.px);
+        l.py = fma(a_, fma(-s.lzr, py, ly), l.py);
         double const s1 = fma(ly, py, lx * px);
-        double const w_ = fma(lz, s.drvv, s.drpp * fma(-lz, s2, s1));
-        l.d = fma(L, w_, l.d);
+        l.d = fma(L, fma(s.drpp, fma(-s.lzr, p2, s1), s.lzdrvv), l.d);
         break;
     }
     case OP_DRIFT_EXACT: {  // be_drift/track.h:71-97
@@ -206,70 +275,12 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         l.d += lx * (px * a_d) + ly * (py * a_d) + lz * (L * drvv - lpzi - opd * a_d);
         break;
     }
-    case OP_MULTIPOLE:
-    case OP_MULTIPOLE_CURV: {  // be_multipole/track.h:38-112
-        int const n = (int)aux;
-        const uint64_t *bal = rec + 1;
-        bool const curv = op == OP_MULTIPOLE_CURV;
-        double const chi = s.chi, x = s.x, y = s.y;
-        double const hxl = curv ? W(bal[2 * n + 2]) : 0.0;
-        double const hyl = curv ? W(bal[2 * n + 3]) : 0.0;
-        double const length = curv ? W(bal[2 * n + 4]) : 0.0;
-        double const lpx = l.px, lpy = l.py;
-        if (on) {
-            double pr, pi, dr, di;
-            horner2(bal, n, x, y, pr, pi, dr, di);
-            double dpx = -chi * pr, dpy = chi * pi;
-            if (curv) {
-                s.zeta -= chi * (y * hyl - x * hxl);
-                dpx += hxl + hxl * s.delta;
-                dpy -= hyl + hyl * s.delta;
-                if (length > 0.0) {
-                    dpx -= chi * W(bal[0]) * x * hxl / length;
-                    dpy += chi * W(bal[1]) * y * hyl / length;
-                }
-            }
-            s.px -= dpx;
-            s.py -= dpy;
-            l.x += chi * (-lpx * dr + lpy * di);
-            l.y += chi * (lpx * di + lpy * dr);
-            if (curv) {
-                l.x -= l.z * chi * hxl;
-                l.y += l.z * chi * hyl;
-                l.d += lpx * hxl - lpy * hyl;
-                if (length > 0.0) {
-                    l.x -= lpx * chi * W(bal[0]) * hxl / length;
-                    l.y += lpy * chi * W(bal[1]) * hyl / length;
-                }
-            }
-        }
-        if (a.pbeg) {
-            // d(dpx, dpy)/d bal[2k] = chi (-Re z^k, Im z^k); / d bal[2k+1] = chi (Im z^k, Re z^k)
-            double const cx = chi * lpx, cy = chi * lpy;
-            for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j) {
-                int const k2 = a.pkind[j];
-                double g = 0.0;
-                if (on && k2 >= 0) {
-                    int const kk = k2 >> 1;
-                    double zr = 1.0, zi = 0.0;
-                    if (kk > 0) {
-                        zr = x;
-                        zi = y;
-                        for (int k = 1; k < kk; ++k) {
-                            double const t = fma(zr, x, -zi * y);
-                            zi = fma(zr, y, zi * x);
-                            zr = t;
-                        }
-                    }
-                    g = (k2 & 1) ? fma(cx, zi, cy * zr) : fma(-cx, zr, cy * zi);
-                    if (length > 0.0 && k2 == 0) g -= cx * hxl * x / length;
-                    if (length > 0.0 && k2 == 1) g += cy * hyl * y / length;
-                }
-                add_grad(a, j, g, on);
-            }
-        }
+    case OP_MULTIPOLE:  // be_multipole/track.h:38-112
+        reverse_multipole<false>(s, l, rec + 1, (int)aux, a, e, on);
         break;
-    }
+    case OP_MULTIPOLE_CURV:
+        reverse_multipole<true>(s, l, rec + 1, (int)aux, a, e, on);
+        break;
     case OP_CAVITY: {  // be_cavity/track.h:39-67 + particles.h:5255-5297
         double gV = 0.0;
         if (on) {
@@ -312,6 +323,9 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
             gV = lP * s.q * sph / s.energy0;
             l.z = lz;
             l.d = ld;
+            s.hr2 = 0.5 * s.rpp * s.rpp;
+            s.lzr = lz * s.rpp;
+            s.lzdrvv = lz * drvv;
         }
         if (a.pbeg) {
             for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j)
@@ -394,13 +408,13 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams a)
         s.chi = d[15 * n + i];
         s.q = d[0 * n + i] * d[16 * n + i];
         s.energy0 = sqrt(p0c * p0c + mass0 * mass0);
-        set_delta_terms(s);
         l.x = a.lam[0 * n + i];
         l.px = a.lam[1 * n + i];
         l.y = a.lam[2 * n + i];
         l.py = a.lam[3 * n + i];
         l.z = a.lam[4 * n + i];
         l.d = a.lam[5 * n + i];
+        set_delta_terms(s, l.z);
     }
     for (int64_t turn = a.turn_end - 1; turn >= a.turn_begin; --turn) {
         bool const act = part && turn >= t_first && turn <= t_last;

@@ -79,9 +79,14 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             aux = (uint32_t)order;
             p.assign(bal, bal + 2 * order + 2);
             if (curv) {
+                double const length = w2d(w[1]);
                 p.push_back(w[2]);
                 p.push_back(w[3]);
                 p.push_back(w[1]);
+                // hxl / length, hyl / length (0 without length): the
+                // derivative kernels' form of the b1 / a1 terms
+                p.push_back(d2w(length > 0.0 ? hxl / length : 0.0));
+                p.push_back(d2w(length > 0.0 ? hyl / length : 0.0));
             }
             break;
         }

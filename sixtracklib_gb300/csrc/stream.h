@@ -18,7 +18,7 @@ enum Op : uint32_t {
     OP_DRIFT = 1,           // [L]            aux bit0: global aperture check
     OP_DRIFT_EXACT = 2,     // [L]            aux bit0: global aperture check
     OP_MULTIPOLE = 3,       // [bal 0..2n+1]  aux = order n
-    OP_MULTIPOLE_CURV = 4,  // [bal..., hxl, hyl, length]  aux = order n
+    OP_MULTIPOLE_CURV = 4,  // [bal..., hxl, hyl, length, hxl/length, hyl/length]  aux = order n
     OP_CAVITY = 5,          // [voltage, k*frequency, deg2rad*lag]
     OP_XYSHIFT = 6,         // [-dx, -dy]
     OP_SROTATION = 7,       // [cos_z, sin_z]
