@@ -16,21 +16,32 @@ Loss bookkeeping follows NS(Track_particle_until_turn) (track/track.h and
 track.h): a particle stops at the element where an aperture check fails and
 keeps the coordinates (and their derivatives) it had there.  Supported
 elements: Drift, DriftExact (with the global aperture check after each drift,
-limits 1 m, be_limit/track.h:54-88), Multipole, Cavity, XYShift, SRotation,
-DipoleEdge, LimitRect, LimitEllipse, LimitRectEllipse, BeamMonitor (no-op).
+limits 1 m, be_limit/track.h:54-88), Multipole, Cavity, RFMultipole, XYShift,
+SRotation, DipoleEdge, LimitRect, LimitEllipse, LimitRectEllipse,
+BeamBeam4D, SCCoasting, SCQGaussProfile, SCInterpolatedProfile, BeamMonitor
+(no-op).  The Faddeeva function's value comes from the C oracle's cerrf; its
+derivative is w'(z) = -2 z w(z) + 2 i / sqrt(pi) at that value.
 """
 
 from __future__ import annotations
 
 import numpy as np
 
+import ctypes as C
+
 from sixtracklib_gb300.beam_elements import (
-    BeamMonitor, Cavity, DipoleEdge, Drift, DriftExact, LimitEllipse, LimitRect,
-    LimitRectEllipse, Multipole, SRotation, XYShift)
+    BeamBeam4D, BeamMonitor, Cavity, DipoleEdge, Drift, DriftExact, LimitEllipse, LimitRect,
+    LimitRectEllipse, Multipole, RFMultipole, SCCoasting, SCInterpolatedProfile,
+    SCQGaussProfile, SRotation, XYShift)
 from sixtracklib_gb300.particles import COL
 
 PI = 3.1415926535897932384626433832795028841971693993751  # constants.h
 C_LIGHT = 299792458.0
+EPS0 = 8.854187817620e-12
+SQRT_PI = 1.7724538509055160272981674833411451827975494561224
+QELEM = 1.60217662e-19        # SIXTRL_QELEM (beam-beam)
+CHARGE0_SI = 1.602176634e-19  # NS(PhysConst_charge0_si) (space charge)
+DEG2RAD_C = 0.0174532925199432957692369076848861271344287188854172546
 
 
 class Dual:
@@ -87,8 +98,74 @@ def dsin(a: Dual) -> Dual:
     return Dual(np.sin(a.v), a.d * np.cos(a.v))
 
 
+def dexp(a: Dual) -> Dual:
+    e = np.exp(a.v)
+    return Dual(e, a.d * e)
+
+
+def dcos(a: Dual) -> Dual:
+    return Dual(np.cos(a.v), -a.d * np.sin(a.v))
+
+
+def dabs(a: Dual) -> Dual:
+    sg = np.where(a.v < 0, -1.0, 1.0)
+    return Dual(np.abs(a.v), a.d * sg)
+
+
 def _where(mask, a: Dual, b: Dual) -> Dual:
     return Dual(np.where(mask, a.v, b.v), np.where(mask, a.d, b.d))
+
+
+_CERRF = None  # vectorised w(z) of the C oracle, set by track_until
+
+
+def dcerrf(zr: Dual, zi: Dual):
+    """w(z) as two Duals: the C oracle's value, derivative -2 z w + 2i/sqrt(pi)."""
+    wr, wi = _CERRF(np.broadcast_to(zr.v, np.shape(zr.v)), np.broadcast_to(zi.v, np.shape(zi.v)))
+    dr = -2.0 * (zr.v * wr - zi.v * wi)
+    di = -2.0 * (zr.v * wi + zi.v * wr) + 2.0 / SQRT_PI
+    return Dual(wr, dr * zr.d - di * zi.d), Dual(wi, dr * zi.d + di * zr.d)
+
+
+def fields_gauss(x: Dual, y: Dual, sigma_x, sigma_y, min_sigma_diff):
+    """NS(get_Ex_Ey_Gx_Gy_gauss) without G terms (be_beamfields/
+    gauss_fields.h:56-208): (Ex, Ey)."""
+    if abs(sigma_x - sigma_y) < min_sigma_diff:
+        sigma = 0.5 * (sigma_x + sigma_y)
+        r2 = x * x + y * y
+        lin = r2.v < 1e-20
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t_main = (1 - dexp(-0.5 * r2 / (sigma * sigma))) / (2. * PI * EPS0 * r2)
+            t_lin = dsqrt(r2) / (2. * PI * EPS0 * sigma)
+        t_lin.d = np.where(np.isfinite(t_lin.d), t_lin.d, 0.0)
+        t = _where(lin, t_lin, t_main)
+        return t * x, t * y
+    abx, aby = dabs(x), dabs(y)
+    if sigma_x > sigma_y:
+        S = np.sqrt(2. * (sigma_x * sigma_x - sigma_y * sigma_y))
+        fact = 1. / (2. * EPS0 * SQRT_PI * S)
+        eta_re = sigma_y / sigma_x * abx
+        eta_im = sigma_x / sigma_y * aby
+        wzr, wzi = dcerrf(abx / S, aby / S)
+        wer, wei = dcerrf(eta_re / S, eta_im / S)
+        e = dexp(-abx * abx / (2 * sigma_x * sigma_x) - aby * aby / (2 * sigma_y * sigma_y))
+        ex = fact * (wzi - wei * e)
+        ey = fact * (wzr - wer * e)
+    elif sigma_x < sigma_y:
+        S = np.sqrt(2. * (sigma_y * sigma_y - sigma_x * sigma_x))
+        fact = 1. / (2. * EPS0 * SQRT_PI * S)
+        eta_re = sigma_x / sigma_y * aby
+        eta_im = sigma_y / sigma_x * abx
+        wzr, wzi = dcerrf(aby / S, abx / S)
+        wer, wei = dcerrf(eta_re / S, eta_im / S)
+        e = dexp(-aby * aby / (2 * sigma_y * sigma_y) - abx * abx / (2 * sigma_x * sigma_x))
+        ey = fact * (wzi - wei * e)
+        ex = fact * (wzr - wer * e)
+    else:
+        raise ValueError("equal beam sizes outside the round-beam tolerance")
+    ex = _where(x.v < 0, -ex, ex)
+    ey = _where(y.v < 0, -ey, ey)
+    return ex, ey
 
 
 class DualParticles:
@@ -106,7 +183,10 @@ class DualParticles:
             setattr(self, name, Dual(f[COL[name]].copy(), np.zeros((k, n))))
         self.beta0 = f[COL["beta0"]].copy()
         self.chi = f[COL["chi"]].copy()
+        self.q0 = f[COL["q0"]].copy()
+        self.charge_ratio = f[COL["charge_ratio"]].copy()
         self.q = f[COL["q0"]] * f[COL["charge_ratio"]]
+        self.p0c = f[COL["p0c"]].copy()
         self.energy0 = np.sqrt(f[COL["p0c"]] ** 2 + f[COL["mass0"]] ** 2)
         self.state = i[COL["state"]].copy()
         self.at_turn = i[COL["at_turn"]].copy()
@@ -183,14 +263,18 @@ def multipole(p: DualParticles, order, bal, hxl, hyl, length):
 
 
 def cavity(p: DualParticles, voltage, frequency, lag):
-    """be_cavity/track.h:39-67 and NS(Particles_add_to_energy_value),
-    particles.h:5255-5297; `voltage` may be a Dual."""
+    """be_cavity/track.h:39-67; `voltage` may be a Dual."""
     deg2rad = PI / 180.0
     k_factor = (2.0 * PI) / C_LIGHT
     beta0 = p.beta0
     tau = p.zeta / (beta0 * p.rvv)
     phase = deg2rad * lag - (k_factor * frequency) * tau
-    energy = p.q * voltage * dsin(phase)
+    add_energy(p, p.q * voltage * dsin(phase))
+
+
+def add_energy(p: DualParticles, energy):
+    """NS(Particles_add_to_energy_value), particles.h:5255-5297."""
+    beta0 = p.beta0
     db0 = p.delta * beta0
     ptau_beta0 = energy / p.energy0 + dsqrt(db0 * db0 + 2.0 * db0 * beta0 + 1.0) - 1.0
     ptau = ptau_beta0 / beta0
@@ -202,6 +286,156 @@ def cavity(p: DualParticles, voltage, frequency, lag):
     p.zeta = p.zeta * (rvv / p.rvv)
     p.rvv = rvv
     p.rpp = 1.0 / opd
+
+
+def rf_multipole(p: DualParticles, obj):
+    """be_rfmultipole/track.h:39-118."""
+    order = int(obj.order)
+    bal = np.asarray(obj.bal)
+    phase = np.asarray(obj.phase)
+    deg2rad = PI / 180.0
+    k = float(obj.frequency) * (2.0 * PI) / C_LIGHT
+    x, y = p.x, p.y
+    q = p.q * 1.0
+    ktau = k * p.zeta / (p.beta0 * p.rvv)
+    dpx = dpy = dptr = 0.0
+    zre, zim = 1.0, 0.0
+    for kk in range(order + 1):
+        pn = DEG2RAD_C * float(phase[2 * kk]) - ktau
+        ps = deg2rad * float(phase[2 * kk + 1]) - ktau
+        bn, bs = float(bal[2 * kk]), float(bal[2 * kk + 1])
+        cn, cs, sn, ss = dcos(pn), dcos(ps), dsin(pn), dsin(ps)
+        dpx = dpx + (cn * (bn * zre) - cs * (bs * zim))
+        dpy = dpy + (cs * (bs * zre) + cn * (bn * zim))
+        zret = zre * x - zim * y
+        zim = zim * x + zre * y
+        zre = zret
+        dptr = dptr + (sn * (bn * zre) - ss * (bs * zim))
+    cav = q * (float(obj.voltage) * dsin(float(obj.lag) * DEG2RAD_C - ktau))
+    rfm = -q * ((k * p.p0c) * dptr)
+    p.px = p.px + (-p.chi * dpx)
+    p.py = p.py + p.chi * dpy
+    add_energy(p, cav + rfm)
+
+
+def beam_beam_4d(p: DualParticles, d):
+    """be_beamfields/track.h:89-149 (qratio = 1)."""
+    if not d[10] > 0.:
+        return
+    charge = 1. * p.q0 * QELEM
+    x = p.x - d[6]
+    y = p.y - d[7]
+    beta = p.beta0 / p.rvv
+    p0c = p.p0c * QELEM
+    ex, ey = fields_gauss(x, y, d[2], d[3], d[5])
+    fk = p.chi * d[1] * d[0] * charge * (1. + beta * d[4]) / (p0c * (beta + d[4]))
+    p.px = p.px + (fk * ex - d[8])
+    p.py = p.py + (fk * ey - d[9])
+
+
+def sc_coasting(p: DualParticles, o):
+    """be_beamfields/track.h:154-198."""
+    charge = CHARGE0_SI * p.q0
+    beta0 = p.beta0
+    pc0 = p.p0c * CHARGE0_SI
+    fk = (o.number_of_particles * o.length * p.chi * p.charge_ratio * charge * charge *
+          (1.0 - beta0 * beta0))
+    fk = fk / (o.circumference * pc0 * beta0 * p.rvv)
+    ex, ey = fields_gauss(p.x - o.x_co, p.y - o.y_co, o.sigma_x, o.sigma_y, o.min_sigma_diff)
+    p.px = p.px + fk * ex
+    p.py = p.py + fk * ey
+
+
+def q_gauss(z: Dual, q, sqrt_beta, cq):
+    """NS(Math_q_gauss), internal/math_qgauss.h:114-175."""
+    arg = -(sqrt_beta * sqrt_beta * z * z)
+    omq = 1.0 - q
+    if abs(omq) >= 1e-6:
+        u = 1.0 + omq * arg
+        neg = u.v < 0.0
+        uv = np.where(neg, 0.0, u.v)
+        ud = np.where(neg, 0.0, u.d)
+        ev = uv ** (1.0 / omq)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ed = np.where(uv > 0.0, ud * (ev / uv) / omq, 0.0)
+        e = Dual(ev, ed)
+    else:
+        e = dexp(arg)
+    return (sqrt_beta / cq) * e
+
+
+def sc_qgauss(p: DualParticles, o):
+    """be_beamfields/track.h:203-268."""
+    charge = CHARGE0_SI * p.q0
+    beta0 = p.beta0
+    beta = beta0 * p.rvv
+    pc0 = p.p0c * CHARGE0_SI
+    z = p.zeta / p.rvv
+    fk = p.chi * p.charge_ratio * o.length * charge * charge * (1.0 - beta0 * beta)
+    fk = fk * o.number_of_particles
+    fk = fk * q_gauss(z, o.q_param, 1.0 / (np.sqrt(2.0) * o.bunchlength_rms), o.cq)
+    fk = fk / (pc0 * beta)
+    ex, ey = fields_gauss(p.x - o.x_co, p.y - o.y_co, o.sigma_x, o.sigma_y, o.min_sigma_diff)
+    p.px = p.px + fk * ex
+    p.py = p.py + fk * ey
+
+
+def _read_table(addr):
+    """A NS(LineDensityProfileData) at a host address: (method, num_values,
+    z0, dz, window, values offset, derivatives offset) -- the window spans
+    both arrays (reads outside it give 0, as in the oracle)."""
+    w = C.cast(C.c_void_p(int(addr)), C.POINTER(C.c_uint64))
+    method, cap, va, da, nv = int(w[0]), int(w[1]), int(w[2]), int(w[3]), int(w[6])
+    z0 = C.cast(C.c_void_p(int(addr) + 32), C.POINTER(C.c_double))[0]
+    dz = C.cast(C.c_void_p(int(addr) + 40), C.POINTER(C.c_double))[0]
+    lo, hi = min(va, da), max(va, da) + cap * 8
+    win = np.ctypeslib.as_array(C.cast(C.c_void_p(lo), C.POINTER(C.c_double)),
+                                shape=((hi - lo) // 8,)).copy()
+    return method, nv, z0, dz, win, (va - lo) // 8, (da - lo) // 8
+
+
+def _interp(table, z: Dual):
+    """NS(LineDensityProfileData_interpolate_value) on Duals."""
+    method, nv, z0, dz, win, vo, do = table
+    inside = (z.v <= z0 + dz * nv) & (z.v >= z0)
+    idx = np.where(inside, ((z.v - z0) / dz).astype(np.int64), 0)
+
+    def rd(off, i):
+        k = off + i
+        ok = (k >= 0) & (k < win.size)
+        return np.where(ok, win[np.clip(k, 0, win.size - 1)], 0.0)
+
+    if method == 0:
+        r = rd(vo, idx) + (z - (z0 + dz * idx)) * rd(do, idx)
+    elif method == 1:
+        t2 = (z0 + dz * (idx + 1) - z) / dz
+        t1 = (z - (z0 + dz * idx)) / dz
+        r = rd(vo, idx + 1) * t1 + rd(vo, idx) * t2
+        r = r - rd(do, idx) * dz * dz * (t2 - t2 * t2 * t2) / 6.0
+        r = r - rd(do, idx + 1) * dz * dz * (t1 - t1 * t1 * t1) / 6.0
+    else:
+        r = Dual(np.zeros_like(z.v), np.zeros_like(z.d))
+    zero = Dual(np.zeros_like(z.v), np.zeros_like(z.d))
+    return _where(inside, r, zero)
+
+
+def sc_interpolated(p: DualParticles, o):
+    """be_beamfields/track.h:273-337."""
+    charge = CHARGE0_SI * p.q0
+    beta0 = p.beta0
+    beta = beta0 * p.rvv
+    pc0 = p.p0c * CHARGE0_SI
+    fk = (p.chi * p.charge_ratio * o.length * o.number_of_particles * charge * charge *
+          (1.0 - beta0 * beta))
+    table = _read_table(o.interpol_data_addr) if o.interpol_data_addr else None
+    if table is not None and table[0] != 255 and table[1] > 0:
+        fk = fk * _interp(table, p.zeta)
+    else:
+        fk = fk * o.line_density_prof_fallback
+    fk = fk / (pc0 * beta)
+    ex, ey = fields_gauss(p.x - o.x_co, p.y - o.y_co, o.sigma_x, o.sigma_y, o.min_sigma_diff)
+    p.px = p.px + fk * ex
+    p.py = p.py + fk * ey
 
 
 def srotation(p: DualParticles, cz, sz):
@@ -248,6 +482,11 @@ def track_until(elements, block: np.ndarray, until_turn: int, params=(), x_limit
     Returns ``(values 6 x n, derivatives (6 + m) x 6 x n, state, at_turn,
     at_element)``; rows in the order x, px, y, py, zeta, delta.
     """
+    global _CERRF
+    if _CERRF is None:
+        from oracle.pyoracle import Oracle
+
+        _CERRF = Oracle().cerrf_n
     objs = list(elements.get_elements())
     m = len(params)
     k = 6 + m
@@ -298,6 +537,16 @@ def track_until(elements, block: np.ndarray, until_turn: int, params=(), x_limit
                 t = x * x * obj.b_squ + y * y * obj.a_squ
                 alive = ((x <= obj.max_x) & (x >= -obj.max_x) & (y <= obj.max_y) &
                          (y >= -obj.max_y) & (t <= obj.a_b_squ))
+            elif isinstance(obj, RFMultipole):
+                rf_multipole(p, obj)
+            elif isinstance(obj, BeamBeam4D):
+                beam_beam_4d(p, [float(v) for v in np.asarray(obj.data)])
+            elif isinstance(obj, SCCoasting):
+                sc_coasting(p, obj)
+            elif isinstance(obj, SCQGaussProfile):
+                sc_qgauss(p, obj)
+            elif isinstance(obj, SCInterpolatedProfile):
+                sc_interpolated(p, obj)
             elif isinstance(obj, BeamMonitor):
                 pass
             else:

@@ -491,6 +491,12 @@ void orc_cerrf(double in_re, double in_im, double *w_re, double *w_im)
     *w_im = wy;
 }
 
+/* Vectorised form for the dual-number oracle (one call per array). */
+void orc_cerrf_n(const double *re, const double *im, double *w_re, double *w_im, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) orc_cerrf(re[i], im[i], &w_re[i], &w_im[i]);
+}
+
 /* gauss_fields.h:56-66 (Delta_x = Delta_y = 0 at every call site) */
 static void field_round(double sigma, double x, double y, double *ex,
                         double *ey)

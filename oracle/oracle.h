@@ -74,6 +74,7 @@ int64_t orc_ebe_store_index(const orc_ebe_config *cfg, int64_t particle_id,
                             int64_t at_element, int64_t at_turn);
 
 void orc_cerrf(double re, double im, double *w_re, double *w_im);
+void orc_cerrf_n(const double *re, const double *im, double *w_re, double *w_im, int64_t n);
 
 void orc_fields_gauss(double x, double y, double sigma_x, double sigma_y,
                       double min_sigma_diff, int skip_gs, double *ex,

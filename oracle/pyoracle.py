@@ -158,6 +158,16 @@ class Oracle:
     def ebe_store_index(self, cfg, pid, elem, turn):
         return self._ebe_idx(C.addressof(cfg), pid, elem, turn)
 
+    def cerrf_n(self, re, im):
+        """w(z) of arrays (the oracle's cerrf, element by element)."""
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = np.ascontiguousarray(im, dtype=np.float64)
+        wr, wi = np.empty_like(re), np.empty_like(re)
+        fn = self.lib.orc_cerrf_n
+        fn.argtypes = [C.c_void_p] * 4 + [C.c_int64]
+        fn(re.ctypes.data, im.ctypes.data, wr.ctypes.data, wi.ctypes.data, re.size)
+        return wr, wi
+
     def cerrf(self, re, im):
         a, b = C.c_double(), C.c_double()
         self._cerrf(float(re), float(im), C.byref(a), C.byref(b))

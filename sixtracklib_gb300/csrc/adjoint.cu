@@ -82,7 +82,7 @@ struct RState {
     double hr2;     // rpp^2 / 2
     double lzr;     // lambda_zeta * rpp
     double lzdrvv;  // lambda_zeta * d rvv / d delta
-    double beta0, chi, q, energy0;
+    double beta0, chi, q, energy0, p0c, q0, cr;  // q = q0 * charge_ratio (cr)
 };
 
 // Q(delta) = sqrt(delta^2 b0^2 + 2 delta b0^2 + 1) = 1 + ptau * beta0
@@ -160,6 +160,338 @@ __device__ __forceinline__ void horner2(const uint64_t *bal, int n, double x, do
         pr = npr;
         pi = npi;
     }
+}
+
+__device__ __forceinline__ void refresh_lz(RState &s, const Lam &l)
+{
+    s.lzr = l.z * s.rpp;
+    s.lzdrvv = l.z * s.drvv;
+}
+
+// Reverse of NS(Particles_add_to_energy_value) (particles.h:5255-5297) for
+// an energy change dE (in units of energy0) that the caller knows from the
+// map's output: restores delta, rvv, rpp and zeta (zeta *= rvv_new / rvv_old
+// is undone), applies the transposed Jacobian of the direct dependencies
+// and returns lambda_P, the adjoint of P = dE + Q(delta) - 1, from which the
+// caller adds the terms of dE's own dependencies.  Call refresh_lz after
+// the last change to lambda_zeta.
+__device__ __forceinline__ double reverse_add_energy(RState &s, Lam &l, double dEn)
+{
+    double const beta0 = s.beta0, b2 = beta0 * beta0;
+    double const zeta_o = s.zeta, rvv_o = s.rvv, delta_o = s.delta;
+    double const Qo = q_of_delta(delta_o, beta0);
+    double const P = b2 * delta_o * (delta_o + 2.0) / (Qo + 1.0);  // Qo - 1
+    double const opdn = 1.0 + delta_o;
+    // input: Q_in - 1 = P - dE / E0
+    double const qm1 = P - dEn;
+    double const Qi = 1.0 + qm1;
+    double const r = qm1 * (qm1 + 2.0) / b2;  // (1 + delta_in)^2 - 1
+    double const opd = sqrt(r + 1.0);
+    double const rvv = opd / Qi;
+    double const zeta = zeta_o * rvv / rvv_o;
+    s.delta = r / (opd + 1.0);
+    s.rvv = rvv;
+    s.rpp = 1.0 / opd;
+    s.zeta = zeta;
+    double const drvv = (1.0 - b2) / (Qi * Qi * Qi);
+    s.drvv = drvv;
+    s.drpp = -s.rpp * s.rpp;
+    s.rvvm1 = rvv - 1.0;
+    s.hr2 = 0.5 * s.rpp * s.rpp;
+    double const dopd_dP = (1.0 + P) / (b2 * opdn);
+    double const drvvn_dP = dopd_dP / (1.0 + P) - opdn / ((1.0 + P) * (1.0 + P));
+    double const lP = l.d * dopd_dP + l.z * (zeta / rvv) * drvvn_dP;
+    double const lz = l.z * (rvv_o / rvv);
+    l.d = -l.z * (zeta * rvv_o / (rvv * rvv)) * drvv + lP * (b2 * opd / Qi);
+    l.z = lz;
+    return lP;
+}
+
+// Adjoint of tau = zeta / (beta0 rvv(delta)) at the (restored) input.
+__device__ __forceinline__ void add_tau_adjoint(const RState &s, Lam &l, double ltau)
+{
+    double const br = s.beta0 * s.rvv;
+    l.z += ltau / br;
+    l.d -= ltau * s.zeta / (br * s.rvv) * s.drvv;
+}
+
+// The Gaussian field of NS(get_Ex_Ey_Gx_Gy_gauss) without the G terms
+// (be_beamfields/gauss_fields.h:56-208), as the forward kernel computes it,
+// and its Jacobian d(Ex, Ey)/d(x, y).  Elliptic beams: d w / d z = -2 z w +
+// 2 i / sqrt(pi) evaluated with the same w(z) (CERN algorithm), so the
+// Jacobian is that of the exact Faddeeva function at the approximated w.
+struct FieldJ {
+    double ex, ey, exx, exy, eyx, eyy;
+};
+
+__device__ __noinline__ FieldJ field_jacobian(double x, double y, double sigma_x, double sigma_y,
+                                              double min_sigma_diff)
+{
+    FieldJ f{};
+    if (fabs(sigma_x - sigma_y) < min_sigma_diff) {
+        double const sigma = 0.5 * (sigma_x + sigma_y);
+        double const r2 = x * x + y * y;
+        double t, dt;  // dt = d t / d r2
+        if (r2 < 1e-20) {
+            t = sqrt(r2) / (2. * kPiD * kEps0D * sigma);
+            dt = (r2 > 0.0) ? t / (2.0 * r2) : 0.0;
+        } else {
+            double const e = exp(-0.5 * r2 / (sigma * sigma));
+            t = (1 - e) / (2. * kPiD * kEps0D * r2);
+            dt = (e / (2. * kPiD * kEps0D * 2.0 * sigma * sigma) - t) / r2;
+        }
+        f.ex = t * x;
+        f.ey = t * y;
+        f.exx = t + 2.0 * x * x * dt;
+        f.exy = 2.0 * x * y * dt;
+        f.eyx = f.exy;
+        f.eyy = t + 2.0 * y * y * dt;
+        return f;
+    }
+    double const abx = fabs(x), aby = fabs(y);
+    double const sgn_xy = ((x < 0) != (y < 0)) ? -1.0 : 1.0;
+    double const two_isqpi = 2.0 / kSqrtPiD;
+    // first quadrant: u along the wider axis, v along the other
+    bool const xwide = sigma_x > sigma_y;
+    if (!(sigma_x > sigma_y) && !(sigma_x < sigma_y)) return f;  // the reference's 1/0
+    double const su = xwide ? sigma_x : sigma_y, sv = xwide ? sigma_y : sigma_x;
+    double const au = xwide ? abx : aby, av = xwide ? aby : abx;
+    double const S = sqrt(2. * (su * su - sv * sv));
+    double const fact = 1. / (2. * kEps0D * kSqrtPiD * S);
+    double const eta_re = sv / su * au, eta_im = su / sv * av;
+    double z1r = au / S, z1i = av / S, z2r = eta_re / S, z2i = eta_im / S;
+    double w1r, w1i, w2r, w2i;
+    cerrf(z1r, z1i, &w1r, &w1i);
+    cerrf(z2r, z2i, &w2r, &w2i);
+    double const e = exp(-au * au / (2 * su * su) - av * av / (2 * sv * sv));
+    // fields along (v, u): Fv = fact (Im w1 - Im w2 e), Fu = fact (Re w1 - Re w2 e)
+    double const fv = fact * (w1i - w2i * e);
+    double const fu = fact * (w1r - w2r * e);
+    // w'(z) = -2 z w + 2 i / sqrt(pi)
+    double const d1r = -2.0 * (z1r * w1r - z1i * w1i), d1i = -2.0 * (z1r * w1i + z1i * w1r) + two_isqpi;
+    double const d2r = -2.0 * (z2r * w2r - z2i * w2i), d2i = -2.0 * (z2r * w2i + z2i * w2r) + two_isqpi;
+    // d/du: w1 -> d1 / S, w2 -> d2 (sv / su) / S, e -> -au / su^2 e
+    // d/dv: w1 -> i d1 / S, w2 -> i d2 (su / sv) / S, e -> -av / sv^2 e
+    double const cu2 = sv / su / S, cv2 = su / sv / S;
+    double const eu = -au / (su * su) * e, ev = -av / (sv * sv) * e;
+    double const fv_u = fact * (d1i / S - (d2i * cu2 * e + w2i * eu));
+    double const fv_v = fact * (d1r / S - (d2r * cv2 * e + w2i * ev));
+    double const fu_u = fact * (d1r / S - (d2r * cu2 * e + w2r * eu));
+    double const fu_v = fact * (-d1i / S - (-d2i * cv2 * e + w2r * ev));
+    // map back: the wide axis carries Fv (Ex for sigma_x > sigma_y)
+    double exq, eyq, ex_x, ex_y, ey_x, ey_y;
+    if (xwide) {  // u = x, v = y: Ex = Fv, Ey = Fu
+        exq = fv;
+        eyq = fu;
+        ex_x = fv_u;
+        ex_y = fv_v;
+        ey_x = fu_u;
+        ey_y = fu_v;
+    } else {      // u = y, v = x: Ey = Fv, Ex = Fu
+        eyq = fv;
+        exq = fu;
+        ey_y = fv_u;
+        ey_x = fv_v;
+        ex_y = fu_u;
+        ex_x = fu_v;
+    }
+    f.ex = (x < 0) ? -exq : exq;
+    f.ey = (y < 0) ? -eyq : eyq;
+    f.exx = ex_x;
+    f.eyy = ey_y;
+    f.exy = sgn_xy * ex_y;
+    f.eyx = sgn_xy * ey_x;
+    return f;
+}
+
+// A thin transverse kick px += K E_x(x - x0, y - y0) - cx, py += K E_y - cy
+// with K depending on delta and zeta: restore px, py and apply the
+// transposed Jacobian.
+__device__ __forceinline__ void reverse_field_kick(RState &s, Lam &l, const FieldJ &f, double K,
+                                                   double dK_ddelta, double dK_dzeta, double cx,
+                                                   double cy)
+{
+    s.px -= K * f.ex - cx;
+    s.py -= K * f.ey - cy;
+    double const lpx = l.px, lpy = l.py;
+    l.x += K * (lpx * f.exx + lpy * f.eyx);
+    l.y += K * (lpx * f.exy + lpy * f.eyy);
+    double const le = lpx * f.ex + lpy * f.ey;
+    l.d += le * dK_ddelta;
+    l.z += le * dK_dzeta;
+}
+
+// q-Gaussian line density and its derivative (internal/math_qgauss.h:114-175)
+__device__ __forceinline__ double q_gauss_d(double z, double q, double sqrt_beta, double cq,
+                                            double *dq_dz)
+{
+    double const arg = -(sqrt_beta * sqrt_beta * z * z);
+    double const darg = -2.0 * sqrt_beta * sqrt_beta * z;
+    double const omq = 1.0 - q;
+    double const abs_omq = (omq >= 0.0) ? omq : -omq;
+    double e, de;
+    if (abs_omq >= 1e-6) {
+        double u = 1.0 + omq * arg;
+        if (u < 0.0) u = 0.0;
+        e = pow(u, 1.0 / omq);
+        de = (u > 0.0) ? e / u * darg : 0.0;
+    } else {
+        e = exp(arg);
+        de = e * darg;
+    }
+    *dq_dz = (sqrt_beta / cq) * de;
+    return (sqrt_beta / cq) * e;
+}
+
+// d lambda / d z of the tabulated line density (see ldp_interpolate)
+__device__ __forceinline__ double ldp_slope(const uint64_t *c, double z)
+{
+    uint64_t const method = c[8];
+    int64_t const nv = (int64_t)c[9];
+    double const z0 = W(c[10]), dz = W(c[11]);
+    if (!((z <= z0 + dz * (double)nv) && (z >= z0))) return 0.0;
+    int64_t const idx = (int64_t)((z - z0) / dz);
+    if (method == 0) return ldp_word(c, c[13], idx);
+    if (method == 1) {
+        double const t2 = (z0 + dz * (double)(idx + 1) - z) / dz;
+        double const t1 = (z - (z0 + dz * (double)idx)) / dz;
+        return (ldp_word(c, c[12], idx + 1) - ldp_word(c, c[12], idx)) / dz +
+               ldp_word(c, c[13], idx) * dz * (1.0 - 3.0 * t2 * t2) / 6.0 -
+               ldp_word(c, c[13], idx + 1) * dz * (1.0 - 3.0 * t1 * t1) / 6.0;
+    }
+    return 0.0;
+}
+
+// be_rfmultipole/track.h:39-118: kicks of px, py and an energy change, all
+// functions of x, y and tau = zeta / (beta0 rvv), which the map preserves.
+__device__ __forceinline__ void reverse_rf_multipole_impl(RState &s, Lam &l, const uint64_t *rec,
+                                                          int order)
+{
+    double const voltage = W(rec[1]), frequency = W(rec[2]), lag = W(rec[3]);
+    const uint64_t *bal = rec + 4;
+    const uint64_t *phase = rec + 4 + 2 * order + 2;
+    double const DEG2RAD = kPiD / 180.0;
+    double const DEG2RAD_C = 0.0174532925199432957692369076848861271344287188854172546;
+    double const k = frequency * (2.0 * kPiD) / kClightD;
+    double const x = s.x, y = s.y, chi = s.chi;
+    double const ktau = k * s.zeta / (s.beta0 * s.rvv);
+    double dpx = 0, dpy = 0, dptr = 0, zre = 1.0, zim = 0.0, pre = 0.0, pim = 0.0;
+    double dpx_x = 0, dpx_y = 0, dpx_t = 0, dpy_x = 0, dpy_y = 0, dpy_t = 0;
+    double dptr_x = 0, dptr_y = 0, dptr_t = 0;
+    for (int kk = 0; kk <= order; ++kk) {
+        double sn, cn, ss, cs;
+        sincos(DEG2RAD_C * W(phase[2 * kk]) - ktau, &sn, &cn);
+        sincos(DEG2RAD * W(phase[2 * kk + 1]) - ktau, &ss, &cs);
+        double const bn = W(bal[2 * kk]), bs = W(bal[2 * kk + 1]);
+        // d z^kk / dx = kk z^(kk-1), d z^kk / dy = i kk z^(kk-1)
+        double const ar = kk * pre, ai = kk * pim;
+        dpx += cn * (bn * zre) - cs * (bs * zim);
+        dpy += cs * (bs * zre) + cn * (bn * zim);
+        dpx_x += cn * bn * ar - cs * bs * ai;
+        dpx_y -= cn * bn * ai + cs * bs * ar;
+        dpy_x += cs * bs * ar + cn * bn * ai;
+        dpy_y += cn * bn * ar - cs * bs * ai;
+        // d cos(a - k tau) / d tau = k sin(a - k tau)
+        dpx_t += k * (sn * (bn * zre) - ss * (bs * zim));
+        dpy_t += k * (ss * (bs * zre) + sn * (bn * zim));
+        pre = zre;
+        pim = zim;
+        double const zret = zre * x - zim * y;
+        zim = zim * x + zre * y;
+        zre = zret;
+        double const br = (kk + 1) * pre, bi = (kk + 1) * pim;
+        dptr += sn * (bn * zre) - ss * (bs * zim);
+        dptr_x += sn * bn * br - ss * bs * bi;
+        dptr_y -= sn * bn * bi + ss * bs * br;
+        // d sin(a - k tau) / d tau = -k cos(a - k tau)
+        dptr_t -= k * (cn * (bn * zre) - cs * (bs * zim));
+    }
+    double sc, cc;
+    sincos(lag * DEG2RAD_C - ktau, &sc, &cc);
+    double const q = s.q;
+    double const E = q * (voltage * sc) - q * ((k * s.p0c) * dptr);
+    double const E_x = -q * (k * s.p0c) * dptr_x, E_y = -q * (k * s.p0c) * dptr_y;
+    double const E_t = -q * voltage * cc * k - q * (k * s.p0c) * dptr_t;
+    // kicks: px_out = px_in - chi dpx, py_out = py_in + chi dpy
+    s.px += chi * dpx;
+    s.py -= chi * dpy;
+    double const lpx = l.px, lpy = l.py;
+    double const lE = reverse_add_energy(s, l, E / s.energy0) / s.energy0;
+    l.x += -chi * lpx * dpx_x + chi * lpy * dpy_x + lE * E_x;
+    l.y += -chi * lpx * dpx_y + chi * lpy * dpy_y + lE * E_y;
+    add_tau_adjoint(s, l, -chi * lpx * dpx_t + chi * lpy * dpy_t + lE * E_t);
+    refresh_lz(s, l);
+}
+
+// The space-charge and 4D beam-beam kicks (be_beamfields/track.h:89-337).
+__device__ __forceinline__ void reverse_beam_field_impl(RState &s, Lam &l, const uint64_t *rec,
+                                                        uint32_t op, uint32_t aux)
+{
+    const uint64_t *c = rec + 1;
+    double const beta0 = s.beta0, rvv = s.rvv;
+    if (op == OP_BB4D) {  // :89-149; c: q_part N sigma_x sigma_y beta_s msd Dx Dy Dpx Dpy
+        double const ch = 1. * s.q0 * kQelemD;  // qratio = 1 (track.h:121)
+        double const beta = beta0 / rvv, bs = W(c[4]);
+        double const A = s.chi * W(c[1]) * W(c[0]) * ch / (s.p0c * kQelemD);
+        double const K = A * (1. + beta * bs) / (beta + bs);
+        double const dK_dbeta = A * (bs * bs - 1.0) / ((beta + bs) * (beta + bs));
+        double const dK_dd = dK_dbeta * (-beta0 / (rvv * rvv)) * s.drvv;
+        FieldJ const f = field_jacobian(s.x - W(c[6]), s.y - W(c[7]), W(c[2]), W(c[3]), W(c[5]));
+        reverse_field_kick(s, l, f, K, dK_dd, 0.0, W(c[8]), W(c[9]));
+        return;
+    }
+    double const charge = kCharge0SiD * s.q0;
+    double const pc0 = s.p0c * kCharge0SiD;
+    if (op == OP_SC_COASTING) {  // :154-198; c: N C sigma_x sigma_y length x_co y_co msd
+        double const K = W(c[0]) * W(c[4]) * s.chi * s.cr * charge * charge * (1.0 - beta0 * beta0) /
+                         (W(c[1]) * pc0 * beta0 * rvv);
+        FieldJ const f = field_jacobian(s.x - W(c[5]), s.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]));
+        reverse_field_kick(s, l, f, K, -K / rvv * s.drvv, 0.0, 0.0, 0.0);
+        return;
+    }
+    // K = C0 g(rvv) lambda, g = (1 - beta0^2 rvv) / (beta0 rvv), g' = -1 / (beta0 rvv^2)
+    double const g = (1.0 - beta0 * beta0 * rvv) / (beta0 * rvv);
+    double const dg = -1.0 / (beta0 * rvv * rvv);
+    if (op == OP_SC_QGAUSS) {  // :203-268; c: N blen sigma_x sigma_y length x_co y_co msd q cq
+        double const C0 = s.chi * s.cr * W(c[4]) * charge * charge * W(c[0]) / pc0;
+        double const z = s.zeta / rvv;
+        double dq;
+        double const lam =
+            q_gauss_d(z, W(c[8]), 1.0 / (sqrt(2.0) * W(c[1])), W(c[9]), &dq);
+        double const K = C0 * g * lam;
+        double const dK_dz = C0 * g * dq / rvv;
+        double const dK_dd = C0 * (dg * lam + g * dq * (-s.zeta / (rvv * rvv))) * s.drvv;
+        FieldJ const f = field_jacobian(s.x - W(c[5]), s.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]));
+        reverse_field_kick(s, l, f, K, dK_dd, dK_dz, 0.0, 0.0);
+    } else {  // OP_SC_INTERP, :273-337; c: N sigma_x sigma_y length x_co y_co fallback msd ...
+        double const C0 = s.chi * s.cr * W(c[3]) * W(c[0]) * charge * charge / pc0;
+        double const lam = (aux & 1u) ? ldp_interpolate(c, s.zeta) : W(c[6]);
+        double const dlam = (aux & 1u) ? ldp_slope(c, s.zeta) : 0.0;
+        double const K = C0 * g * lam;
+        FieldJ const f = field_jacobian(s.x - W(c[4]), s.y - W(c[5]), W(c[1]), W(c[2]), W(c[7]));
+        reverse_field_kick(s, l, f, K, C0 * dg * lam * s.drvv, C0 * g * dlam, 0.0, 0.0);
+    }
+    refresh_lz(s, l);
+}
+
+// Out-of-line entry points take and return the state by value: a reference
+// would pin the caller's state to the stack for the whole walk.
+struct RevState {
+    RState s;
+    Lam l;
+};
+
+__device__ __noinline__ RevState reverse_rf_multipole(RevState r, const uint64_t *rec, int order)
+{
+    reverse_rf_multipole_impl(r.s, r.l, rec, order);
+    return r;
+}
+
+__device__ __noinline__ RevState reverse_beam_field(RevState r, const uint64_t *rec, uint32_t op,
+                                                    uint32_t aux)
+{
+    reverse_beam_field_impl(r.s, r.l, rec, op, aux);
+    return r;
 }
 
 // Multipole (be_multipole/track.h:38-112), with the curvature terms only in
@@ -284,48 +616,15 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
     case OP_CAVITY: {  // be_cavity/track.h:39-67 + particles.h:5255-5297
         double gV = 0.0;
         if (on) {
-            double const beta0 = s.beta0, b2 = beta0 * beta0;
             double const V = W(rec[1]), kf = W(rec[2]), lag = W(rec[3]);
-            // outputs; tau = zeta / (beta0 rvv) is unchanged by the map
-            double const zeta_o = s.zeta, rvv_o = s.rvv, delta_o = s.delta;
-            double const phase = lag - kf * (zeta_o / (beta0 * rvv_o));
+            // tau = zeta / (beta0 rvv) is unchanged by the map
+            double const phase = lag - kf * (s.zeta / (s.beta0 * s.rvv));
             double sph, cph;
             sincos(phase, &sph, &cph);
-            double const dEn = s.q * V * sph / s.energy0;
-            double const Qo = q_of_delta(delta_o, beta0);
-            double const P = b2 * delta_o * (delta_o + 2.0) / (Qo + 1.0);  // Qo - 1
-            double const opdn = 1.0 + delta_o;
-            // input: Q_in - 1 = P - dE / E0
-            double const qm1 = P - dEn;
-            double const Qi = 1.0 + qm1;
-            double const r = qm1 * (qm1 + 2.0) / b2;  // (1 + delta_in)^2 - 1
-            double const opd = sqrt(r + 1.0);
-            double const delta = r / (opd + 1.0);
-            double const rvv = opd / Qi;
-            double const zeta = zeta_o * rvv / rvv_o;
-            s.delta = delta;
-            s.rvv = rvv;
-            s.rpp = 1.0 / opd;
-            s.zeta = zeta;
-            // transposed Jacobian
-            double const drvv = (1.0 - b2) / (Qi * Qi * Qi);
-            s.drvv = drvv;
-            s.drpp = -s.rpp * s.rpp;
-            s.rvvm1 = rvv - 1.0;
-            double const dEc = s.q * V * cph / s.energy0;
-            double const dP_dzeta = -dEc * kf / (beta0 * rvv);
-            double const dP_ddelta = dEc * kf * zeta / (beta0 * rvv * rvv) * drvv + b2 * opd / Qi;
-            double const dopd_dP = (1.0 + P) / (b2 * opdn);
-            double const drvvn_dP = dopd_dP / (1.0 + P) - opdn / ((1.0 + P) * (1.0 + P));
-            double const lP = l.d * dopd_dP + l.z * (zeta / rvv) * drvvn_dP;
-            double const lz = l.z * (rvv_o / rvv) + lP * dP_dzeta;
-            double const ld = -l.z * (zeta * rvv_o / (rvv * rvv)) * drvv + lP * dP_ddelta;
+            double const lP = reverse_add_energy(s, l, s.q * V * sph / s.energy0);
+            add_tau_adjoint(s, l, lP * (-s.q * V * cph * kf / s.energy0));
+            refresh_lz(s, l);
             gV = lP * s.q * sph / s.energy0;
-            l.z = lz;
-            l.d = ld;
-            s.hr2 = 0.5 * s.rpp * s.rpp;
-            s.lzr = lz * s.rpp;
-            s.lzdrvv = lz * drvv;
         }
         if (a.pbeg) {
             for (int32_t j = a.pbeg[e]; j < a.pbeg[e + 1]; ++j)
@@ -333,6 +632,23 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         }
         break;
     }
+    case OP_RF_MULTIPOLE:
+        if (on) {
+            RevState r = reverse_rf_multipole(RevState{s, l}, rec, (int)aux);
+            s = r.s;
+            l = r.l;
+        }
+        break;
+    case OP_BB4D:
+    case OP_SC_COASTING:
+    case OP_SC_QGAUSS:
+    case OP_SC_INTERP:
+        if (on) {
+            RevState r = reverse_beam_field(RevState{s, l}, rec, op, aux);
+            s = r.s;
+            l = r.l;
+        }
+        break;
     case OP_XYSHIFT:  // be_xyshift/track.h:38-55
         if (!on) break;
         s.x -= W(rec[1]);
@@ -408,6 +724,9 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams a)
         s.chi = d[15 * n + i];
         s.q = d[0 * n + i] * d[16 * n + i];
         s.energy0 = sqrt(p0c * p0c + mass0 * mass0);
+        s.p0c = p0c;
+        s.q0 = d[0 * n + i];
+        s.cr = d[16 * n + i];
         l.x = a.lam[0 * n + i];
         l.px = a.lam[1 * n + i];
         l.y = a.lam[2 * n + i];
@@ -467,13 +786,10 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
         set_error("adjoint: invalid lattice");
         return -1;
     }
-    uint32_t const no_adjoint = (1u << OP_RF_MULTIPOLE) | (1u << OP_BB4D) | (1u << OP_BB6D) |
-                                (1u << OP_SC_COASTING) | (1u << OP_SC_QGAUSS) |
-                                (1u << OP_SC_INTERP) |
-                                (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
+    uint32_t const no_adjoint = (1u << OP_BB6D) | (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
     if (v.op_mask & no_adjoint) {
         set_error("adjoint: the lattice contains elements without an adjoint "
-                  "(RF multipole, beam-beam, space charge or a disabled map)");
+                  "(6D beam-beam or a disabled map)");
         return -1;
     }
     if (turn_end < turn_begin) {

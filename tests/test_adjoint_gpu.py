@@ -102,6 +102,28 @@ def test_adjoint_matches_dual_numbers(case, reconstruct):
     assert np.max(np.abs(gp - gp_d) / np.abs(gp_d)) < 1e-8, (gp, gp_d)
 
 
+@pytest.mark.parametrize("p0c", [7e12, 20e9])
+def test_field_kick_adjoints_match_dual_numbers(p0c):
+    """RF multipole, 4D beam-beam (round and elliptic), coasting, q-Gaussian
+    (q = 1, 1.2, 0.8) and interpolated (linear, cubic, fallback) space charge:
+    gradients of the coordinates and of the strengths within 1e-9 of the
+    dual-number pass."""
+    from .adjoint_cases import field_ring
+
+    e, params, tables = field_ring()
+    T, n = 8, 300
+    blk = lattices.gaussian_particles(n, seed=31, sz=0.08, p0c=p0c).block.copy()
+    w = np.random.default_rng(6).normal(size=(6, n)) / SIGMA[:, None]
+    gc_d, gp_d, vals_d, st_d = _dual_grads(e, params, blk, T, w)
+    for reconstruct in ("inverse", "recompute"):
+        gc, gp, vals, st = _gpu_grads(e, params, blk, T, w, every=3, reconstruct=reconstruct)
+        assert np.array_equal(st, st_d)
+        np.testing.assert_allclose(vals, vals_d, rtol=1e-11, atol=1e-20)
+        assert np.all(_rel_rows(gc, gc_d) < 1e-9), _rel_rows(gc, gc_d)
+        assert np.max(np.abs(gp - gp_d) / np.abs(gp_d)) < 1e-8, (gp, gp_d)
+    del tables
+
+
 def test_adjoint_fast_mode_matches_dual_numbers():
     e, params = lattices.learnable_fodo_ring()
     T, n = 20, 300
@@ -175,6 +197,7 @@ def test_adjoint_vs_central_finite_differences():
 
 
 def test_lattice_without_adjoint_is_refused():
+    """6D beam-beam has no adjoint: the backward pass reports it."""
     torch = _torch()
     from sixtracklib_gb300.autodiff import DifferentiableLattice, coordinates
 
