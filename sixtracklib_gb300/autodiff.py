@@ -44,6 +44,55 @@ COORDS = ("x", "px", "y", "py", "zeta", "delta")
 COORD_ROWS = tuple(COL[c] for c in COORDS)
 
 
+def parameter_table(elements: Elements, params) -> dict:
+    """Resolve learnable parameters against a lattice.
+
+    ``params``: ``(element_index, "knl" | "ksl", k)`` or ``(element_index,
+    "voltage")``.  Returns per parameter its element, its kind (the ``bal``
+    index 2k or 2k+1, or -1 for a cavity voltage), the factor from the
+    user's value to the stored one (1/k! for ``knl`` / ``ksl``) and the
+    current value; and the per-element table the adjoint kernel reads:
+    ``begin`` (num_elements + 1 offsets), ``entry_kind`` and ``entry_id``
+    (the parameter each entry belongs to), entries sorted by element."""
+    objs = elements.get_elements()
+    kinds, elems, scales, init = [], [], [], []
+    for p in params:
+        e = int(p[0])
+        if not 0 <= e < len(objs):
+            raise IndexError(f"element index {e} out of range")
+        obj = objs[e]
+        name = p[1]
+        if name in ("knl", "ksl"):
+            if not isinstance(obj, Multipole):
+                raise TypeError(f"element {e} is not a Multipole")
+            k = int(p[2])
+            if not 0 <= k <= int(obj.order):
+                raise ValueError(f"element {e}: order {obj.order} has no {name}[{k}]")
+            kind = 2 * k + (name == "ksl")
+            scale = 1.0 / factorial(k)  # bal[2k] = knl[k] / k!
+            value = float(obj.bal[kind]) / scale
+        elif name == "voltage":
+            if not isinstance(obj, Cavity):
+                raise TypeError(f"element {e} is not a Cavity")
+            kind, scale, value = -1, 1.0, float(obj.voltage)
+        else:
+            raise ValueError(f"unknown parameter {name!r}")
+        elems.append(e)
+        kinds.append(kind)
+        scales.append(scale)
+        init.append(value)
+    el = np.asarray(elems, dtype=np.int64)
+    ki = np.asarray(kinds, dtype=np.int32)
+    n_el = len(objs)
+    order = np.argsort(el, kind="stable")
+    counts = np.bincount(el, minlength=n_el) if len(elems) else np.zeros(n_el, np.int64)
+    begin = np.zeros(n_el + 1, dtype=np.int32)
+    begin[1:] = np.cumsum(counts)
+    return {"element": el, "kind": ki, "scale": np.asarray(scales, dtype=np.float64),
+            "value": np.asarray(init, dtype=np.float64), "begin": begin,
+            "entry_kind": ki[order].astype(np.int32), "entry_id": order.astype(np.int32)}
+
+
 class DifferentiableLattice:
     """A compiled lattice plus the list of its learnable parameters.
 
@@ -52,48 +101,13 @@ class DifferentiableLattice:
     """
 
     def __init__(self, elements: Elements, params, config: str | None = "mode=exact"):
+        self.params = list(params)
+        t = parameter_table(elements, self.params)
+        self._elems, self._kinds, self.scales, self.initial_values = (
+            t["element"], t["kind"], t["scale"], t["value"])
+        self._pbeg, self._pkind, self._pid = t["begin"], t["entry_kind"], t["entry_id"]
         self.tracker = DeviceTracker(elements, config)
         self._lib = _native.load()
-        objs = elements.get_elements()
-        kinds, elems, scales, init = [], [], [], []
-        for p in params:
-            e = int(p[0])
-            if not 0 <= e < len(objs):
-                raise IndexError(f"element index {e} out of range")
-            obj = objs[e]
-            name = p[1]
-            if name in ("knl", "ksl"):
-                if not isinstance(obj, Multipole):
-                    raise TypeError(f"element {e} is not a Multipole")
-                k = int(p[2])
-                if not 0 <= k <= int(obj.order):
-                    raise ValueError(f"element {e}: order {obj.order} has no {name}[{k}]")
-                kind = 2 * k + (name == "ksl")
-                scale = 1.0 / factorial(k)  # bal[2k] = knl[k] / k!
-                value = float(obj.bal[kind]) / scale
-            elif name == "voltage":
-                if not isinstance(obj, Cavity):
-                    raise TypeError(f"element {e} is not a Cavity")
-                kind, scale, value = -1, 1.0, float(obj.voltage)
-            else:
-                raise ValueError(f"unknown parameter {name!r}")
-            elems.append(e)
-            kinds.append(kind)
-            scales.append(scale)
-            init.append(value)
-        self.params = list(params)
-        self._elems = np.asarray(elems, dtype=np.int64)
-        self._kinds = np.asarray(kinds, dtype=np.int32)
-        self.scales = np.asarray(scales, dtype=np.float64)
-        self.initial_values = np.asarray(init, dtype=np.float64)
-        # per-element parameter table for the adjoint kernel
-        E = self.tracker.num_elements
-        order = np.argsort(self._elems, kind="stable")
-        counts = np.bincount(self._elems, minlength=E) if len(elems) else np.zeros(E, np.int64)
-        self._pbeg = np.zeros(E + 1, dtype=np.int32)
-        self._pbeg[1:] = np.cumsum(counts)
-        self._pkind = self._kinds[order].astype(np.int32)
-        self._pid = order.astype(np.int32)
         self._dev_tables = {}
 
     @property

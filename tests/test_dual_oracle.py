@@ -168,3 +168,28 @@ def test_dual_field_kicks_vs_finite_differences(oracle, p0c):
         assert err < 2e-6, (c, err)
     del tables
 
+
+def test_parameter_table():
+    """The per-element table the adjoint kernel reads, and the errors for
+    parameters the lattice does not have."""
+    from sixtracklib_gb300.autodiff import parameter_table
+
+    e, params = lattices.learnable_fodo_ring()
+    extra = [(params[3][0], "ksl", 1), (256, "voltage"), (params[0][0], "knl", 0)]
+    t = parameter_table(e, params + extra)
+    n = len(params) + len(extra)
+    assert t["begin"][-1] == n and t["begin"].size == len(e) + 1
+    assert np.all(np.diff(t["begin"]) >= 0)
+    for el in range(len(e)):
+        ids = t["entry_id"][t["begin"][el]:t["begin"][el + 1]]
+        assert all(t["element"][i] == el for i in ids)
+        assert list(t["entry_kind"][t["begin"][el]:t["begin"][el + 1]]) == [t["kind"][i] for i in ids]
+    assert t["kind"][len(params)] == 3 and t["kind"][len(params) + 1] == -1
+    assert t["value"][len(params) + 1] == 6e6
+    assert t["scale"][params.index(params[-1])] == 0.5  # knl[2]: bal = knl / 2!
+    for bad, exc in (((0, "knl", 1), TypeError), ((1, "knl", 5), ValueError),
+                     ((1, "kn", 1), ValueError), ((999, "voltage"), IndexError),
+                     ((1, "voltage"), TypeError)):
+        with pytest.raises(exc):
+            parameter_table(e, [bad])
+
