@@ -480,8 +480,9 @@ st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *lat, int64_t
  * the entries of element e in d_param_kind (bal index, or -1 for a cavity
  * voltage) and d_param_id (slot of d_grad, every id < num_slots);
  * num_elements + 1 offsets; the range's contribution is added to d_grad.
- * Pass d_param_begin = NULL for coordinate derivatives only.  Lattices with
- * RF multipoles, beam-beam or space-charge elements are refused (-1).
+ * Pass d_param_begin = NULL for coordinate derivatives only.  Every map the
+ * engine tracks has an adjoint; lattices with a map compiled out (TriCub) or
+ * an unknown type id are refused (-1).
  * Asynchronous on `stream`; device pointers except `lat`. */
 st_track_status_t st_DeviceLattice_adjoint_turns(st_DeviceLattice *lat, const void *d_start,
                                                  const void *d_end, int64_t num_particles,

@@ -18,8 +18,8 @@ keeps the coordinates (and their derivatives) it had there.  Supported
 elements: Drift, DriftExact (with the global aperture check after each drift,
 limits 1 m, be_limit/track.h:54-88), Multipole, Cavity, RFMultipole, XYShift,
 SRotation, DipoleEdge, LimitRect, LimitEllipse, LimitRectEllipse,
-BeamBeam4D, SCCoasting, SCQGaussProfile, SCInterpolatedProfile, BeamMonitor
-(no-op).  The Faddeeva function's value comes from the C oracle's cerrf; its
+BeamBeam4D, BeamBeam6D, SCCoasting, SCQGaussProfile, SCInterpolatedProfile,
+BeamMonitor (no-op).  The Faddeeva function's value comes from the C oracle's cerrf; its
 derivative is w'(z) = -2 z w(z) + 2 i / sqrt(pi) at that value.
 """
 
@@ -30,7 +30,7 @@ import numpy as np
 import ctypes as C
 
 from sixtracklib_gb300.beam_elements import (
-    BeamBeam4D, BeamMonitor, Cavity, DipoleEdge, Drift, DriftExact, LimitEllipse, LimitRect,
+    BeamBeam4D, BeamBeam6D, BeamMonitor, Cavity, DipoleEdge, Drift, DriftExact, LimitEllipse, LimitRect,
     LimitRectEllipse, Multipole, RFMultipole, SCCoasting, SCInterpolatedProfile,
     SCQGaussProfile, SRotation, XYShift)
 from sixtracklib_gb300.particles import COL
@@ -333,6 +333,252 @@ def beam_beam_4d(p: DualParticles, d):
     p.py = p.py + (fk * ey - d[9])
 
 
+def _const(val, like: Dual) -> Dual:
+    return Dual(np.broadcast_to(np.asarray(val, dtype=np.float64), like.v.shape).copy(),
+                np.zeros_like(like.d))
+
+
+def _sgn(v):
+    """(a >= 0) - (a < 0) of the value."""
+    return (v >= 0).astype(np.float64) - (v < 0).astype(np.float64)
+
+
+def _sqrt0(a: Dual) -> Dual:
+    """sqrt with derivative 0 where the value is 0: the rotation angle's
+    cos / sin at an uncoupled beam, where the tangent of the argument is 0
+    or rounding noise."""
+    r = np.sqrt(a.v)
+    with np.errstate(divide="ignore"):
+        g = np.where(r > 0, 0.5 / np.where(r > 0, r, 1.0), 0.0)
+    return Dual(r, a.d * g)
+
+
+def _masked(a: Dual, m, fill) -> Dual:
+    return Dual(np.where(m, a.v, fill), np.where(m, a.d, 0.0))
+
+
+def _ell_fields(a: Dual, b: Dual, sa: Dual, sb: Dual):
+    """Elliptic-beam field (E_a, E_b) at |a|, |b| >= 0 for sa > sb
+    (gauss_fields.h:56-208, the two orientations are this with a <-> b)."""
+    S = dsqrt(2. * (sa * sa - sb * sb))
+    fact = 1. / (2. * EPS0 * SQRT_PI * S)
+    eta_re = sb / sa * a
+    eta_im = sa / sb * b
+    wzr, wzi = dcerrf(a / S, b / S)
+    wer, wei = dcerrf(eta_re / S, eta_im / S)
+    e = dexp(-a * a / (2 * sa * sa) - b * b / (2 * sb * sb))
+    return fact * (wzi - wei * e), fact * (wzr - wer * e)
+
+
+def fields_gauss_g(x: Dual, y: Dual, sigma_x: Dual, sigma_y: Dual, min_sigma_diff):
+    """NS(get_Ex_Ey_Gx_Gy_gauss) with the G terms and per-particle beam sizes
+    (be_beamfields/gauss_fields.h:56-208): (Ex, Ey, Gx, Gy).  Every branch is
+    evaluated on all particles (the elliptic ones on masked, harmless
+    arguments) and the particle's own branch is selected."""
+    with np.errstate(all="ignore"):
+        rnd = np.abs(sigma_x.v - sigma_y.v) < min_sigma_diff
+        sigma = 0.5 * (sigma_x + sigma_y)
+        r2 = x * x + y * y
+        t_lin = dsqrt(r2) / (2. * PI * EPS0 * sigma)
+        t_main = (1 - dexp(-0.5 * r2 / (sigma * sigma))) / (2. * PI * EPS0 * r2)
+        t = _where(r2.v < 1e-20, t_lin, t_main)
+        ex_r, ey_r = t * x, t * y
+        eg = dexp(-(x * x + y * y) / (2. * sigma * sigma))
+        c = 1. / (2 * PI * EPS0 * sigma * sigma)
+        gx_r = 1 / (2. * (x * x + y * y)) * (y * ey_r - x * ex_r + c * x * x * eg)
+        gy_r = 1. / (2 * (x * x + y * y)) * (x * ex_r - y * ey_r + c * y * y * eg)
+        abx, aby = dabs(x), dabs(y)
+        gt = ~rnd & (sigma_x.v > sigma_y.v)
+        lt = ~rnd & (sigma_x.v < sigma_y.v)
+        ex_g, ey_g = _ell_fields(_masked(abx, gt, 0.0), _masked(aby, gt, 0.0),
+                                 _masked(sigma_x, gt, 2.0), _masked(sigma_y, gt, 1.0))
+        ey_l, ex_l = _ell_fields(_masked(aby, lt, 0.0), _masked(abx, lt, 0.0),
+                                 _masked(sigma_y, lt, 2.0), _masked(sigma_x, lt, 1.0))
+        ex_e, ey_e = _where(gt, ex_g, ex_l), _where(gt, ey_g, ey_l)
+        ex_e = _where(x.v < 0, -ex_e, ex_e)
+        ey_e = _where(y.v < 0, -ey_e, ey_e)
+        s11, s33 = sigma_x * sigma_x, sigma_y * sigma_y
+        eg = dexp(-x * x / (2 * s11) - y * y / (2 * s33))
+        k = 1. / (2 * PI * EPS0)
+        gx_e = -1. / (2 * (s11 - s33)) * (x * ex_e + y * ey_e + k * (sigma_y / sigma_x * eg - 1.))
+        gy_e = 1. / (2 * (s11 - s33)) * (x * ex_e + y * ey_e + k * (sigma_x / sigma_y * eg - 1.))
+    return (_where(rnd, ex_r, ex_e), _where(rnd, ey_r, ey_e), _where(rnd, gx_r, gx_e),
+            _where(rnd, gy_r, gy_e))
+
+
+def bb6d_sigma(sg, S: Dual, thr):
+    """NS(BeamBeam6D_propagate_Sigma_matrix) (be_beamfields.h:2232-2385) on
+    Duals, branches chosen per particle: (Sig_11_hat, Sig_33_hat, cos theta,
+    sin theta and their derivatives along S)."""
+    S11_0, S12_0, S13_0, S14_0, S22_0, S23_0, S24_0, S33_0, S34_0, S44_0 = [float(v) for v in sg]
+    S11 = S11_0 + 2. * S12_0 * S + S22_0 * S * S
+    S33 = S33_0 + 2. * S34_0 * S + S44_0 * S * S
+    S13 = S13_0 + (S14_0 + S23_0) * S + S24_0 * S * S
+    S12 = S12_0 + S22_0 * S
+    S14 = S14_0 + S24_0 * S
+    S23 = S23_0 + S24_0 * S
+    S34 = S34_0 + S44_0 * S
+    S22, S24, S44 = S22_0, S24_0, S44_0
+    R = S11 - S33
+    Wv = S11 + S33
+    T = R * R + 4 * S13 * S13
+    dS_R = 2. * (S12_0 - S34_0) + 2 * S * (S22_0 - S44_0)
+    dS_W = 2. * (S12_0 + S34_0) + 2 * S * (S22_0 + S44_0)
+    dS_S13 = S14_0 + S23_0 + 2 * S24_0 * S
+    dS_T = 2 * R * dS_R + 8. * S13 * dS_S13
+    signR = _sgn(R.v)
+    zero = _const(0.0, S)
+    with np.errstate(all="ignore"):
+        # T >= thr
+        sqrtT = _sqrt0(T)
+        c2t = signR * R / sqrtT
+        ct_c = _sqrt0(0.5 * (1. + c2t))
+        st_c = signR * _sgn(S13.v) * _sqrt0(0.5 * (1. - c2t))
+        s11_c = 0.5 * (Wv + signR * sqrtT)
+        s33_c = 0.5 * (Wv - signR * sqrtT)
+        dc2t = signR * (dS_R / sqrtT - R / (2 * sqrtT * sqrtT * sqrtT) * dS_T)
+        dct_c = 1. / (4. * ct_c) * dc2t
+        dst_c = _where(np.abs(st_c.v) < thr, (S14 + S23) / R, -1. / (4. * st_c) * dc2t)
+        ds11_c = 0.5 * (dS_W + signR * 0.5 / sqrtT * dS_T)
+        ds33_c = 0.5 * (dS_W - signR * 0.5 / sqrtT * dS_T)
+        # T < thr
+        a = S12 - S34
+        b = S22 - S44
+        c = S14 + S23
+        dd = S24
+        sq = _sqrt0(a * a + c * c)
+        flat = sq.v * sq.v * sq.v < thr
+        # ... with a = c = 0: a fixed rotation
+        c2 = abs(b) / np.sqrt(b * b + 4 * dd * dd) if abs(dd) > thr else 1.
+        ct_a = _const(np.sqrt(0.5 * (1. + c2)), S)
+        st_a = _const(float(_sgn(np.float64(b))) * float(_sgn(np.float64(dd))) *
+                      np.sqrt(0.5 * (1. - c2)), S)
+        # ... otherwise
+        c2t_b = dabs(2. * a) / (2 * sq)
+        ct_b = _sqrt0(0.5 * (1. + c2t_b))
+        sa = _sgn(a.v)
+        st_b = sa * _sgn(c.v) * _sqrt0(0.5 * (1. - c2t_b))
+        dc2t_b = sa * (0.5 * b / sq - a * (a * b + 2. * c * dd) / (2. * sq * sq * sq))
+        dct_b = 1. / (4. * ct_b) * dc2t_b
+        dst_b = _where(np.abs(st_b.v) > thr, -1. / (4. * st_b) * dc2t_b, dd / (2. * a))
+        s_ab = 0.5 * Wv
+        ds11_ab = 0.5 * dS_W
+        ds11_b = 0.5 * dS_W + sa * sq
+        ds33_b = 0.5 * dS_W - sa * sq
+    sing = T.v < thr
+    A, B = sing & flat, sing & ~flat
+
+    def pick(va, vb, vc):
+        return _where(A, va, _where(B, vb, vc))
+
+    return (pick(s_ab, s_ab, s11_c), pick(s_ab, s_ab, s33_c), pick(ct_a, ct_b, ct_c),
+            pick(st_a, st_b, st_c), pick(ds11_ab, ds11_b, ds11_c),
+            pick(ds11_ab, ds33_b, ds33_c), pick(zero, dct_b, dct_c), pick(zero, dst_b, dst_c))
+
+
+def _bb6d_boost(b, x, px, y, py, sg, dl):
+    """NS(BeamBeam6D_boost), be_beamfields.h:2101-2160."""
+    sphi, cphi, tphi, salpha, calpha = b
+    h = dl + 1. - dsqrt((1. + dl) * (1. + dl) - px * px - py * py)
+    px_st = px / cphi - h * calpha * tphi / cphi
+    py_st = py / cphi - h * salpha * tphi / cphi
+    dl_st = dl - px * calpha * tphi - py * salpha * tphi + h * tphi * tphi
+    pz_st = dsqrt((1. + dl_st) * (1. + dl_st) - px_st * px_st - py_st * py_st)
+    hx = px_st / pz_st
+    hy = py_st / pz_st
+    hs = 1. - (dl_st + 1) / pz_st
+    L11 = 1. + hx * calpha * sphi
+    L12 = hx * salpha * sphi
+    L13 = calpha * tphi
+    L21 = hy * calpha * sphi
+    L22 = 1. + hy * salpha * sphi
+    L23 = salpha * tphi
+    L31 = hs * calpha * sphi
+    L32 = hs * salpha * sphi
+    L33 = 1. / cphi
+    return (L11 * x + L12 * y + L13 * sg, px_st, L21 * x + L22 * y + L23 * sg, py_st,
+            L31 * x + L32 * y + L33 * sg, dl_st)
+
+
+def _bb6d_inv_boost(b, x, px, y, py, sg, dl):
+    """NS(BeamBeam6D_inv_boost), be_beamfields.h:2162-2230."""
+    sphi, cphi, tphi, salpha, calpha = b
+    pz = dsqrt((1. + dl) * (1. + dl) - px * px - py * py)
+    hx = px / pz
+    hy = py / pz
+    hs = 1. - (dl + 1) / pz
+    Det = 1. / cphi + (hx * calpha + hy * salpha - hs * sphi) * tphi
+    Li11 = (1. / cphi + salpha * tphi * (hy - hs * salpha * sphi)) / Det
+    Li12 = (salpha * tphi * (hs * calpha * sphi - hx)) / Det
+    Li13 = -tphi * (calpha - hx * salpha * salpha * sphi + hy * calpha * salpha * sphi) / Det
+    Li21 = (calpha * tphi * (-hy + hs * salpha * sphi)) / Det
+    Li22 = (1. / cphi + calpha * tphi * (hx - hs * calpha * sphi)) / Det
+    Li23 = -tphi * (salpha - hy * calpha * calpha * sphi + hx * calpha * salpha * sphi) / Det
+    Li31 = -hs * calpha * sphi / Det
+    Li32 = -hs * salpha * sphi / Det
+    Li33 = (1. + hx * calpha * sphi + hy * salpha * sphi) / Det
+    xi = Li11 * x + Li12 * y + Li13 * sg
+    yi = Li21 * x + Li22 * y + Li23 * sg
+    si = Li31 * x + Li32 * y + Li33 * sg
+    h = (dl + 1. - pz) * cphi * cphi
+    pxi = px * cphi + h * calpha * tphi
+    pyi = py * cphi + h * salpha * tphi
+    dli = dl + pxi * calpha * tphi + pyi * salpha * tphi - h * tphi * tphi
+    return xi, pxi, yi, pyi, si, dli
+
+
+def beam_beam_6d(p: DualParticles, words):
+    """be_beamfields/track.h:342-507 (payload be_beamfields.h:222-250):
+    shift, boost, the strong beam's slices, inverse boost, shift back."""
+    d = np.asarray(words, dtype=np.float64)
+    if not d[33] > 0.:
+        return
+    w = d.view(np.uint64)
+    ns = int(np.int64(w[18]))
+
+    def rel(f):  # relative-offset array of the payload
+        o = int(f + int(w[f]) + 1)
+        return d[o:o + ns]
+
+    n_part, x_sl, y_sl, s_sl = rel(34), rel(35), rel(36), rel(37)
+    b = [float(v) for v in d[1:6]]
+    q0 = QELEM * p.q0
+    P0 = p.p0c / C_LIGHT * QELEM
+    x, px, y, py, sg, dl = _bb6d_boost(
+        b, p.x - d[21] - d[19], p.px - d[22], p.y - d[23] - d[20], p.py - d[24],
+        p.zeta - d[25], p.delta - d[26])
+    for i in range(ns):
+        Ksl = n_part[i] * d[0] * q0 / (P0 * C_LIGHT)
+        S = 0.5 * (sg - s_sl[i])
+        s11h, s33h, ct, st, ds11h, ds33h, dct, dst = bb6d_sigma(d[6:16], S, d[17])
+        xb = x + px * S - x_sl[i]
+        yb = y + py * S - y_sl[i]
+        xbh = xb * ct + yb * st
+        ybh = -xb * st + yb * ct
+        dxbh = xb * dct + yb * dst
+        dybh = -xb * dst + yb * dct
+        ex, ey, gx, gy = fields_gauss_g(xbh, ybh, dsqrt(s11h), dsqrt(s33h), d[16])
+        Fxh = Ksl * ex
+        Fyh = Ksl * ey
+        Gxh = Ksl * gx
+        Gyh = Ksl * gy
+        Fx = Fxh * ct - Fyh * st
+        Fy = Fxh * st + Fyh * ct
+        Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * ds11h + Gyh * ds33h)
+        dl = dl + Fz + 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy))
+        x = x - S * Fx
+        px = px + Fx
+        y = y - S * Fy
+        py = py + Fy
+    x, px, y, py, sg, dl = _bb6d_inv_boost(b, x, px, y, py, sg, dl)
+    p.x = x + d[21] + d[19] - d[27]
+    p.px = px + d[22] - d[28]
+    p.y = y + d[23] + d[20] - d[29]
+    p.py = py + d[24] - d[30]
+    p.zeta = sg + d[25] - d[31]
+    p.set_delta(dl + d[26] - d[32])
+
+
 def sc_coasting(p: DualParticles, o):
     """be_beamfields/track.h:154-198."""
     charge = CHARGE0_SI * p.q0
@@ -541,6 +787,8 @@ def track_until(elements, block: np.ndarray, until_turn: int, params=(), x_limit
                 rf_multipole(p, obj)
             elif isinstance(obj, BeamBeam4D):
                 beam_beam_4d(p, [float(v) for v in np.asarray(obj.data)])
+            elif isinstance(obj, BeamBeam6D):
+                beam_beam_6d(p, np.asarray(obj.data))
             elif isinstance(obj, SCCoasting):
                 sc_coasting(p, obj)
             elif isinstance(obj, SCQGaussProfile):

@@ -10,7 +10,8 @@
 //
 // Every differentiable map here is explicitly invertible (drifts and
 // rotations trivially, thin kicks because they leave x and y unchanged, the
-// cavity because it preserves tau = zeta / (beta0 rvv)).  So the reverse
+// cavity because it preserves tau = zeta / (beta0 rvv), the 6D beam-beam
+// slice by slice).  So the reverse
 // sweep needs no tape: each thread holds one particle's state and adjoint in
 // registers and, for each element, last to first, restores the element's
 // input from its output and applies the transposed Jacobian at that input.
@@ -27,8 +28,8 @@
 // memory and added to the global gradient once per CTA and launch.
 //
 // Apertures contribute no derivative (a loss is a discontinuity).  Lattices
-// with elements that have no adjoint here (RF multipole, beam-beam, space
-// charge, disabled maps) are refused before launch.
+// with elements that have no adjoint (maps compiled out, such as TriCub, and
+// unknown type ids) are refused before launch.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -36,6 +37,7 @@
 #include "common.h"
 #include "kernel_api.h"
 #include "lattice_view.h"
+#include "dual.cuh"
 #include "maps.cuh"
 
 namespace stg {
@@ -43,6 +45,12 @@ namespace stg {
 namespace {
 
 constexpr int kAdjThreads = 128;
+// 3 CTAs per SM: at most 168 registers a thread, which the walk over the
+// ordinary maps needs without spilling; the out-of-line beam-beam and
+// space-charge reverses spill into the stack instead of lowering the
+// occupancy of every lattice's sweep
+constexpr int kAdjBlocksPerSm = 3;
+
 // Parameter sums: per-thread columns in shared memory while they fit
 // (no reduction on the FP64 pipe until the end of the launch), else per-CTA
 // slots fed by warp reductions, else global atomics.
@@ -494,6 +502,92 @@ __device__ __noinline__ RevState reverse_beam_field(RevState r, const uint64_t *
     return r;
 }
 
+// 6D beam-beam (be_beamfields/track.h:342-507), reversed stage by stage
+// from the output: the shifts (identity Jacobian), the inverse boost (its
+// input is the boost of its output), the slices last to first, the boost.
+// Each slice leaves sigma, x + S px and y + S py unchanged, so its kick
+// F(xb, yb, S) is recomputed from the slice's output -- once, on Dual<3>
+// numbers, which also gives dF/d(xb, yb, S) -- and taken back; lambda goes
+// through the slice by the chain rule below.  The map does not read rpp or
+// rvv; they follow the restored delta.
+__device__ __noinline__ RevState reverse_bb6d(RevState r, const uint64_t *rec, int n_slices)
+{
+    RState &s = r.s;
+    Lam &l = r.l;
+    const uint64_t *d = rec + 1;
+    const uint64_t *np_ = d + 34;
+    const uint64_t *xs_ = np_ + n_slices;
+    const uint64_t *ys_ = xs_ + n_slices;
+    const uint64_t *ss_ = ys_ + n_slices;
+    double const q0 = kQelemD * s.q0;
+    double const P0 = s.p0c / kClightD * kQelemD;
+    double x = s.x + W(d[27]) - W(d[19]) - W(d[21]);
+    double px = s.px + W(d[28]) - W(d[22]);
+    double y = s.y + W(d[29]) - W(d[20]) - W(d[23]);
+    double py = s.py + W(d[30]) - W(d[24]);
+    double sg = s.zeta + W(d[31]) - W(d[25]);
+    double dl = s.delta + W(d[32]) - W(d[26]);
+    double lam[6] = {l.x, l.px, l.y, l.py, l.z, l.d};
+    bb6d_boost_t(d + 1, x, px, y, py, sg, dl);  // the inverse boost's input
+    {
+        double const u[6] = {x, px, y, py, sg, dl};
+        bb6d_boost_jt<true>(d + 1, u, lam);
+    }
+    for (int i = n_slices - 1; i >= 0; --i) {
+        double const Ksl = W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
+        double const Sv = 0.5 * (sg - W(ss_[i]));
+        Dual<3> F[3];
+        bb6d_slice_kick_dn(d, Ksl, dseed<3>(x + px * Sv - W(xs_[i]), 0),
+                           dseed<3>(y + py * Sv - W(ys_[i]), 1), dseed<3>(Sv, 2), F);
+        double const Fx = F[0].v, Fy = F[1].v, Fz = F[2].v;
+        // the slice's input: x' = x - S Fx, px' = px + Fx, ...,
+        // delta' = delta + Fz + (Fx (px + Fx / 2) + Fy (py + Fy / 2)) / 2
+        x += Sv * Fx;
+        px -= Fx;
+        y += Sv * Fy;
+        py -= Fy;
+        dl = dl - Fz - 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy));
+        // adjoints of F, then of xb, yb and S, at that input
+        double const lx = lam[0], lpx = lam[1], ly = lam[2], lpy = lam[3], ldl = lam[5];
+        double const lFx = -Sv * lx + lpx + 0.5 * ldl * (px + Fx);
+        double const lFy = -Sv * ly + lpy + 0.5 * ldl * (py + Fy);
+        double const lxb = lFx * F[0].d[0] + lFy * F[1].d[0] + ldl * F[2].d[0];
+        double const lyb = lFx * F[0].d[1] + lFy * F[1].d[1] + ldl * F[2].d[1];
+        double const lS = lFx * F[0].d[2] + lFy * F[1].d[2] + ldl * F[2].d[2] + px * lxb +
+                          py * lyb - Fx * lx - Fy * ly;
+        lam[0] = lx + lxb;
+        lam[1] = lpx + 0.5 * Fx * ldl + Sv * lxb;
+        lam[2] = ly + lyb;
+        lam[3] = lpy + 0.5 * Fy * ldl + Sv * lyb;
+        lam[4] += 0.5 * lS;
+    }
+    bb6d_inv_boost_t(d + 1, x, px, y, py, sg, dl);  // the boost's input
+    {
+        double const u[6] = {x, px, y, py, sg, dl};
+        bb6d_boost_jt<false>(d + 1, u, lam);
+    }
+    l.x = lam[0];
+    l.px = lam[1];
+    l.y = lam[2];
+    l.py = lam[3];
+    l.z = lam[4];
+    l.d = lam[5];
+    s.x = x + W(d[19]) + W(d[21]);
+    s.px = px + W(d[22]);
+    s.y = y + W(d[20]) + W(d[23]);
+    s.py = py + W(d[24]);
+    s.zeta = sg + W(d[25]);
+    s.delta = dl + W(d[26]);
+    // NS(Particles_update_delta_value) (particles.h:5459-5496)
+    double const db0 = s.delta * s.beta0;
+    double const ptb = sqrt(db0 * db0 + 2.0 * db0 * s.beta0 + 1.0) - 1.0;
+    double const opd = 1.0 + s.delta;
+    s.rvv = opd / (1.0 + ptb);
+    s.rpp = 1.0 / opd;
+    set_delta_terms(s, l.z);
+    return r;
+}
+
 // Multipole (be_multipole/track.h:38-112), with the curvature terms only in
 // the CURV instantiation: a runtime branch around them is if-converted, and
 // predicated-off FP64 instructions still occupy the FP64 pipe.
@@ -559,7 +653,10 @@ __device__ __forceinline__ void reverse_multipole(RState &s, Lam &l, const uint6
 
 // Restore the input of one element from its output (state s) and apply
 // lambda <- J^T lambda at that input.  `on` is false for lanes that do not
-// take part (they still join the warp reductions).
+// take part (they still join the warp reductions).  The 6D beam-beam
+// reverse is compiled in only where BB6D is set: its call site alone costs
+// lattices without the element a few percent (registers saved around it).
+template <bool BB6D>
 __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *rec,
                                              const AdjParams &a, int64_t e, bool on)
 {
@@ -649,6 +746,13 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
             l = r.l;
         }
         break;
+    case OP_BB6D:
+        if (BB6D && on) {
+            RevState r = reverse_bb6d(RevState{s, l}, rec, (int)aux);
+            s = r.s;
+            l = r.l;
+        }
+        break;
     case OP_XYSHIFT:  // be_xyshift/track.h:38-55
         if (!on) break;
         s.x -= W(rec[1]);
@@ -681,7 +785,8 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
     }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams a)
+template <bool BB6D>
+__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) adjoint_kernel(AdjParams a)
 {
     int const acc_words = a.acc == ACC_COLUMNS ? a.slots * kAdjThreads
                           : (a.acc == ACC_CTA ? a.slots : 0);
@@ -745,7 +850,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_kernel(AdjParams a)
             wl = v > wl ? v : wl;
         }
         for (int64_t e = (int64_t)wl; e >= 0; --e)
-            reverse_elem(s, l, a.stream + a.elem_offset[e], a, e, act && e <= mine);
+            reverse_elem<BB6D>(s, l, a.stream + a.elem_offset[e], a, e, act && e <= mine);
     }
     if (part) {
         a.lam[0 * n + i] = l.x;
@@ -786,10 +891,10 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
         set_error("adjoint: invalid lattice");
         return -1;
     }
-    uint32_t const no_adjoint = (1u << OP_BB6D) | (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
+    uint32_t const no_adjoint = (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
     if (v.op_mask & no_adjoint) {
         set_error("adjoint: the lattice contains elements without an adjoint "
-                  "(6D beam-beam or a disabled map)");
+                  "(a disabled map or an unknown type)");
         return -1;
     }
     if (turn_end < turn_begin) {
@@ -840,9 +945,13 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
     if (smem > 48 * 1024) {
         static bool attr_set[64] = {};
         if (v.device >= 0 && v.device < 64 && !attr_set[v.device]) {
-            if (cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)((size_t)kMaxColumnSlots * kAdjThreads * 8)) !=
-                cudaSuccess) {
+            int const lim = (int)((size_t)kMaxColumnSlots * kAdjThreads * 8);
+            if (cudaFuncSetAttribute(adjoint_kernel<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(adjoint_kernel<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                    cudaSuccess) {
                 set_error("adjoint: cannot raise the shared-memory limit");
                 return -1;
             }
@@ -850,7 +959,10 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
         }
     }
     unsigned const blocks = (unsigned)((n + kAdjThreads - 1) / kAdjThreads);
-    adjoint_kernel<<<blocks, kAdjThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+    if (v.op_mask & (1u << OP_BB6D))
+        adjoint_kernel<true><<<blocks, kAdjThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
+    else
+        adjoint_kernel<false><<<blocks, kAdjThreads, smem, static_cast<cudaStream_t>(stream)>>>(a);
     rc = (int)cudaGetLastError();
     if (rc != 0) {
         set_error(std::string("adjoint launch: ") + cudaGetErrorString((cudaError_t)rc));

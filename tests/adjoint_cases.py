@@ -84,3 +84,47 @@ def field_ring(seed=5):
                   ksl=[0.0, 2e-4], pn=[10.0, 20.0, 0.0], ps=[5.0, 0.0])
     assert isinstance(QELEM, float)
     return e, params, tables
+
+
+def bb6d_ring(p0c, n_slices=5, sigma_z=0.08):
+    """The FODO ring with three 6D beam-beam elements, one per branch of the
+    strong beam's sigma-matrix propagation and field: a round uncoupled beam
+    (singular branch, round field, crossing angle 1 mrad), a coupled
+    elliptic beam (general branch, sigma_x > sigma_y, 2 mrad in a tilted
+    plane) and an uncoupled elliptic beam with sigma_x < sigma_y (head on);
+    closed orbit, separation and dipolar subtraction are non-zero.  The
+    strong bunch, 1e10 x p0c / 20 GeV protons in equal-charge slices, gives
+    a beam-beam parameter of a few 1e-3 at any energy.  Learnable: two
+    quadrupole strengths and the cavity voltage."""
+    from math import erf, sqrt
+
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.beam_elements import QELEM, bb6d_data
+
+    rng = np.random.default_rng(17)
+    e = lattices.fodo_ring()
+    params = [(1, "knl", 1), (3, "knl", 1), (256, "voltage")]
+    edges = np.linspace(0.0, 1.0, n_slices + 1)
+    z = np.zeros(n_slices)
+    for i in range(n_slices):  # Gaussian quantile of each slice's middle
+        lo, hi, mid = -8.0, 8.0, 0.5 * (edges[i] + edges[i + 1])
+        for _ in range(80):
+            m = 0.5 * (lo + hi)
+            lo, hi = (m, hi) if 0.5 * (1 + erf(m / sqrt(2))) < mid else (lo, m)
+        z[i] = 0.5 * (lo + hi) * sigma_z
+    n_part = np.full(n_slices, 1e10 * p0c / 20e9 / n_slices)
+    A = np.diag([1e-3, 2e-3, 1e-3, 2e-3]) @ (np.eye(4) + 0.3 * rng.normal(size=(4, 4)))
+    sig = A @ A.T
+    coupled = [sig[i, j] for i, j in ((0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3),
+                                      (2, 2), (2, 3), (3, 3))]
+    beams = [((1e-6, 0, 0, 0, 4e-6, 0, 0, 1e-6, 0, 4e-6), 1e-3, 0.2),
+             (tuple(coupled), 2e-3, 1.0),
+             ((0.7e-6, 0.2e-6, 0, 0, 2e-6, 0, 0, 1.3e-6, -0.3e-6, 5e-6), 0.0, 0.0)]
+    for sigmas, phi, alpha in beams:
+        e.BeamBeam6D(data=bb6d_data(
+            q_part=QELEM, phi=phi, alpha=alpha, delta_x=float(rng.normal(0, 1e-4)),
+            delta_y=float(rng.normal(0, 1e-4)), n_part_per_slice=n_part, z_slices=z,
+            sigmas=sigmas, co=(1e-5, 1e-7, -1e-5, 2e-7, 1e-3, 1e-6),
+            d_sub=(1e-6, 1e-8, -1e-6, 2e-8, 1e-4, 1e-7)))
+        e.Drift(length=0.5)
+    return e, params

@@ -124,6 +124,28 @@ def test_field_kick_adjoints_match_dual_numbers(p0c):
     del tables
 
 
+@pytest.mark.parametrize("p0c", [7e12, 20e9])
+def test_beam_beam_6d_adjoint_matches_dual_numbers(p0c):
+    """6D beam-beam: round uncoupled, coupled elliptic and head-on elliptic
+    strong beams with crossing angles, offsets and dipolar subtraction
+    (tests/adjoint_cases.bb6d_ring); gradients of the coordinates and of the
+    ring's strengths within 1e-9 of the dual-number pass, with the
+    reconstruction by inverse maps and by recomputed turns."""
+    from .adjoint_cases import bb6d_ring
+
+    e, params = bb6d_ring(p0c)
+    T, n = 8, 300
+    blk = lattices.gaussian_particles(n, seed=31, sz=0.08, p0c=p0c).block.copy()
+    w = np.random.default_rng(6).normal(size=(6, n)) / SIGMA[:, None]
+    gc_d, gp_d, vals_d, st_d = _dual_grads(e, params, blk, T, w)
+    for reconstruct in ("inverse", "recompute"):
+        gc, gp, vals, st = _gpu_grads(e, params, blk, T, w, every=3, reconstruct=reconstruct)
+        assert np.array_equal(st, st_d)
+        np.testing.assert_allclose(vals, vals_d, rtol=1e-11, atol=1e-20)
+        assert np.all(_rel_rows(gc, gc_d) < 1e-9), _rel_rows(gc, gc_d)
+        assert np.max(np.abs(gp - gp_d) / np.abs(gp_d)) < 1e-8, (gp, gp_d)
+
+
 def test_adjoint_fast_mode_matches_dual_numbers():
     e, params = lattices.learnable_fodo_ring()
     T, n = 20, 300
@@ -197,15 +219,22 @@ def test_adjoint_vs_central_finite_differences():
 
 
 def test_lattice_without_adjoint_is_refused():
-    """6D beam-beam has no adjoint: the backward pass reports it."""
+    """Every map the engine tracks has an adjoint.  A map compiled out of
+    the engine (TriCub, as in the reference's default build) fails the
+    forward tracking, and the adjoint entry point refuses such a lattice
+    before launch."""
     torch = _torch()
     from sixtracklib_gb300.autodiff import DifferentiableLattice, coordinates
+    from sixtracklib_gb300.beam_elements import TYPE_TRICUB
 
-    e = lattices.bb_sc_ring(n_sc=4)
+    e = lattices.fodo_ring()
+    e.cbuffer.add_object(TYPE_TRICUB, np.zeros(3, np.uint64))
     lat = DifferentiableLattice(e, [])
     blk = _beam(64, seed=1, n_lost=0)
     cols = torch.from_numpy(blk.view(np.int64).copy()).cuda()
     coords = coordinates(cols).clone().requires_grad_(True)
-    out, _ = lat.track(coords, torch.zeros(0, dtype=torch.float64, device="cuda"), cols, 2)
+    with pytest.raises(RuntimeError, match="tracking failed"):
+        lat.track(coords, torch.zeros(0, dtype=torch.float64, device="cuda"), cols, 2)
+    lam = torch.ones((6, 64), dtype=torch.float64, device="cuda")
     with pytest.raises(RuntimeError, match="without an adjoint"):
-        out.sum().backward()
+        lat.adjoint_turns(cols, cols.clone(), lam, 0, 1)
