@@ -27,6 +27,13 @@ particle passes counts once (lost particles stop counting where they are lost).
               loss = mean over surviving particles of x^2 + y^2 plus a
               penalty on the lost fraction; forward and backward timed with
               CUDA events; ratio = backward / plain tracking of the same turns.
+  beam_beam_space_charge
+              the beam-beam and space-charge mix: the FODO ring plus 4
+              BeamBeam6D (21 slices), 4 BeamBeam4D and 200 q-Gaussian
+              space-charge kicks, 262,144 Gaussian protons, round and
+              elliptic (sigma_y = 1.3 sigma_x) strong beams; 5 turns timed
+              with CUDA events after 2 warm-up turns, next to the oracle on
+              the host cores on a strided sample of the same particles.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -64,6 +71,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-bbsc", action="store_true")
     ap.add_argument("--batch-variants", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
@@ -392,6 +400,29 @@ def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
     return out
 
 
+def bbsc_bench(args, n=262144, turns=5):
+    """The beam-beam and space-charge mix (see module doc): GPU figures per
+    strong-beam shape, and the oracle on a sample of the same particles."""
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.run_case import bbsc_measure
+
+    gpu = bbsc_measure(n, turns, modes=(args.mode,))
+    out = {"workload": f"FODO ring + 4 BeamBeam6D (21 slices) + 4 BeamBeam4D + 200 "
+                       f"SCQGaussProfile, {n} Gaussian protons, FP64 {args.mode}, "
+                       f"{turns} turns after 2 warm-up turns",
+           "unit": METRIC, "gpu": gpu}
+    if not args.no_cpu:
+        parts = lattices.gaussian_particles(n, seed=3)
+        cpu = {}
+        for g in gpu:
+            ring = lattices.bb_sc_ring(elliptic=g["beams"] != "round")
+            c = cpu_baseline(ring, parts, args.cpu_seconds / 2)
+            cpu[g["beams"]] = c
+            g["vs_cpu"] = g["value"] / c["value"]
+        out["cpu_baseline"] = cpu
+    return out
+
+
 def aggregate_over_ranks(pet, elapsed, device):
     """Whole-job figures of a weak-scaling run: PET summed over ranks, time =
     the slowest rank's (every rank tracks its own particles, no exchange)."""
@@ -576,6 +607,11 @@ def run_ours(args):
             line["adjoint"] = adjoint_measure(dev, args.mode)
         except Exception as exc:  # report, do not hide
             line["adjoint"] = {"error": str(exc)}
+    if not args.no_bbsc:
+        try:
+            line["beam_beam_space_charge"] = bbsc_bench(args)
+        except Exception as exc:  # report, do not hide
+            line["beam_beam_space_charge"] = {"error": str(exc)}
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_measure(ring, parts, max(2, args.steps // 2), 1, args.mode,

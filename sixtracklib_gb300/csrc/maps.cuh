@@ -286,51 +286,76 @@ static __device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec
 
 // ----------------------------------------------------- Gaussian beam fields
 // Complex error function w(z): the CERN algorithm of K. Koelbig (program
-// C335), as used by be_beamfields/faddeeva_cern.h:45-120.  The backward
-// recursion and the series are fused into one loop (the series consumes
-// R[n-1] as soon as the recursion yields it), so no arrays are needed.
+// C335) as be_beamfields/faddeeva_cern.h:45-120 evaluates it -- the same
+// truncated continued fraction and series (same h, nc, nu), evaluated
+// without a division per term.  With U(n) the conjugate of the recursion's
+// R, U(n) = 0.5 / (w0 + n U(n+1)), U(nu + 1) = 0, w0 = (y + 0.5 / h) + i x,
+// is U(n) = 0.5 Q(n+1) / Q(n) for the three-term recurrence
+// Q(n) = w0 Q(n+1) + (n / 2) Q(n+2), Q(nu+1) = 1, Q(nu+2) = 0; the series
+// V(n) = U(n) (V(n+1) + h^(1-n)) then telescopes to
+// V(1) = sum_{m=1..nc} h^(1-m) 0.5^m Q(m+1) / Q(1).  One complex division
+// per call instead of two real divisions per term (|Q| stays below ~1e30);
+// the values agree with the term-by-term evaluation to rounding (a few
+// 1e-15 relative).
 static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
 {
     double const a_const = 1.12837916709551;
     double const xlim = 5.33, ylim = 4.29;
     double const x = fabs(in_re), y = fabs(in_im);
     double wx, wy;
+    double q1r = 1.0, q1i = 0.0, q2r = 0.0, q2i = 0.0;  // Q(n+1), Q(n+2)
     if (y < ylim && x < xlim) {
         double const q = (1.0 - y / ylim) * sqrt(1.0 - (x / xlim) * (x / xlim));
         double const h = 1.0 / (3.2 * q);
         int const nc = 7 + (int)(23.0 * q);
-        double xl = pow(h, (double)(1 - nc));
-        double const xh = y + 0.5 / h;
-        double const yh = x;
         int const nu = 10 + (int)(21.0 * q);
-        double rx = 0.0, ry = 0.0, sx = 0.0, sy = 0.0;
+        double const w0r = y + 0.5 / h, w0i = x;
+        // c = h^(1-n) 0.5^n at n = nc: 0.5 (0.5 / h)^(nc - 1)
+        double c = 0.5, r = 0.5 / h;
+        for (int e = nc - 1; e > 0; e >>= 1) {
+            if (e & 1) c *= r;
+            r *= r;
+        }
+        double const c_step = 2.0 * h;
+        double sr = 0.0, si = 0.0;
         for (int n = nu; n > 0; n--) {
-            double const tx = xh + n * rx;
-            double const ty = yh - n * ry;
-            double const tn = tx * tx + ty * ty;
-            rx = 0.5 * tx / tn;
-            ry = 0.5 * ty / tn;
             if (n <= nc) {
-                double const saux = sx + xl;
-                sx = rx * saux - ry * sy;
-                sy = rx * sy + ry * saux;
-                xl = h * xl;
+                sr = fma(c, q1r, sr);
+                si = fma(c, q1i, si);
+                c *= c_step;
             }
+            double const hn = 0.5 * n;
+            double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
+            double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
+            q2r = q1r;
+            q2i = q1i;
+            q1r = qr;
+            q1i = qi;
         }
-        wx = a_const * sx;
-        wy = a_const * sy;
+        // w = a_const conj(V(1)), V(1) = s / Q(1)
+        double const inv = a_const / fma(q1r, q1r, q1i * q1i);
+        wx = fma(sr, q1r, si * q1i) * inv;
+        wy = fma(sr, q1i, -si * q1r) * inv;
     } else {
-        double const xh = y, yh = x;
-        double rx = 0.0, ry = 0.0;
+        // |w0| is unbounded here: Q(n) = s^(10-n) Q'(n) with s a power of two
+        // near |w0| (exact scaling), Q'(n) = (w0 / s) Q'(n+1) + (n / 2 s^2) Q'(n+2)
+        int ex;
+        frexp(fmax(x, y), &ex);
+        double const is = ldexp(1.0, -ex);
+        double const w0r = y * is, w0i = x * is;
         for (int n = 9; n > 0; n--) {
-            double const tx = xh + n * rx;
-            double const ty = yh - n * ry;
-            double const tn = tx * tx + ty * ty;
-            rx = 0.5 * tx / tn;
-            ry = 0.5 * ty / tn;
+            double const hn = 0.5 * n * is * is;
+            double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
+            double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
+            q2r = q1r;
+            q2i = q1i;
+            q1r = qr;
+            q1i = qi;
         }
-        wx = a_const * rx;
-        wy = a_const * ry;
+        // w = a_const conj(U(1)), U(1) = 0.5 Q(2) / Q(1) = 0.5 Q'(2) / (s Q'(1))
+        double const inv = 0.5 * a_const * is / fma(q1r, q1r, q1i * q1i);
+        wx = fma(q2r, q1r, q2i * q1i) * inv;
+        wy = fma(q2r, q1i, -q2i * q1r) * inv;
     }
     if (y == 0.) wx = exp(-x * x);
     if (in_im < 0.) {

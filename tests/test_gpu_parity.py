@@ -251,6 +251,47 @@ def test_beam_beam_space_charge_ring(torch_cuda, oracle, elliptic):
             assert_parity(got, exp, tol=tol)
 
 
+@pytest.mark.parametrize("sigmas", [(2e-3, 1e-3), (1e-3, 2.5e-3), (1.5e-3, 1.5e-3)])
+def test_gaussian_field_kicks(torch_cuda, oracle, sigmas):
+    """The Gaussian field itself, one 4D beam-beam element with a strong
+    beam: particles at rest in px, py on a grid out to 40 sigma (both
+    branches of the Faddeeva function, the round formula for equal sizes),
+    so px, py after the element are the kicks.  The device evaluates the
+    CERN algorithm's truncated continued fraction and series in a
+    division-free form whose values differ from the reference's
+    term-by-term loop by rounding (<= 3.2e-15 relative).  Near the centre
+    the field is the difference of two nearly equal Faddeeva terms, which
+    amplifies any rounding difference by ~1 / r; so each kick must agree
+    within 1e-13 of its magnitude, or of a tenth of the largest kick where
+    it is smaller (inside ~0.2 sigma)."""
+    sx, sy = sigmas
+    e = Elements()
+    e.BeamBeam4D(charge=1e13, sigma_x=sx, sigma_y=sy, beta_r=1.0, min_sigma_diff=1e-10,
+                 x_bb=0.0, y_bb=0.0, d_px=0.0, d_py=0.0, enabled=1.0)
+    lat = e.cbuffer.to_image()
+    r = np.concatenate([np.linspace(0.01, 6.0, 24), np.geomspace(6.0, 40.0, 8)])
+    ang = np.linspace(0.0, 2 * np.pi, 17)[:-1] + 0.1
+    xs = (r[:, None] * np.cos(ang)[None, :] * sx).ravel()
+    ys = (r[:, None] * np.sin(ang)[None, :] * sy).ravel()
+    p = lattices.gaussian_particles(xs.size, seed=2)
+    p.x[:] = xs
+    p.y[:] = ys
+    p.px[:] = 0.0
+    p.py[:] = 0.0
+    exp = p.block.copy()
+    assert oracle.track_until(lat, exp, 1) == 0
+    f = exp.view(np.float64)
+    kick = np.hypot(f[8], f[9])
+    assert kick.min() > 0
+    scale = np.maximum(kick, 0.1 * kick.max())
+    for mode in ("exact", "fast"):
+        st, got = run_device(torch_cuda, lat, p.block, until=1, mode=mode)
+        assert st == 0
+        g = got.view(np.float64)
+        err = np.hypot(g[8] - f[8], g[9] - f[9]) / scale
+        assert err.max() < 1e-13, (mode, float(err.max()))
+
+
 def test_interpolated_space_charge(torch_cuda, oracle):
     """SCInterpolatedProfile (linear / cubic / disabled tables and the
     fallback density): 1e-13 after one turn, 1e-10 after 20."""
