@@ -73,7 +73,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for f in HOST_SOURCES:
         o = os.path.join(OBJ_DIR, f + ".o")
         objs.append(o)
-        jobs.append(["g++", "-std=c++17", "-fPIC", "-Wall", *common, "-c",
+        # no FMA contraction: the lattice compiler's element constants are the
+        # reference's expressions, rounded as it rounds them
+        jobs.append(["g++", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", *common, "-c",
                      os.path.join(CSRC, f), "-o", o])
     for f, extra in CUDA_SOURCES.items():
         o = os.path.join(OBJ_DIR, f + ".o")

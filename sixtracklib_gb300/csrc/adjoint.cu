@@ -748,7 +748,7 @@ __device__ __forceinline__ void reverse_elem(RState &s, Lam &l, const uint64_t *
         break;
     case OP_BB6D:
         if (BB6D && on) {
-            RevState r = reverse_bb6d(RevState{s, l}, rec, (int)aux);
+            RevState r = reverse_bb6d(RevState{s, l}, rec, (int)(aux & BB6D_SLICES));
             s = r.s;
             l = r.l;
         }

@@ -171,6 +171,14 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             if (ns < 0 || ns > 100000) return bad(err, i, "beam-beam 6d slice count out of range");
             op = OP_BB6D;
             aux = (uint32_t)ns;
+            {
+                auto f = [&](int k) { return w2d(bd[k]); };  // Sigma at words 6-15
+                bool finite = true;
+                for (int k = 6; k < 18; ++k) finite = finite && std::isfinite(f(k));
+                if (finite && f(6) == f(13) && f(7) == f(14) && f(10) == f(15) && f(8) == 0.0 &&
+                    f(9) == 0.0 && f(11) == 0.0 && f(12) == 0.0 && f(16) > 0.0 && f(17) > 0.0)
+                    aux |= BB6D_ROUND;
+            }
             p.assign(bd, bd + 34);
             for (int f = 34; f < 38; ++f) {
                 uint64_t const off = (uint64_t)f + bd[f] + 1;
@@ -188,6 +196,16 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             if (!need(11)) return bad(err, i, "truncated space-charge q-gaussian");
             op = OP_SC_QGAUSS;
             p.assign(w, w + 11);
+            {
+                // element constants of the kick, as track.h:203-268 and
+                // NS(Math_q_gauss) compute them for every particle
+                double const sqrt_beta = 1.0 / (std::sqrt(2.0) * w2d(w[1]));
+                double const omq = 1.0 - w2d(w[8]);
+                double const abs_omq = (omq >= 0.0) ? omq : -omq;
+                for (double v : {sqrt_beta, sqrt_beta * sqrt_beta, sqrt_beta / w2d(w[9]),
+                                 abs_omq >= 1e-6 ? 1.0 / omq : 0.0})
+                    p.push_back(d2w(v));
+            }
             break;
         case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {
             // be_beamfields/track.h:273-337.  interpol_data_addr (field 6)

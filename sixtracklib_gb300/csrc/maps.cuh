@@ -546,8 +546,34 @@ static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, dou
     out[7] = dst;
 }
 
+// The round field of NS(get_Ex_Ey_Gx_Gy_gauss) with the G terms
+// (gauss_fields.h:56-208) for sigma_x = sigma_y = sigma.  The reference's
+// second exponential, exp(-(x^2 + y^2) / (2 sigma^2)), is the same number as
+// the first, exp(-0.5 r2 / sigma^2) (both arguments are r2 / sigma^2 scaled
+// by -1/2 exactly), so it is evaluated once.
+__device__ __forceinline__ void fields_round_g(double x, double y, double sigma, double *ex,
+                                               double *ey, double *gx, double *gy)
+{
+    double const r2 = x * x + y * y;
+    double const e = exp(-0.5 * r2 / (sigma * sigma));
+    double const t = (r2 < 1e-20) ? sqrt(r2) / (2. * kPiD * kEps0D * sigma)
+                                  : (1 - e) / (2. * kPiD * kEps0D * r2);
+    double const exv = t * x, eyv = t * y;
+    double const c = 1. / (2 * kPiD * kEps0D * sigma * sigma);
+    double const h = 1 / (2. * r2);
+    *ex = exv;
+    *ey = eyv;
+    *gx = h * (y * eyv - x * exv + c * x * x * e);
+    *gy = h * (x * exv - y * eyv + c * y * y * e);
+}
+
 // be_beamfields/track.h:342-507 with NS(BeamBeam6D_boost / inv_boost)
-// (be_beamfields.h:2101-2230); rec = [hdr, 34 head words, slices...]
+// (be_beamfields.h:2101-2230); rec = [hdr, 34 head words, slices...].
+// ROUND: the strong beam is round and uncoupled (BB6D_ROUND): the Sigma
+// propagation's singular branch reduces to Sig_11_hat = Sig_33_hat = W / 2,
+// cos theta = 1, sin theta = 0, no theta derivative, and the field is the
+// round one -- the same values as the general code for such a beam.
+template <bool ROUND>
 static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n_slices)
 {
     const uint64_t *d = rec + 1;
@@ -598,21 +624,38 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
     for (int i = 0; i < n_slices; ++i) {
         double const Ksl = W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
         double const S = 0.5 * (sg - W(ss_[i]));
-        double sm[8];
-        bb6d_sigma(d + 6, S, thr, sm);
-        double const ct = sm[2], st = sm[3];
         double const xb = x + px * S - W(xs_[i]);
         double const yb = y + py * S - W(ys_[i]);
-        double const xbh = xb * ct + yb * st;
-        double const ybh = -xb * st + yb * ct;
-        double const dxbh = xb * sm[6] + yb * sm[7];
-        double const dybh = -xb * sm[7] + yb * sm[6];
-        double ex, ey, gx = 0.0, gy = 0.0;
-        fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
-        double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
-        double const Fx = Fxh * ct - Fyh * st;
-        double const Fy = Fxh * st + Fyh * ct;
-        double const Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * sm[4] + Gyh * sm[5]);
+        double Fx, Fy, Fz;
+        if (ROUND) {
+            const uint64_t *sgm = d + 6;  // S11 S12 S13 S14 S22 S23 S24 S33 S34 S44
+            double const S11_0 = W(sgm[0]), S12_0 = W(sgm[1]), S22_0 = W(sgm[4]);
+            double const S33_0 = W(sgm[7]), S34_0 = W(sgm[8]), S44_0 = W(sgm[9]);
+            double const S11 = S11_0 + 2. * S12_0 * S + S22_0 * S * S;
+            double const S33 = S33_0 + 2. * S34_0 * S + S44_0 * S * S;
+            double const dS_W = 2. * (S12_0 + S34_0) + 2 * S * (S22_0 + S44_0);
+            double const s_hat = 0.5 * (S11 + S33);
+            double const ds_hat = 0.5 * dS_W;
+            double ex, ey, gx, gy;
+            fields_round_g(xb, yb, sqrt(s_hat), &ex, &ey, &gx, &gy);
+            Fx = Ksl * ex;
+            Fy = Ksl * ey;
+            Fz = 0.5 * (Ksl * gx * ds_hat + Ksl * gy * ds_hat);
+        } else {
+            double sm[8];
+            bb6d_sigma(d + 6, S, thr, sm);
+            double const ct = sm[2], st = sm[3];
+            double const xbh = xb * ct + yb * st;
+            double const ybh = -xb * st + yb * ct;
+            double const dxbh = xb * sm[6] + yb * sm[7];
+            double const dybh = -xb * sm[7] + yb * sm[6];
+            double ex, ey, gx = 0.0, gy = 0.0;
+            fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
+            double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
+            Fx = Fxh * ct - Fyh * st;
+            Fy = Fxh * st + Fyh * ct;
+            Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * sm[4] + Gyh * sm[5]);
+        }
         dl = dl + Fz + 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy));
         x = x - S * Fx;
         px = px + Fx;
@@ -687,20 +730,21 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
     double const z = p.zeta / p.rvv;
     double fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
     fk *= W(c[0]);
-    double const sqrt_beta = 1.0 / (sqrt(2.0) * W(c[1]));
+    // c[11..14]: sqrt_beta = 1 / (sqrt(2) bunchlength_rms), sqrt_beta^2,
+    // sqrt_beta / cq, 1 / (1 - q), computed by the lattice compiler
     double const q = W(c[8]);
-    double const arg = -(sqrt_beta * sqrt_beta * z * z);
+    double const arg = -(W(c[12]) * z * z);
     double const omq = 1.0 - q;
     double const abs_omq = (omq >= 0.0) ? omq : -omq;
     double e;
     if (abs_omq >= 1e-6) {
         double u = 1.0 + omq * arg;
         if (u < 0.0) u = 0.0;
-        e = pow(u, 1.0 / omq);
+        e = pow(u, W(c[14]));
     } else {
         e = exp(arg);
     }
-    fk *= (sqrt_beta / W(c[9])) * e;
+    fk *= W(c[13]) * e;
     fk /= pc0 * beta;
     double ex, ey, gx, gy;
     fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);

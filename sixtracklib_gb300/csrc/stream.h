@@ -28,9 +28,12 @@ enum Op : uint32_t {
     OP_DIPEDGE = 11,        // [r21, r43]
     OP_RF_MULTIPOLE = 12,   // [voltage, frequency, lag, bal..., phase...] aux = order
     OP_BB4D = 13,           // [11 BB4D data words]
-    OP_BB6D = 14,           // [34 head words, n_part[N], x[N], y[N], sigma[N]] aux = N
+    OP_BB6D = 14,           // [34 head words, n_part[N], x[N], y[N], sigma[N]]
+                            // aux = N | BB6D_ROUND
     OP_SC_COASTING = 15,    // [9 SCCoasting words]
-    OP_SC_QGAUSS = 16,      // [11 SCQGaussProfile words]
+    OP_SC_QGAUSS = 16,      // [11 SCQGaussProfile words, sqrt_beta = 1 / (sqrt(2)
+                            //  bunchlength_rms), sqrt_beta^2, sqrt_beta / cq,
+                            //  1 / (1 - q) (0 when |1 - q| < 1e-6)]
     OP_MONITOR = 17,        // [num_stores, start, skip, max_pid, min_pid, rolling,
                             //  turn_ordered, out_ptr, out_capacity]
     OP_NOP = 18,            // success, no effect (disabled beam-beam)
@@ -44,6 +47,14 @@ enum Op : uint32_t {
 };
 
 constexpr uint32_t DRIFT_APERTURE = 1u;
+// BB6D aux flag: the strong beam's Sigma matrix is round and uncoupled
+// (S11 = S33, S12 = S34, S22 = S44, S13 = S14 = S23 = S24 = 0) with
+// threshold_singular > 0 and min_sigma_diff > 0.  Then R = S13 = 0 at every
+// S, and NS(BeamBeam6D_propagate_Sigma_matrix) always takes its singular
+// branch with cos theta = 1, sin theta = 0 and no theta derivative, and the
+// field is the round one: the map computes only what that branch needs.
+constexpr uint32_t BB6D_ROUND = 1u << 31;
+constexpr uint32_t BB6D_SLICES = BB6D_ROUND - 1u;
 
 inline uint64_t make_header(uint32_t op, uint32_t nwords, uint32_t aux)
 {

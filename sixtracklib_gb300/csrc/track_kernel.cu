@@ -233,7 +233,10 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         p = beam_beam_4d(p, rec);
         return 0;
     case OP_BB6D:
-        p = beam_beam_6d(p, rec, (int)aux);
+        if (aux & BB6D_ROUND)
+            p = beam_beam_6d<true>(p, rec, (int)(aux & BB6D_SLICES));
+        else
+            p = beam_beam_6d<false>(p, rec, (int)aux);
         return 0;
     case OP_SC_COASTING:
         p = sc_coasting(p, rec);

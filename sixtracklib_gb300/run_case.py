@@ -8,6 +8,12 @@
         one batched call over lattice variants of 500-4000 elements with
         1024-32768 particles each, checked bit for bit against per-lattice
         tracking;
+    python -m sixtracklib_gb300.run_case elements <particles>
+        one turn (fast arithmetic) of each of: the FODO ring, and the FODO
+        ring plus 200 round / 200 elliptic q-Gaussian space-charge kicks,
+        50 round 4D beam-beam kicks, 4 round / 4 elliptic 6D beam-beam
+        elements of 21 slices -- under a profiler's instruction counters,
+        the differences to the plain ring give each element's cost;
     python -m sixtracklib_gb300.run_case bbsc <particles> <turns>
         the beam-beam and space-charge mix (FODO ring + 4 BeamBeam6D of 21
         slices + 4 BeamBeam4D + 200 q-Gaussian space-charge kicks), round
@@ -110,6 +116,70 @@ def bbsc_measure(n: int, turns: int, modes=("fast", "exact")) -> list:
     return out
 
 
+def element_cost_lattices() -> dict:
+    """The FODO ring with one kind of beam-field element added (see the
+    module doc); strong beams of 16.7 um (beam-beam) and 1 mm (space
+    charge), as in lattices.bb_sc_ring."""
+    from math import erf, sqrt
+
+    from . import lattices
+    from .beam_elements import QELEM, bb6d_data
+
+    def sc(ell):
+        e = lattices.fodo_ring()
+        for _ in range(200):
+            e.SCQGaussProfile(number_of_particles=1e11, bunchlength_rms=0.1, sigma_x=1e-3,
+                              sigma_y=1.2e-3 if ell else 1e-3, length=1.0, x_co=0.0, y_co=0.0,
+                              min_sigma_diff=1e-10, q_param=1.0, enabled=1)
+        return e
+
+    def bb4d():
+        e = lattices.fodo_ring()
+        for _ in range(50):
+            e.BeamBeam4D(charge=1.15e11, sigma_x=16.7e-6, sigma_y=16.7e-6, beta_r=1.0,
+                         min_sigma_diff=1e-10, x_bb=1e-6, y_bb=-1e-6, d_px=0.0, d_py=0.0,
+                         enabled=1.0)
+        return e
+
+    def bb6d(ell, ns=21, sz=0.0755):
+        edges = np.linspace(0.0, 1.0, ns + 1)
+        z = np.zeros(ns)
+        for i in range(ns):  # equal-charge slices of a Gaussian bunch
+            lo, hi, mid = -8.0, 8.0, 0.5 * (edges[i] + edges[i + 1])
+            for _ in range(80):
+                m = 0.5 * (lo + hi)
+                lo, hi = (m, hi) if 0.5 * (1 + erf(m / sqrt(2))) < mid else (lo, m)
+            z[i] = 0.5 * (lo + hi) * sz
+        sx = 16.7e-6
+        sy = sx * (1.3 if ell else 1.0)
+        e = lattices.fodo_ring()
+        for _ in range(4):
+            e.BeamBeam6D(data=bb6d_data(
+                q_part=QELEM, phi=1.5e-4, alpha=0.3, delta_x=1e-6, delta_y=-1e-6,
+                n_part_per_slice=np.full(ns, 1.15e11 / ns), z_slices=z,
+                sigmas=(sx * sx, 0, 0, 0, 1e-12, 0, 0, sy * sy, 0, 1e-12)))
+        return e
+
+    return {"fodo": lattices.fodo_ring(), "sc_round": sc(False), "bb4d_round": bb4d(),
+            "bb6d_round": bb6d(False), "sc_elliptic": sc(True), "bb6d_elliptic": bb6d(True)}
+
+
+def elements(n: int) -> None:
+    import torch
+
+    from . import lattices
+    from .device import DeviceTracker
+
+    block = lattices.gaussian_particles(n, seed=3).block
+    for name, ring in element_cost_lattices().items():
+        trk = DeviceTracker(ring, config="mode=fast")
+        cols = torch.from_numpy(block.copy().view(np.int64)).cuda()
+        if trk.track_until(cols, 1) != 0:
+            raise SystemExit(f"elements: tracking {name} failed")
+        torch.cuda.synchronize()
+        print(f"elements {name:<14} {len(ring)} elements, {int((cols[20] == 1).sum())} alive")
+
+
 def bbsc(n: int, turns: int) -> None:
     for r in bbsc_measure(n, turns):
         print(f"bbsc {r['beams']:<33} {r['mode']:<5} {r['particles']} particles: "
@@ -121,6 +191,8 @@ def main(argv) -> None:
         adjoint(int(argv[1]), int(argv[2]), argv[3])
     elif len(argv) >= 1 and argv[0] == "batch":
         batch(int(argv[1]), int(argv[2]))
+    elif len(argv) >= 1 and argv[0] == "elements":
+        elements(int(argv[1]))
     elif len(argv) >= 1 and argv[0] == "bbsc":
         bbsc(int(argv[1]), int(argv[2]))
     else:
