@@ -17,6 +17,9 @@ import numpy as np
 from .cbuffer import CBuffer, CObject
 
 QELEM = 1.60217662e-19  # sixtracklib/common/constants.h:35
+# q_part of beam-beam elements built from named parameters: the reference's
+# Python binding uses scipy.constants.e there (beam_elements.py:11, :490, :508)
+Q_PART_NAMED = 1.602176634e-19
 
 TYPE_DRIFT = 2
 TYPE_DRIFT_EXACT = 3
@@ -101,6 +104,17 @@ class _Element:
     def _array_len(self, expr):
         return int(eval(expr, {}, dict(self.__dict__)))
 
+    def _set_array_entry(self, name, i, value):
+        """array field ``name``[i] = value, here and in the lattice buffer
+        the element belongs to (the reference's elements are views of their
+        buffer, so its setters write the buffer in place)."""
+        getattr(self, name)[i] = value
+        if self._cbuffer is not None and self._index is not None:
+            fi = [f for f, _ in self._fields].index(name)
+            obj = self._cbuffer.objects[self._index]
+            obj.words[int(obj.words[fi]) + i] = np.float64(value).view(np.uint64)
+            self._cbuffer.touch()
+
     def to_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields}
 
@@ -135,7 +149,29 @@ def _knl_ksl_to_bal(order, knl, ksl):
     return n - 1, bal
 
 
-class Multipole(_Element):
+class _BalAccess:
+    """knl / ksl of ``bal`` (bal[2k] = knl[k] / k!, bal[2k+1] = ksl[k] / k!)
+    and their in-place setters (python/sixtracklib/beam_elements.py:112-128,
+    :232-248)."""
+
+    @property
+    def knl(self):
+        return np.array([self.bal[2 * k] * factorial(k) for k in range(self.order + 1)])
+
+    @property
+    def ksl(self):
+        return np.array([self.bal[2 * k + 1] * factorial(k) for k in range(self.order + 1)])
+
+    def set_knl(self, value, order):
+        assert order <= self.order
+        self._set_array_entry("bal", 2 * order, float(np.squeeze(value)) / factorial(order))
+
+    def set_ksl(self, value, order):
+        assert order <= self.order
+        self._set_array_entry("bal", 2 * order + 1, float(np.squeeze(value)) / factorial(order))
+
+
+class Multipole(_BalAccess, _Element):
     """Thin multipole; ``bal[2k] = knl[k]/k!``, ``bal[2k+1] = ksl[k]/k!``
     (be_multipole.h:449-466)."""
 
@@ -156,16 +192,8 @@ class Multipole(_Element):
             order = (len(bal) - 2) // 2
         super().__init__(cbuffer=cbuffer, order=order, bal=bal, **kw)
 
-    @property
-    def knl(self):
-        return np.array([self.bal[2 * k] * factorial(k) for k in range(self.order + 1)])
 
-    @property
-    def ksl(self):
-        return np.array([self.bal[2 * k + 1] * factorial(k) for k in range(self.order + 1)])
-
-
-class RFMultipole(_Element):
+class RFMultipole(_BalAccess, _Element):
     _typeid = TYPE_RF_MULTIPOLE
     _fields = (
         ("order", "i"),
@@ -179,18 +207,35 @@ class RFMultipole(_Element):
     def __init__(self, order=None, knl=None, ksl=None, pn=None, ps=None, bal=None,
                  p=None, cbuffer=None, **kw):
         if bal is None:
-            lens = [len(a) for a in (knl or [], ksl or [], pn or [], ps or [])]
-            n = max([(order or 0) + 1] + lens)
+            knl, ksl, pn, ps = ([] if a is None else list(np.atleast_1d(a))
+                                for a in (knl, ksl, pn, ps))
+            n = max([(order or 0) + 1] + [len(a) for a in (knl, ksl, pn, ps)])
             order, bal = _knl_ksl_to_bal(n - 1, knl, ksl)
             ph = np.zeros(2 * n)
-            ph[0::2][: len(pn or [])] = pn or []
-            ph[1::2][: len(ps or [])] = ps or []
+            ph[0::2][: len(pn)] = pn
+            ph[1::2][: len(ps)] = ps
         else:
             bal = np.asarray(bal, dtype=np.float64)
             ph = np.asarray(p if p is not None else kw.pop("phase"), dtype=np.float64)
             order = (len(bal) - 2) // 2
         kw.pop("phase", None)
         super().__init__(cbuffer=cbuffer, order=order, bal=bal, phase=ph, **kw)
+
+    @property
+    def pn(self):
+        return np.asarray(self.phase)[0::2].copy()
+
+    @property
+    def ps(self):
+        return np.asarray(self.phase)[1::2].copy()
+
+    def set_pn(self, value, order):
+        assert order <= self.order
+        self._set_array_entry("phase", 2 * order, float(np.squeeze(value)))
+
+    def set_ps(self, value, order):
+        assert order <= self.order
+        self._set_array_entry("phase", 2 * order + 1, float(np.squeeze(value)))
 
 
 class Cavity(_Element):
@@ -325,15 +370,38 @@ class BeamBeam4D(_DataElement):
         if data is None and "x_bb" in kw:
             keys = ("charge", "sigma_x", "sigma_y", "beta_r", "min_sigma_diff",
                     "x_bb", "y_bb", "d_px", "d_py", "enabled")
-            data = [QELEM] + [float(kw.pop(k)) for k in keys]
+            data = [Q_PART_NAMED] + [float(kw.pop(k)) for k in keys]
         super().__init__(data=data, cbuffer=cbuffer, **kw)
 
 
 class BeamBeam6D(_DataElement):
     """6D synchro-beam; payload = the BB6D data block
-    (be_beamfields.h:222-250), see :func:`bb6d_data`."""
+    (be_beamfields.h:222-250), see :func:`bb6d_data`.
+
+    Like the reference (beam_elements.py:496-543) it also takes the strong
+    beam's parameters by name, as a pysixtrack ``BeamBeam6D`` lists them --
+    ``phi``, ``alpha``, ``x_bb_co``, ``y_bb_co``, ``charge_slices``,
+    ``zeta_slices``, ``sigma_11`` .. ``sigma_44``, ``x_co`` .. ``delta_co``,
+    ``min_sigma_diff``, ``threshold_singular``, ``d_x`` .. ``d_delta``,
+    ``enabled`` -- and builds the payload with :func:`bb6d_data` (the
+    reference calls pysixtrack's initialisation there)."""
 
     _typeid = TYPE_BEAM_BEAM_6D
+
+    def __init__(self, data=None, cbuffer=None, **kw):
+        if data is None and "x_bb_co" in kw:
+            sig = [kw[f"sigma_{ij}"] for ij in ("11", "12", "13", "14", "22", "23", "24",
+                                                "33", "34", "44")]
+            data = bb6d_data(
+                q_part=Q_PART_NAMED, phi=kw["phi"], alpha=kw["alpha"], delta_x=kw["x_bb_co"],
+                delta_y=kw["y_bb_co"], n_part_per_slice=kw["charge_slices"],
+                z_slices=kw["zeta_slices"], sigmas=sig,
+                co=[kw[k] for k in ("x_co", "px_co", "y_co", "py_co", "zeta_co", "delta_co")],
+                min_sigma_diff=kw["min_sigma_diff"],
+                threshold_singular=kw["threshold_singular"],
+                d_sub=[kw[k] for k in ("d_x", "d_px", "d_y", "d_py", "d_zeta", "d_delta")],
+                enabled=kw["enabled"])
+        super().__init__(data=data, cbuffer=cbuffer, **kw)
 
 
 class SCCoasting(_Element):
@@ -556,12 +624,20 @@ class Elements:
 
     element_types = {cls.__name__: cls for cls in ELEMENT_TYPES.values()}
 
+    @staticmethod
+    def add_element_type(cls, cls_name):
+        """Register an element class under ``cls_name`` for Elements made
+        from now on (beam_elements.py:732-734)."""
+        Elements.element_types.update({cls_name: cls})
+
     def __init__(self, cbuffer=None):
         self.cbuffer = CBuffer() if cbuffer is None else cbuffer
         for tid, cls in ELEMENT_TYPES.items():
             self.cbuffer.typeids[tid] = cls
         for name, cls in self.element_types.items():
             setattr(self, name, self._mk(cls))
+            self.cbuffer.typeids.setdefault(cls._typeid, cls)
+        self._builder = self.gen_builder()
 
     def _mk(self, cls):
         def fun(*args, **kw):
@@ -569,9 +645,39 @@ class Elements:
 
         return fun
 
+    def gen_builder(self):
+        """``{class name: function appending such an element}``."""
+        return {name: getattr(self, name) for name in self.element_types}
+
     @classmethod
     def fromfile(cls, filename):
         return cls(cbuffer=CBuffer.fromfile(filename))
+
+    @classmethod
+    def from_line(cls, line):
+        """A lattice from a pysixtrack-style line (beam_elements.py:748-757):
+        ``line.elements``, each with ``to_dict(keepextra=True)``; the class
+        name selects the element type."""
+        return cls().append_line(line)
+
+    def append_line(self, line):
+        for element in line.elements:
+            getattr(self, element.__class__.__name__)(**element.to_dict(keepextra=True))
+        return self
+
+    @classmethod
+    def from_mad(cls, seq, exact_drift=False):
+        """A lattice from a thin MAD-X sequence (beam_elements.py:786-795;
+        conversion rules in :mod:`sixtracklib_gb300.mad_helper`);
+        ``exact_drift`` makes the drifts DriftExact."""
+        from .mad_helper import madseq_to_generator
+
+        self = cls()
+        for _label, name, element in madseq_to_generator(seq):
+            if exact_drift and name == "Drift":
+                name = "DriftExact"
+            getattr(self, name)(**element._asdict())
+        return self
 
     def to_file(self, filename):
         self.cbuffer.tofile(filename)
