@@ -3,6 +3,7 @@
 from .cbuffer import CBuffer, CObject
 from .beam_elements import *  # noqa: F401,F403
 from .beam_elements import Elements
-from .particles import Particles, ParticlesSet
+from .particles import (Particles, ParticlesSet, calcParticlesDifference,  # noqa: F401
+                        compareParticlesDifference, makeCopy)
 
 __version__ = "0.1.0"

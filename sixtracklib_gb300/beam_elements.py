@@ -596,6 +596,44 @@ SpaceChargeCoasting = SCCoasting
 SpaceChargeQGaussianProfile = SCQGaussProfile
 SpaceChargeBunched = SCQGaussProfile
 
+class TriCubData(_Element):
+    """Tricubic interpolation table (python/sixtracklib/tricub.py:21-49):
+    grid origin, step and size per axis, mirror flags, and nx ny nz x 8
+    coefficients.  The TriCub map is compiled out of the reference's default
+    build, and here: tracking through a TriCub (or a TriCubData in the
+    lattice) fails, as there."""
+
+    _typeid = TYPE_TRICUB_DATA
+    _fields = (
+        ("x0", "f"), ("dx", "f"), ("nx", "i"),
+        ("y0", "f"), ("dy", "f"), ("ny", "i"),
+        ("z0", "f"), ("dz", "f"), ("nz", "i"),
+        ("mirror_x", "i"), ("mirror_y", "i"), ("mirror_z", "i"),
+        ("table_addr", ("p", "nx*ny*nz*8")),
+    )
+
+    @staticmethod
+    def ptr_offset():
+        return 0
+
+
+class TriCub(_Element):
+    """Tricubic-interpolated kick element (python/sixtracklib/tricub.py:52-68);
+    ``data_addr`` holds the address of its TriCubData (the reference's
+    TrackJob assigns it).  Compiled out: tracking through it fails."""
+
+    _typeid = TYPE_TRICUB
+    _fields = (
+        ("x_shift", "f"), ("y_shift", "f"), ("tau_shift", "f"),
+        ("dipolar_kick_px", "f"), ("dipolar_kick_py", "f"), ("dipolar_kick_ptau", "f"),
+        ("length", "f"), ("data_addr", "u"),
+    )
+
+    @staticmethod
+    def data_addr_offset():
+        return 7 * 8
+
+
 ELEMENT_TYPES = {
     TYPE_DRIFT: Drift,
     TYPE_DRIFT_EXACT: DriftExact,
@@ -615,6 +653,8 @@ ELEMENT_TYPES = {
     TYPE_SC_QGAUSSIAN_PROF: SCQGaussProfile,
     TYPE_SC_INTERPOLATED_PROF: SCInterpolatedProfile,
     TYPE_LINE_DENSITY_PROF_DATA: LineDensityProfileData,
+    TYPE_TRICUB_DATA: TriCubData,
+    TYPE_TRICUB: TriCub,
 }
 
 

@@ -32,15 +32,23 @@ PROTON_MASS_EV = 938272088.16  # internal/physics_constants.h:53
 class Particles:
     """A particle set backed by one contiguous column block.
 
-    ``Particles(num_particles=n)`` creates a fresh set (chi = charge_ratio =
-    state = 1, particle_id = 0..n-1); pass ``cbuffer=`` to append it to a
-    CObjects buffer, in which case the columns live inside the buffer object
-    and edits are visible to whoever serialises the buffer.
+    ``Particles(num_particles=n, **columns)`` creates a fresh set with the
+    reference's column defaults (python/sixtracklib/particles.py:24-192:
+    mass0 = ``pmass``, beta0 = gamma0 = p0c = 1, rpp = rvv = chi =
+    charge_ratio = state = 1, the rest 0) except particle_id, which is
+    0..n-1 here (0 in the reference, whose ``from_ref`` numbers them), then
+    any column given by name (a scalar or n values; ``at_element_id`` is an
+    alias of ``at_element``).  Pass ``cbuffer=`` to append it to a CObjects
+    buffer, in which case the columns live inside the buffer object and
+    edits are visible to whoever serialises the buffer.
     """
 
-    pmass = PROTON_MASS_EV
+    pmass = 938.2720813e6  # the reference's Python default (particles.py:23)
 
-    def __init__(self, num_particles=0, cbuffer=None, _words=None, _index=None):
+    def __init__(self, num_particles=0, cbuffer=None, _words=None, _index=None, **columns):
+        unknown = set(columns) - set(FIELDS) - {"at_element_id"}
+        if unknown:
+            raise TypeError(f"Particles: unknown column(s) {sorted(unknown)}")
         n = int(num_particles)
         self.num_particles = n
         if _words is None:
@@ -52,6 +60,8 @@ class Particles:
             self._init_defaults()
         else:
             self._words = _words
+        for name, value in columns.items():
+            self.column("at_element" if name == "at_element_id" else name)[:] = value
         self._cbuffer = None
         self._index = _index
         if cbuffer is not None:
@@ -64,6 +74,10 @@ class Particles:
 
     def _init_defaults(self):
         n = self.num_particles
+        self.mass0[:] = self.pmass
+        self.beta0[:] = 1.0
+        self.gamma0[:] = 1.0
+        self.p0c[:] = 1.0
         self.chi[:] = 1.0
         self.charge_ratio[:] = 1.0
         self.state[:] = 1
@@ -101,8 +115,10 @@ class Particles:
         return p
 
     # --------------------------------------------------------- physics
-    def set_reference(self, p0c=7e12, mass0=PROTON_MASS_EV, q0=1.0):
-        """Reference momentum, mass and charge; beta0/gamma0 from p0c."""
+    def set_reference(self, p0c=7e12, mass0=pmass, q0=1.0):
+        """Reference momentum, mass and charge; beta0/gamma0 from p0c (the
+        reference sets q0, mass0 and p0c only and leaves beta0, gamma0 as
+        they were)."""
         energy0 = np.sqrt(p0c * p0c + mass0 * mass0)
         self.q0[:] = q0
         self.mass0[:] = mass0
@@ -126,8 +142,49 @@ class Particles:
         return self
 
     @classmethod
-    def from_ref(cls, num_particles=1, mass0=PROTON_MASS_EV, p0c=1e9, q0=1.0):
+    def from_ref(cls, num_particles=1, mass0=pmass, p0c=1e9, q0=1.0):
         return cls(num_particles=num_particles).set_reference(p0c=p0c, mass0=mass0, q0=q0)
+
+    # the reference's derived quantities (particles.py:202-208)
+    @property
+    def ptau(self):
+        return np.sqrt(self.delta ** 2 + 2 * self.delta + 1 / self.beta0 ** 2) - 1 / self.beta0
+
+    @property
+    def beta(self):
+        return (1 + self.delta) / (1 / self.beta0 + self.ptau)
+
+    @property
+    def sigma(self):
+        return (self.beta0 / self.beta) * self.zeta
+
+    # one particle to / from a pysixtrack Particles (particles.py:216-270)
+    _PYSIX = (("q0", "q0"), ("mass0", "mass0"), ("beta0", "beta0"), ("gamma0", "gamma0"),
+              ("p0c", "p0c"), ("s", "s"), ("x", "x"), ("y", "y"), ("px", "px"), ("py", "py"),
+              ("zeta", "zeta"), ("psigma", "psigma"), ("delta", "delta"), ("chi", "chi"),
+              ("charge_ratio", "qratio"), ("at_element", "elemid"), ("at_turn", "turn"),
+              ("state", "state"))
+
+    def from_pysixtrack(self, inp, particle_index):
+        assert particle_index < self.num_particles
+        for mine, theirs in self._PYSIX:
+            getattr(self, mine)[particle_index] = getattr(inp, theirs)
+        self.rpp[particle_index] = inp.rpp
+        self.rvv[particle_index] = inp.rvv
+        pid = getattr(inp, "partid", None)
+        self.particle_id[particle_index] = pid if pid is not None else particle_index
+        if self._cbuffer is not None:
+            self._cbuffer.touch()
+
+    def to_pysixtrack(self, other, particle_index):
+        """Write particle ``particle_index`` into ``other`` with its
+        coordinate update suspended, as the reference does."""
+        assert particle_index < self.num_particles
+        other._update_coordinates = False
+        for mine, theirs in self._PYSIX:
+            setattr(other, theirs, getattr(self, mine)[particle_index])
+        other.partid = self.particle_id[particle_index]
+        other._update_coordinates = True
 
     @classmethod
     def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
@@ -155,6 +212,45 @@ def _make_prop(name):
 for _name in FIELDS:
     setattr(Particles, _name, _make_prop(_name))
 Particles.at_element_id = _make_prop("at_element")
+
+
+def makeCopy(orig, cbuffer=None):
+    """A new particle set with the columns of ``orig`` (particles.py:292-320)."""
+    return Particles(num_particles=orig.num_particles, cbuffer=cbuffer,
+                     **{name: getattr(orig, name) for name in FIELDS})
+
+
+def calcParticlesDifference(lhs, rhs, cbuffer=None):
+    """Column-wise lhs - rhs as a particle set (particles.py:323-358)."""
+    assert lhs.num_particles == rhs.num_particles
+    diff = Particles(num_particles=lhs.num_particles, cbuffer=cbuffer)
+    for name in FIELDS:
+        diff.column(name)[:] = getattr(lhs, name) - getattr(rhs, name)
+    return diff
+
+
+def compareParticlesDifference(lhs, rhs, abs_treshold=None):
+    """0 when the sets agree, else the sign of the first differing entry
+    (lhs > rhs: +1), columns in order, float columns first; with
+    ``abs_treshold`` > 0 float entries differing by no more than it count as
+    equal; -1 for different or zero particle counts (particles.py:361-415)."""
+    n = lhs.num_particles
+    if n != rhs.num_particles or n <= 0:
+        return -1
+    tol = abs_treshold if abs_treshold is not None and abs_treshold > 0.0 else None
+    for names, use_tol in ((REAL_FIELDS, True), (INT_FIELDS, False)):
+        for name in names:
+            a, b = getattr(lhs, name), getattr(rhs, name)
+            if np.array_equal(a, b):
+                continue
+            if use_tol and tol is not None:
+                bad = np.nonzero(np.abs(a - b) > tol)[0]
+            else:  # NaN compares neither greater nor smaller
+                bad = np.nonzero((a > b) | (a < b))[0]
+            if bad.size:
+                i = bad[0]
+                return +1 if a[i] > b[i] else -1
+    return 0
 
 
 class ParticlesSet:

@@ -199,3 +199,27 @@ def test_element_converter():
 def test_bb6d_named_parameters_need_all_fields():
     with pytest.raises(KeyError):
         BeamBeam6D(x_bb_co=0.0, phi=0.0)
+
+
+def test_tricub_elements_round_trip(oracle):
+    """TriCubData / TriCub (python/sixtracklib/tricub.py) encode and decode;
+    the map is compiled out, so tracking through the lattice fails, as in
+    the reference's default build."""
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.beam_elements import TriCub, TriCubData
+    from sixtracklib_gb300.cbuffer import CBuffer
+
+    e = Elements()
+    e.Drift(length=1.0)
+    table = np.arange(2 * 3 * 4 * 8, dtype=np.float64) * 0.5
+    e.TriCubData(x0=-1.0, dx=0.5, nx=2, y0=-2.0, dy=0.25, ny=3, z0=0.0, dz=0.1, nz=4,
+                 mirror_x=1, table_addr=table)
+    e.TriCub(x_shift=1e-3, length=0.2, data_addr=0)
+    back = Elements(cbuffer=CBuffer.from_image(e.cbuffer.to_image()))
+    d, t = back.get(1), back.get(2)
+    assert isinstance(d, TriCubData) and isinstance(t, TriCub)
+    assert (d.nx, d.ny, d.nz, d.mirror_x, d.dy) == (2, 3, 4, 1, 0.25)
+    np.testing.assert_array_equal(d.table_addr, table)
+    assert (t.x_shift, t.length) == (1e-3, 0.2) and TriCub.data_addr_offset() == 56
+    p = lattices.gaussian_particles(8, seed=1).block.copy()
+    assert oracle.track_until(e.cbuffer.to_image(), p, 1) == -1

@@ -1,0 +1,82 @@
+"""The Python particle-set API of the reference (python/sixtracklib/
+particles.py) on the CPU: column keywords and defaults, derived quantities,
+copies, differences and comparisons, pysixtrack transfers."""
+
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from sixtracklib_gb300 import (ParticlesSet, calcParticlesDifference,
+                               compareParticlesDifference, makeCopy)
+from sixtracklib_gb300.particles import FIELDS, Particles
+
+
+def test_defaults_and_keywords():
+    p = Particles(num_particles=4)
+    assert np.all(p.mass0 == Particles.pmass) and np.all(p.beta0 == 1.0)
+    assert np.all(p.gamma0 == 1.0) and np.all(p.p0c == 1.0) and np.all(p.q0 == 0.0)
+    assert np.all(p.rpp == 1.0) and np.all(p.rvv == 1.0) and np.all(p.state == 1)
+    q = Particles(num_particles=3, x=[1e-3, 2e-3, 3e-3], p0c=7e12, at_element_id=5)
+    np.testing.assert_array_equal(q.x, [1e-3, 2e-3, 3e-3])
+    assert np.all(q.p0c == 7e12) and np.all(q.at_element == 5)
+    with pytest.raises(TypeError):
+        Particles(num_particles=2, xx=1.0)
+    ps = ParticlesSet()
+    r = ps.Particles(num_particles=2, zeta=[0.1, -0.1])
+    np.testing.assert_array_equal(ps.particles[0].zeta, [0.1, -0.1])
+    assert r.num_particles == 2
+
+
+def test_derived_quantities():
+    p = Particles.from_ref(num_particles=3, p0c=20e9)
+    p.set_delta([0.0, 1e-3, -2e-3])
+    b0 = p.beta0
+    ptau = np.sqrt(p.delta ** 2 + 2 * p.delta + 1 / b0 ** 2) - 1 / b0
+    np.testing.assert_allclose(p.ptau, ptau, rtol=1e-15)
+    # ptau / beta0 = psigma: the set_delta of NS(Particles_update_delta_value)
+    np.testing.assert_allclose(p.ptau / b0, p.psigma, rtol=1e-9, atol=1e-18)
+    np.testing.assert_allclose(p.beta, b0 * p.rvv, rtol=1e-14)
+    p.zeta[:] = 0.01
+    np.testing.assert_allclose(p.sigma, 0.01 / p.rvv, rtol=1e-14)
+
+
+def test_copy_difference_compare():
+    p = Particles.from_ref(num_particles=5, p0c=7e12)
+    p.x[:] = np.linspace(-1e-3, 1e-3, 5)
+    c = makeCopy(p)
+    for name in FIELDS:
+        np.testing.assert_array_equal(getattr(c, name), getattr(p, name))
+    assert compareParticlesDifference(p, c) == 0
+    c.x[2] += 1e-12
+    assert compareParticlesDifference(c, p) == +1 and compareParticlesDifference(p, c) == -1
+    assert compareParticlesDifference(c, p, abs_treshold=1e-11) == 0
+    d = calcParticlesDifference(c, p)
+    assert d.x[2] == pytest.approx(1e-12) and np.count_nonzero(d.x) == 1
+    c.x[2] = p.x[2]
+    c.at_turn[4] = 3
+    assert compareParticlesDifference(c, p, abs_treshold=1.0) == +1  # integers: exact
+    c.at_turn[4] = 0
+    c.x[0] = np.nan
+    p.x[0] = np.nan
+    assert compareParticlesDifference(c, p) == 0  # NaN neither greater nor smaller
+    assert compareParticlesDifference(p, Particles(num_particles=4)) == -1
+    assert compareParticlesDifference(Particles(), Particles()) == -1
+
+
+def test_pysixtrack_transfer():
+    p = Particles.from_ref(num_particles=2, p0c=7e12)
+    p.set_delta([1e-4, -1e-4])
+    p.x[:] = [1e-3, -1e-3]
+    p.at_turn[1] = 7
+    other = SimpleNamespace()
+    p.to_pysixtrack(other, 1)
+    assert other.x == -1e-3 and other.turn == 7 and other.qratio == 1.0
+    assert other._update_coordinates is True and other.partid == 1
+    q = Particles(num_particles=2)
+    other.rpp, other.rvv = p.rpp[1], p.rvv[1]
+    q.from_pysixtrack(other, 0)
+    for name in FIELDS:
+        if name != "particle_id":
+            assert getattr(q, name)[0] == getattr(p, name)[1], name
+    assert q.particle_id[0] == 1
