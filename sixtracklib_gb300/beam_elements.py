@@ -83,8 +83,10 @@ class _Element:
 
     @classmethod
     def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
-        self = cls.__new__(cls)
         w = obj.words
+        if w.size < len(cls._fields):  # truncated object: left undecoded
+            return obj
+        self = cls.__new__(cls)
         for i, (name, kind) in enumerate(cls._fields):
             if kind == "f":
                 setattr(self, name, float(w[i : i + 1].view(np.float64)[0]))

@@ -228,7 +228,8 @@ def test_lattice_without_adjoint_is_refused():
     from sixtracklib_gb300.beam_elements import TYPE_TRICUB
 
     e = lattices.fodo_ring()
-    e.cbuffer.add_object(TYPE_TRICUB, np.zeros(3, np.uint64))
+    e.TriCub(length=0.1)
+    assert e.cbuffer.objects[-1].typeid == TYPE_TRICUB
     lat = DifferentiableLattice(e, [])
     blk = _beam(64, seed=1, n_lost=0)
     cols = torch.from_numpy(blk.view(np.int64).copy()).cuda()

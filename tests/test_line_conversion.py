@@ -223,3 +223,17 @@ def test_tricub_elements_round_trip(oracle):
     assert (t.x_shift, t.length) == (1e-3, 0.2) and TriCub.data_addr_offset() == 56
     p = lattices.gaussian_particles(8, seed=1).block.copy()
     assert oracle.track_until(e.cbuffer.to_image(), p, 1) == -1
+
+
+def test_truncated_objects_stay_undecoded():
+    """An object shorter than its type's struct (a malformed or placeholder
+    entry) is returned as the raw CObject instead of being decoded."""
+    from sixtracklib_gb300.autodiff import parameter_table
+    from sixtracklib_gb300.beam_elements import TYPE_TRICUB
+    from sixtracklib_gb300.cbuffer import CObject
+
+    e = Elements()
+    e.Drift(length=1.0)
+    e.cbuffer.add_object(TYPE_TRICUB, np.zeros(3, np.uint64))
+    assert isinstance(e.get(1), CObject)
+    assert parameter_table(e, [])["begin"].size == 3
