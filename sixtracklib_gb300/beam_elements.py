@@ -519,6 +519,13 @@ class LineDensityProfileData(_Element):
     ``capacity`` entries, of which ``num_values`` are used."""
 
     _typeid = TYPE_LINE_DENSITY_PROF_DATA
+
+    @staticmethod
+    def ptr_offset():
+        """Offset added to the object's address when it is assigned to an
+        SCInterpolatedProfile (sc_line_density.py:72-74)."""
+        return 0
+
     _fields = (
         ("method", "u"),
         ("capacity", "i"),
@@ -576,6 +583,11 @@ class SCInterpolatedProfile(_Element):
     _default_line_density_prof_fallback = 1.0
     _default_min_sigma_diff = 1e-10
     _default_enabled = 1
+
+    @staticmethod
+    def interpol_data_addr_offset():
+        """Byte offset of ``interpol_data_addr`` in the struct."""
+        return 6 * 8
 
     def __init__(self, line_density=None, cbuffer=None, **kw):
         self.line_density = None if line_density is None else int(line_density)

@@ -113,6 +113,8 @@ class CBuffer:
     def n_objects(self) -> int:
         return len(self.objects)
 
+    num_objects = n_objects  # the reference's Buffer spells it so
+
     def get_object(self, index: int):
         obj = self.objects[index]
         cls = self.typeids.get(obj.typeid)

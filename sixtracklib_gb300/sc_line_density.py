@@ -59,3 +59,27 @@ class LineDensityBuffer:
             self._release()
         except Exception:
             pass
+
+
+def LineDensityProfileData_create_buffer_assignment(track_job, be_sc_index, interpol_buffer_id,
+                                                    lp_data_index):
+    """Add the assignment of LineDensityProfileData ``lp_data_index`` of the
+    job's stored buffer ``interpol_buffer_id`` to the interpol_data_addr of
+    SCInterpolatedProfile ``be_sc_index`` of the job's beam elements
+    (sc_line_density.py:113-150); True if a new item was added.  The
+    addresses are written by ``track_job.assign_all_addresses()``."""
+    from .beam_elements import (TYPE_LINE_DENSITY_PROF_DATA, TYPE_SC_INTERPOLATED_PROF,
+                                LineDensityProfileData, SCInterpolatedProfile)
+    from .buffer import ARCH_BEAM_ELEMENTS_BUFFER_ID, ARCH_ILLEGAL_BUFFER_ID
+
+    assert interpol_buffer_id != ARCH_ILLEGAL_BUFFER_ID
+    assert track_job.min_stored_buffer_id <= interpol_buffer_id <= track_job.max_stored_buffer_id
+    assert track_job.stored_buffer(interpol_buffer_id).num_objects > lp_data_index
+    before = track_job.num_assign_items(ARCH_BEAM_ELEMENTS_BUFFER_ID, interpol_buffer_id)
+    track_job.add_assign_address_item(
+        dest_elem_type_id=TYPE_SC_INTERPOLATED_PROF, dest_buffer_id=ARCH_BEAM_ELEMENTS_BUFFER_ID,
+        dest_elem_index=be_sc_index,
+        dest_pointer_offset=SCInterpolatedProfile.interpol_data_addr_offset(),
+        src_elem_type_id=TYPE_LINE_DENSITY_PROF_DATA, src_buffer_id=interpol_buffer_id,
+        src_elem_index=lp_data_index, src_pointer_offset=LineDensityProfileData.ptr_offset())
+    return before < track_job.num_assign_items(ARCH_BEAM_ELEMENTS_BUFFER_ID, interpol_buffer_id)

@@ -18,40 +18,23 @@ import ctypes as C
 import numpy as np
 
 from . import _native
+from .buffer import (ARCH_BEAM_ELEMENTS_BUFFER_ID, ARCH_ILLEGAL_BUFFER_ID,
+                     ARCH_MIN_USER_DEFINED_BUFFER_ID, ARCH_PARTICLES_BUFFER_ID,
+                     AddressAssignments, CBufferHandle)
 from .cbuffer import CBuffer
 from .particles import TYPE_PARTICLE, Particles
 
 
 def get_cbuffer_from_obj(obj) -> CBuffer:
-    if isinstance(obj, CBuffer):
-        return obj
-    for attr in ("cbuffer", "_cbuffer"):
-        cb = getattr(obj, attr, None)
-        if isinstance(cb, CBuffer):
-            return cb
-    raise TypeError(f"cannot get a CObjects buffer from {type(obj).__name__}")
+    from .buffer import get_cbuffer_from_obj as find
+
+    cb = find(obj)
+    if cb is None:
+        raise TypeError(f"cannot get a CObjects buffer from {type(obj).__name__}")
+    return cb
 
 
-class _CBufferHandle:
-    """A C-side st_Buffer holding a copy of a Python CBuffer image."""
-
-    def __init__(self, cbuffer: CBuffer):
-        lib = _native.load()
-        img = cbuffer.to_image()
-        self.ptr = lib.st_Buffer_new_on_data(img.ctypes.data, img.nbytes)
-        if not self.ptr:
-            raise RuntimeError("st_Buffer_new_on_data failed: " + _native.last_error())
-
-    def image(self) -> np.ndarray:
-        lib = _native.load()
-        n = lib.st_Buffer_get_size(self.ptr)
-        data = lib.st_Buffer_get_const_data_begin(self.ptr)
-        return np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint64)), shape=(n // 8,)).copy()
-
-    def free(self):
-        if self.ptr:
-            _native.load().st_Buffer_delete(self.ptr)
-            self.ptr = None
+_CBufferHandle = CBufferHandle
 
 
 class TrackJob:
@@ -60,6 +43,16 @@ class TrackJob:
                  config_str=None, particle_set_indices=None):
         self._lib = _native.load()
         self.ptr_st_track_job = None
+        self._stored = {}  # buffer id -> (CBuffer, CBufferHandle, owned)
+        self._next_stored_id = ARCH_MIN_USER_DEFINED_BUFFER_ID
+        self._assign = AddressAssignments()
+        self._assigned = False
+        self._setup(beam_elements_buffer, particles_buffer, until_turn_elem_by_elem, arch,
+                    device_id, device, output_buffer, config_str, particle_set_indices)
+
+    def _setup(self, beam_elements_buffer, particles_buffer, until_turn_elem_by_elem, arch,
+               device_id, device, output_buffer, config_str, particle_set_indices):
+        self._ctor = (arch, device_id, device, config_str)
         self._arch = (arch or "cuda").lower()
         self._particles_buffer = get_cbuffer_from_obj(particles_buffer)
         self._beam_elements_buffer = get_cbuffer_from_obj(beam_elements_buffer)
@@ -93,17 +86,37 @@ class TrackJob:
         if self._lib.st_TrackJob_has_output_buffer(self.ptr_st_track_job):
             self._refresh_output()
 
+    def _release_job(self):
+        if self.ptr_st_track_job:
+            self._lib.st_TrackJob_delete(self.ptr_st_track_job)
+            self.ptr_st_track_job = None
+        for attr in ("_c_particles", "_c_elements", "_c_output"):
+            h = getattr(self, attr, None)
+            if h is not None:
+                h.free()
+            setattr(self, attr, None)
+
     def __del__(self):
         try:
-            if self.ptr_st_track_job:
-                self._lib.st_TrackJob_delete(self.ptr_st_track_job)
-                self.ptr_st_track_job = None
-            for h in (getattr(self, "_c_particles", None), getattr(self, "_c_elements", None),
-                      getattr(self, "_c_output", None)):
-                if h is not None:
-                    h.free()
+            self._release_job()
+            for _cb, h, _own in getattr(self, "_stored", {}).values():
+                h.free()
         except Exception:
             pass
+
+    def reset(self, beam_elements_buffer, particles_buffer, until_turn_elem_by_elem=0,
+              output_buffer=None):
+        """Re-create the job on new buffers (trackjob.py:2044-2100), keeping
+        the arch, device and configuration; stored buffers and assignment
+        items are kept, and assignments already carried out are carried out
+        again on the new beam elements."""
+        arch, device_id, device, config_str = self._ctor
+        self._release_job()
+        self._setup(beam_elements_buffer, particles_buffer, until_turn_elem_by_elem, arch,
+                    device_id, device, output_buffer, config_str, None)
+        if self._assigned:
+            self.assign_all_addresses()
+        return self
 
     # ---------------------------------------------------------- properties
     @property
@@ -221,8 +234,191 @@ class TrackJob:
         return self
 
     def push_beam_elements(self):
+        """Send the beam elements as they are now (edits made after the job
+        was created included) and recompile the lattice."""
+        self._c_elements.refresh(self._beam_elements_buffer)
         self._lib.st_TrackJob_push_beam_elements(self.ptr_st_track_job)
         return self
+
+    # ---------------------------------- stored buffers (trackjob.py:2200-2290)
+    def add_stored_buffer(self, cbuffer=None, size=None, ptr_c_buffer=None,
+                          take_ownership=False, delete_ptr_after_move=False):
+        """Keep a buffer with the job (for example line-density tables that
+        beam elements point at); returns its id (>= 1024), or 0 when nothing
+        usable was given.  ``size`` makes an empty buffer; a raw
+        ``ptr_c_buffer`` is not supported (Python buffers only)."""
+        if ptr_c_buffer is not None:
+            raise NotImplementedError("stored buffers are Python CBuffers here")
+        cb = get_cbuffer_from_obj(cbuffer) if cbuffer is not None else (
+            CBuffer() if size is not None and size > 0 else None)
+        if cb is None:
+            return ARCH_ILLEGAL_BUFFER_ID
+        bid = self._next_stored_id
+        self._next_stored_id += 1
+        self._stored[bid] = (cb, CBufferHandle(cb), cbuffer is None)
+        return bid
+
+    def remove_stored_buffer(self, buffer_id):
+        entry = self._stored.pop(buffer_id, None)
+        if entry is None:
+            return -1
+        entry[1].free()
+        return 0
+
+    @property
+    def has_stored_buffers(self):
+        return bool(self._stored)
+
+    @property
+    def num_stored_buffers(self):
+        return len(self._stored)
+
+    @property
+    def min_stored_buffer_id(self):
+        return min(self._stored) if self._stored else ARCH_ILLEGAL_BUFFER_ID
+
+    @property
+    def max_stored_buffer_id(self):
+        return max(self._stored) if self._stored else ARCH_ILLEGAL_BUFFER_ID
+
+    def owns_stored_buffer(self, buffer_id):
+        return buffer_id in self._stored and self._stored[buffer_id][2]
+
+    def stored_buffer_is_cbuffer(self, buffer_id):
+        return buffer_id in self._stored
+
+    def stored_buffer_cbuffer(self, buffer_id):
+        if buffer_id not in self._stored:
+            raise RuntimeError(f"Unable to retrieve CBuffer for buffer_id={buffer_id}")
+        return self._stored[buffer_id][0]
+
+    def stored_buffer(self, buffer_id):
+        entry = self._stored.get(buffer_id)
+        return entry[0] if entry is not None else None
+
+    def push_stored_buffer(self, buffer_id):
+        """Send the stored buffer's current contents (same structure)."""
+        if buffer_id not in self._stored:
+            raise RuntimeError(f"Unable to push stored buffer {buffer_id}")
+        cb, h, _own = self._stored[buffer_id]
+        h.refresh(cb)
+        if any(it.src_buffer_id == buffer_id for it in self._assign.items) and self._assigned:
+            self.push_beam_elements()  # the lattice holds copies of what it points at
+        return self
+
+    def collect_stored_buffer(self, buffer_id):
+        """The engine does not write stored buffers: nothing to collect."""
+        if buffer_id not in self._stored:
+            raise RuntimeError(f"Unable to collect stored buffer {buffer_id}")
+        return self
+
+    # ------------------------ address assignment (trackjob.py:1833-2035)
+    def _buffers(self):
+        """Sources (C-side copies by id) and destinations (Python buffers by
+        id): the particles buffer can be a source only -- its C-side copy
+        holds the tracked state."""
+        handles = {ARCH_PARTICLES_BUFFER_ID: self._c_particles,
+                   ARCH_BEAM_ELEMENTS_BUFFER_ID: self._c_elements}
+        cbuffers = {ARCH_BEAM_ELEMENTS_BUFFER_ID: self._beam_elements_buffer}
+        for bid, (cb, h, _own) in self._stored.items():
+            handles[bid] = h
+            cbuffers[bid] = cb
+        return handles, cbuffers
+
+    def add_assign_address_item(self, item=None, dest_elem_type_id=None, dest_buffer_id=None,
+                                dest_elem_index=None, dest_pointer_offset=None,
+                                src_elem_type_id=None, src_buffer_id=None, src_elem_index=None,
+                                src_pointer_offset=None):
+        """Add an item (an AssignAddressItem, or its eight fields); an item
+        equal to one already added is not added twice.  Returns the item."""
+        return self._assign.add(AddressAssignments.make(
+            item, dest_elem_type_id=dest_elem_type_id, dest_buffer_id=dest_buffer_id,
+            dest_elem_index=dest_elem_index, dest_pointer_offset=dest_pointer_offset,
+            src_elem_type_id=src_elem_type_id, src_buffer_id=src_buffer_id,
+            src_elem_index=src_elem_index, src_pointer_offset=src_pointer_offset))
+
+    def _find(self, item, fields):
+        try:
+            it = AddressAssignments.make(item, **fields)
+        except ValueError:
+            return None
+        i = self._assign.index_of(it)
+        return None if i is None else self._assign.items[i]
+
+    def has_assign_item(self, item=None, dest_buffer_id=None, src_buffer_id=None, index=None,
+                        **fields):
+        if item is None and index is not None:
+            return 0 <= index < len(self._assign.between(dest_buffer_id, src_buffer_id))
+        return self._find(item, dict(fields, dest_buffer_id=dest_buffer_id,
+                                     src_buffer_id=src_buffer_id)) is not None
+
+    def index_of_assign_address_item(self, item=None, dest_buffer_id=None, src_buffer_id=None,
+                                      **fields):
+        it = self._find(item, dict(fields, dest_buffer_id=dest_buffer_id,
+                                   src_buffer_id=src_buffer_id))
+        if it is None:
+            return None
+        return self._assign.between(int(it.dest_buffer_id), int(it.src_buffer_id)).index(it)
+
+    def ptr_assign_address_item(self, item=None, dest_buffer_id=None, src_buffer_id=None,
+                                index=None, **fields):
+        if item is None and index is not None:
+            items = self._assign.between(dest_buffer_id, src_buffer_id)
+            return items[index] if 0 <= index < len(items) else None
+        return self._find(item, dict(fields, dest_buffer_id=dest_buffer_id,
+                                     src_buffer_id=src_buffer_id))
+
+    def has_assign_items(self, dest_buffer_id, src_buffer_id):
+        return bool(self._assign.between(dest_buffer_id, src_buffer_id))
+
+    def num_assign_items(self, dest_buffer_id, src_buffer_id):
+        return len(self._assign.between(dest_buffer_id, src_buffer_id))
+
+    @property
+    def total_num_assign_items(self):
+        return len(self._assign.items)
+
+    def commit_address_assignments(self):
+        """Check that every item names existing buffers and objects."""
+        handles, cbuffers = self._buffers()
+        sources = dict(cbuffers)
+        sources[ARCH_PARTICLES_BUFFER_ID] = self._particles_buffer
+        for it in self._assign.items:
+            src, dst = sources.get(it.src_buffer_id), cbuffers.get(it.dest_buffer_id)
+            if (src is None or dst is None or
+                    not 0 <= it.src_elem_index < len(src.objects) or
+                    not 0 <= it.dest_elem_index < len(dst.objects)):
+                self._last_status = -1
+                raise RuntimeError("Unable to commit address assignment items")
+        self._last_status = 0
+        return self
+
+    def _perform(self, dest_buffer_id=None, src_buffer_id=None):
+        handles, cbuffers = self._buffers()
+        try:
+            written = self._assign.perform(handles, cbuffers, dest_buffer_id, src_buffer_id)
+        except (RuntimeError, IndexError) as exc:
+            self._last_status = -1
+            raise RuntimeError("Unable to perform assignment of address items: " + str(exc))
+        self._assigned = True
+        self._last_status = 0
+        for bid in written:
+            if bid == ARCH_BEAM_ELEMENTS_BUFFER_ID:
+                self.push_beam_elements()
+            else:
+                handles[bid].refresh(cbuffers[bid])
+        return self
+
+    def assign_all_addresses(self):
+        """Carry out every item and send what changed to the engine."""
+        return self._perform()
+
+    def assign_addresses(self, dest_buffer_id, src_buffer_id):
+        if dest_buffer_id is None and src_buffer_id is None:
+            return self._perform()
+        if dest_buffer_id is None or src_buffer_id is None:
+            raise ValueError("inconsistent dest_buffer_id and src_buffer_id parameters")
+        return self._perform(dest_buffer_id, src_buffer_id)
 
     def _refresh_output(self):
         ptr = self._lib.st_TrackJob_get_output_buffer(self.ptr_st_track_job)

@@ -412,6 +412,63 @@ def test_trackjob_until_line_collect(torch_cuda, oracle):
         TrackJob(e, ps, arch="opencl")
 
 
+def test_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
+    """Line-density tables in a stored buffer assigned to interpolated
+    space-charge kicks through the TrackJob (sc_line_density.py:113-150,
+    trackjob.py:1943-2035), as the reference's space-charge examples do;
+    a strength edited after the job was made reaches the engine on
+    push_beam_elements."""
+    from sixtracklib_gb300 import ParticlesSet
+    from sixtracklib_gb300.sc_line_density import LineDensityProfileData_create_buffer_assignment
+    from sixtracklib_gb300.trackjob import TrackJob
+
+    z = np.linspace(-0.3, 0.3, 41)
+    prof = np.exp(-0.5 * (z / 0.1) ** 2) * 1e12
+    tables = Elements()
+    tables.LineDensityProfileData(values=prof, z0=-0.3, dz=float(z[1] - z[0]), method="linear",
+                                  capacity=48)
+    tables.LineDensityProfileData(values=prof * 1.1, z0=-0.3, dz=float(z[1] - z[0]),
+                                  method="cubic")
+    e = lattices.fodo_ring()
+    first = len(e)
+    for k in range(6):
+        e.SCInterpolatedProfile(number_of_particles=1e11, length=0.5, sigma_x=1e-3,
+                                sigma_y=1.2e-3 if k % 2 else 1e-3, interpol_data_addr=0,
+                                line_density_prof_fallback=5e11, min_sigma_diff=1e-10)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=512)
+    q = lattices.gaussian_particles(512, seed=6, sz=0.12)
+    p.set_block(q.block)
+    job = TrackJob(e, ps, config_str="mode=exact")
+    bid = job.add_stored_buffer(cbuffer=tables)
+    assert bid == 1024 and job.num_stored_buffers == 1 and job.stored_buffer(bid) is tables.cbuffer
+    for k in range(6):
+        assert LineDensityProfileData_create_buffer_assignment(job, first + k, bid, k % 2)
+    assert not LineDensityProfileData_create_buffer_assignment(job, first, bid, 0)
+    assert job.num_assign_items(2, bid) == 6 and job.total_num_assign_items == 6
+    job.commit_address_assignments()
+    job.assign_all_addresses()
+    assert job.track_until(5) == 0
+    job.collect_particles()
+    exp = q.block.copy()
+    assert oracle.track_until(e.cbuffer.to_image(), exp, 5) == 0
+    assert_parity(p.block.copy(), exp, tol=1e-13)
+    fallback = q.block.copy()
+    e_fb = lattices.fodo_ring()
+    for k in range(6):
+        e_fb.SCInterpolatedProfile(number_of_particles=1e11, length=0.5, sigma_x=1e-3,
+                                   sigma_y=1.2e-3 if k % 2 else 1e-3, interpol_data_addr=0,
+                                   line_density_prof_fallback=5e11, min_sigma_diff=1e-10)
+    oracle.track_until(e_fb.cbuffer.to_image(), fallback, 5)
+    assert max_col_dev(p.block.copy(), fallback) > 1e-9  # the tables were used
+    e.get(1).set_knl(0.052, 1)
+    job.push_beam_elements()
+    assert job.track_until(10) == 0
+    job.collect_particles()
+    assert oracle.track_until(e.cbuffer.to_image(), exp, 10) == 0
+    assert_parity(p.block.copy(), exp, tol=1e-12)
+
+
 def test_trackjob_beam_monitor_and_elem_by_elem_output(torch_cuda, oracle):
     """Output buffer: elem-by-elem store first, then one Particles object per
     BeamMonitor (output/output_buffer.c:288-360)."""
