@@ -416,6 +416,63 @@ int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
+/* The rest of the TrackJobNew set that maps onto this job
+ * (track/track_job_base.h:70-420): construction, reset (0 on success, -1 on
+ * failure), buffers and output layout, collect / push flags. */
+st_TrackJobBaseNew *st_TrackJobNew_create(const char *arch_str, const char *config_str);
+st_TrackJobBaseNew *st_TrackJobNew_new(const char *arch, st_Buffer *particles_buffer,
+                                       st_Buffer *beam_elements_buffer, const char *config_str);
+st_TrackJobBaseNew *st_TrackJobNew_new_with_output(const char *arch, st_Buffer *particles_buffer,
+                                                   st_Buffer *beam_elements_buffer,
+                                                   st_Buffer *output_buffer,
+                                                   st_buffer_size_t until_turn_elem_by_elem,
+                                                   const char *config_str);
+st_TrackJobBaseNew *st_TrackJobNew_new_detailed(const char *arch, st_Buffer *particles_buffer,
+                                                st_buffer_size_t num_particle_sets,
+                                                const st_buffer_size_t *particle_set_indices,
+                                                st_Buffer *beam_elements_buffer,
+                                                st_Buffer *output_buffer,
+                                                st_buffer_size_t until_turn_elem_by_elem,
+                                                const char *config_str);
+int32_t st_TrackJobNew_reset(st_TrackJobBaseNew *job, st_Buffer *particles_buffer,
+                             st_Buffer *beam_elements_buffer, st_Buffer *output_buffer);
+int32_t st_TrackJobNew_reset_with_output(st_TrackJobBaseNew *job, st_Buffer *particles_buffer,
+                                         st_Buffer *beam_elements_buffer, st_Buffer *output_buffer,
+                                         st_buffer_size_t until_turn_elem_by_elem);
+int32_t st_TrackJobNew_reset_detailed(st_TrackJobBaseNew *job, st_Buffer *particles_buffer,
+                                      st_buffer_size_t num_particle_sets,
+                                      const st_buffer_size_t *particle_set_indices,
+                                      st_Buffer *beam_elements_buffer, st_Buffer *output_buffer,
+                                      st_buffer_size_t until_turn_elem_by_elem);
+void st_TrackJobNew_clear(st_TrackJobBaseNew *job);
+uint16_t st_TrackJobNew_push(st_TrackJobBaseNew *job, uint16_t flags);
+bool st_TrackJobNew_requires_collecting(const st_TrackJobBaseNew *job);
+st_Buffer *st_TrackJobNew_get_particles_buffer(st_TrackJobBaseNew *job);
+const st_Buffer *st_TrackJobNew_get_const_particles_buffer(const st_TrackJobBaseNew *job);
+st_Buffer *st_TrackJobNew_get_beam_elements_buffer(st_TrackJobBaseNew *job);
+const st_Buffer *st_TrackJobNew_get_const_beam_elements_buffer(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_output_buffer(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_owns_output_buffer(const st_TrackJobBaseNew *job);
+st_Buffer *st_TrackJobNew_get_output_buffer(st_TrackJobBaseNew *job);
+const st_Buffer *st_TrackJobNew_get_const_output_buffer(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_elem_by_elem_output(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_beam_monitor_output(const st_TrackJobBaseNew *job);
+st_buffer_size_t st_TrackJobNew_get_elem_by_elem_output_buffer_offset(
+    const st_TrackJobBaseNew *job);
+st_buffer_size_t st_TrackJobNew_get_beam_monitor_output_buffer_offset(
+    const st_TrackJobBaseNew *job);
+st_buffer_size_t st_TrackJobNew_get_num_beam_monitors(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_beam_monitors(const st_TrackJobBaseNew *job);
+st_buffer_size_t st_TrackJobNew_get_num_particle_sets(const st_TrackJobBaseNew *job);
+st_buffer_size_t st_TrackJobNew_get_total_num_of_particles(const st_TrackJobBaseNew *job);
+const char *st_TrackJobNew_get_arch_string(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_config_str(const st_TrackJobBaseNew *job);
+const char *st_TrackJobNew_get_config_str(const st_TrackJobBaseNew *job);
+uint16_t st_TrackJobNew_get_collect_flags(const st_TrackJobBaseNew *job);
+void st_TrackJobNew_set_collect_flags(st_TrackJobBaseNew *job, uint16_t flags);
+bool st_TrackJobNew_is_collecting_particles(const st_TrackJobBaseNew *job);
+void st_TrackJobNew_enable_collect_particles(st_TrackJobBaseNew *job);
+void st_TrackJobNew_disable_collect_particles(st_TrackJobBaseNew *job);
 uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *job);
 uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *job);
 

@@ -1397,6 +1397,151 @@ int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *j)
 {
     return (j && transfer_outputs(j, true)) ? 0 : -1;
 }
+st_TrackJobBaseNew *st_TrackJobNew_create(const char *arch, const char *cfg)
+{
+    return st_TrackJob_create(arch, cfg);
+}
+st_TrackJobBaseNew *st_TrackJobNew_new(const char *arch, st_Buffer *pb, st_Buffer *eb,
+                                       const char *cfg)
+{
+    return st_TrackJob_new_detailed(arch, pb, 0, nullptr, eb, nullptr, 0, cfg);
+}
+st_TrackJobBaseNew *st_TrackJobNew_new_with_output(const char *arch, st_Buffer *pb, st_Buffer *eb,
+                                                   st_Buffer *ob, st_buffer_size_t until_ebe,
+                                                   const char *cfg)
+{
+    return st_TrackJob_new_detailed(arch, pb, 0, nullptr, eb, ob, until_ebe, cfg);
+}
+st_TrackJobBaseNew *st_TrackJobNew_new_detailed(const char *arch, st_Buffer *pb,
+                                                st_buffer_size_t nsets,
+                                                const st_buffer_size_t *idx, st_Buffer *eb,
+                                                st_Buffer *ob, st_buffer_size_t until_ebe,
+                                                const char *cfg)
+{
+    return st_TrackJob_new_detailed(arch, pb, nsets, idx, eb, ob, until_ebe, cfg);
+}
+int32_t st_TrackJobNew_reset(st_TrackJobBaseNew *j, st_Buffer *pb, st_Buffer *eb, st_Buffer *ob)
+{
+    return st_TrackJob_reset(j, pb, eb, ob) ? 0 : -1;
+}
+int32_t st_TrackJobNew_reset_with_output(st_TrackJobBaseNew *j, st_Buffer *pb, st_Buffer *eb,
+                                         st_Buffer *ob, st_buffer_size_t until_ebe)
+{
+    return st_TrackJob_reset_with_output(j, pb, eb, ob, until_ebe) ? 0 : -1;
+}
+int32_t st_TrackJobNew_reset_detailed(st_TrackJobBaseNew *j, st_Buffer *pb,
+                                      st_buffer_size_t nsets, const st_buffer_size_t *idx,
+                                      st_Buffer *eb, st_Buffer *ob, st_buffer_size_t until_ebe)
+{
+    return st_TrackJob_reset_detailed(j, pb, nsets, idx, eb, ob, until_ebe) ? 0 : -1;
+}
+void st_TrackJobNew_clear(st_TrackJobBaseNew *j) { st_TrackJob_clear(j); }
+uint16_t st_TrackJobNew_push(st_TrackJobBaseNew *j, uint16_t flags)
+{
+    if (!j) return 0;
+    st_TrackJob_push(j, flags);
+    return (uint16_t)(flags & 0x07);
+}
+bool st_TrackJobNew_requires_collecting(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_requires_collecting(j);
+}
+st_Buffer *st_TrackJobNew_get_particles_buffer(st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_particles_buffer(j);
+}
+const st_Buffer *st_TrackJobNew_get_const_particles_buffer(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_const_particles_buffer(j);
+}
+st_Buffer *st_TrackJobNew_get_beam_elements_buffer(st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_beam_elements_buffer(j);
+}
+const st_Buffer *st_TrackJobNew_get_const_beam_elements_buffer(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_const_beam_elements_buffer(j);
+}
+bool st_TrackJobNew_has_output_buffer(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_output_buffer(j);
+}
+bool st_TrackJobNew_owns_output_buffer(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_owns_output_buffer(j);
+}
+st_Buffer *st_TrackJobNew_get_output_buffer(st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_output_buffer(j);
+}
+const st_Buffer *st_TrackJobNew_get_const_output_buffer(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_const_output_buffer(j);
+}
+bool st_TrackJobNew_has_elem_by_elem_output(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_elem_by_elem_output(j);
+}
+bool st_TrackJobNew_has_beam_monitor_output(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_beam_monitor_output(j);
+}
+st_buffer_size_t st_TrackJobNew_get_elem_by_elem_output_buffer_offset(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_elem_by_elem_output_buffer_offset(j);
+}
+st_buffer_size_t st_TrackJobNew_get_beam_monitor_output_buffer_offset(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_beam_monitor_output_buffer_offset(j);
+}
+st_buffer_size_t st_TrackJobNew_get_num_beam_monitors(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_num_beam_monitors(j);
+}
+bool st_TrackJobNew_has_beam_monitors(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_beam_monitors(j);
+}
+st_buffer_size_t st_TrackJobNew_get_num_particle_sets(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_num_particle_sets(j);
+}
+st_buffer_size_t st_TrackJobNew_get_total_num_of_particles(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_total_num_particles_in_sets(j);
+}
+const char *st_TrackJobNew_get_arch_string(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_type_str(j);
+}
+bool st_TrackJobNew_has_config_str(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_config_str(j);
+}
+const char *st_TrackJobNew_get_config_str(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_config_str(j);
+}
+uint16_t st_TrackJobNew_get_collect_flags(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_get_collect_flags(j);
+}
+void st_TrackJobNew_set_collect_flags(st_TrackJobBaseNew *j, uint16_t f)
+{
+    st_TrackJob_set_collect_flags(j, f);
+}
+bool st_TrackJobNew_is_collecting_particles(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_is_collecting_particles(j);
+}
+void st_TrackJobNew_enable_collect_particles(st_TrackJobBaseNew *j)
+{
+    st_TrackJob_enable_collect_particles(j);
+}
+void st_TrackJobNew_disable_collect_particles(st_TrackJobBaseNew *j)
+{
+    st_TrackJob_disable_collect_particles(j);
+}
 uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *j)
 {
     return j ? (uint64_t)j->opt.threads : 0;

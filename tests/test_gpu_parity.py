@@ -535,3 +535,73 @@ def test_free_function_until_single_and_all(torch_cuda, oracle):
     oracle.track_until(lat, exp2, 7, i0=5, i1=6)
     assert_parity(blk2, exp2, tol=1e-13)
     L.st_Buffer_delete(be)
+
+
+def test_trackjobnew_c_abi(torch_cuda, oracle):
+    """The TrackJobNew entry points (track/track_job_base.h) on one job:
+    construction with output, accessors, tracking, collect and reset."""
+    import ctypes as Cc
+
+    from sixtracklib_gb300 import ParticlesSet, _native
+
+    L = _native.load()
+    vp, u64, cb, u16 = Cc.c_void_p, Cc.c_uint64, Cc.c_bool, Cc.c_uint16
+    sig = {"st_TrackJobNew_new_with_output": ([Cc.c_char_p, vp, vp, vp, u64, Cc.c_char_p], vp),
+           "st_TrackJobNew_owns_output_buffer": ([vp], cb),
+           "st_TrackJobNew_has_output_buffer": ([vp], cb),
+           "st_TrackJobNew_has_beam_monitors": ([vp], cb),
+           "st_TrackJobNew_get_num_beam_monitors": ([vp], u64),
+           "st_TrackJobNew_get_total_num_of_particles": ([vp], u64),
+           "st_TrackJobNew_get_arch_string": ([vp], Cc.c_char_p),
+           "st_TrackJobNew_get_particles_buffer": ([vp], vp),
+           "st_TrackJobNew_get_collect_flags": ([vp], u16),
+           "st_TrackJobNew_track_until": ([vp, u64], Cc.c_int32),
+           "st_TrackJobNew_collect_particles": ([vp], Cc.c_int32),
+           "st_TrackJobNew_reset": ([vp, vp, vp, vp], Cc.c_int32),
+           "st_TrackJobNew_delete": ([vp], None)}
+    for name, (args, res) in sig.items():
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = res
+    e = lattices.fodo_ring()
+    e.BeamMonitor(num_stores=4, start=0, skip=1, is_rolling=1, is_turn_ordered=1)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=100)
+    q = lattices.gaussian_particles(100, seed=15)
+    p.set_block(q.block)
+    from tests import capi
+
+    pb = capi.c_buffer_from_image(ps.cbuffer.to_image())
+    eb = capi.c_buffer_from_image(e.cbuffer.to_image())
+    job = L.st_TrackJobNew_new_with_output(b"cuda", pb, eb, None, 0, b"mode=exact")
+    assert job, _native.last_error()
+    assert L.st_TrackJobNew_has_output_buffer(job) and L.st_TrackJobNew_owns_output_buffer(job)
+    assert L.st_TrackJobNew_has_beam_monitors(job)
+    assert L.st_TrackJobNew_get_num_beam_monitors(job) == 1
+    assert L.st_TrackJobNew_get_total_num_of_particles(job) == 100
+    assert L.st_TrackJobNew_get_arch_string(job) == b"cuda"
+    assert L.st_TrackJobNew_get_particles_buffer(job) == pb
+    assert L.st_TrackJobNew_track_until(job, 10) == 0
+    assert L.st_TrackJobNew_collect_particles(job) == 0
+    got = capi_columns(pb)
+    exp = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp, 10)
+    assert_parity(got, exp, tol=1e-13)
+    # reset on fresh particles: tracking starts over
+    pb2 = capi.c_buffer_from_image(ps.cbuffer.to_image())
+    assert L.st_TrackJobNew_reset(job, pb2, eb, None) == 0
+    assert L.st_TrackJobNew_track_until(job, 3) == 0
+    assert L.st_TrackJobNew_collect_particles(job) == 0
+    exp3 = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp3, 3)
+    assert_parity(capi_columns(pb2), exp3, tol=1e-13)
+    L.st_TrackJobNew_delete(job)
+    for b in (pb, pb2, eb):
+        L.st_Buffer_delete(b)
+
+
+def capi_columns(c_buffer):
+    """The 21 x n columns of Particles object 0 of a C-side buffer."""
+    from sixtracklib_gb300.trackjob import _c_columns
+    from sixtracklib_gb300 import _native
+
+    return _c_columns(_native.load(), c_buffer, 0)
