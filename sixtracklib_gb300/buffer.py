@@ -102,10 +102,55 @@ class CBufferHandle:
                 w[f] = begins[target][0]
             C.memmove(b, w.ctypes.data, s)
 
+    def pull_into(self, cbuffer: CBuffer) -> None:
+        """Copy this copy's objects back into the Python buffer (the
+        reference's buffers are one memory on both sides, so what its
+        TrackJob writes -- a monitor's particle-id range at set-up -- is
+        seen by the caller); pointer and link fields keep their Python
+        form."""
+        n = self._lib.st_Buffer_get_num_of_objects(self.ptr)
+        if n != len(cbuffer.objects):
+            raise RuntimeError("buffer structure changed: reset the job")
+        for i, obj in enumerate(cbuffer.objects):
+            b, t, s = self.object_info(i)
+            if t != obj.typeid or s != obj.words.nbytes:
+                raise RuntimeError(f"object {i} changed type or size: reset the job")
+            cw = np.ctypeslib.as_array(C.cast(C.c_void_p(b), C.POINTER(C.c_uint64)),
+                                       shape=(s // 8,))
+            keep = sorted(set(obj.ptr_fields) | {f for f, _ in obj.links})
+            saved = obj.words[keep].copy()
+            obj.words[:] = cw
+            obj.words[keep] = saved
+        cbuffer.touch()
+
     def free(self):
         if self.ptr:
             self._lib.st_Buffer_delete(self.ptr)
             self.ptr = None
+
+
+class Buffer:
+    """The view of a stored buffer that ``TrackJob.stored_buffer`` returns
+    (buffer.py:92-200): the job's C-side copy (``pointer``), its object
+    count and size, and the Python buffer it copies (``cbuffer``)."""
+
+    maps_to_cbuffer = True
+
+    def __init__(self, cbuffer: CBuffer, handle: CBufferHandle):
+        self.cbuffer = cbuffer
+        self._handle = handle
+
+    @property
+    def pointer(self):
+        return self._handle.ptr
+
+    @property
+    def num_objects(self):
+        return int(self._handle._lib.st_Buffer_get_num_of_objects(self._handle.ptr))
+
+    @property
+    def size(self):
+        return int(self._handle._lib.st_Buffer_get_size(self._handle.ptr))
 
 
 class AssignAddressItem(_Element):

@@ -115,6 +115,11 @@ class CBuffer:
 
     num_objects = n_objects  # the reference's Buffer spells it so
 
+    @property
+    def size(self) -> int:
+        """Size of the buffer's image in bytes."""
+        return int(self.to_image().nbytes)
+
     def get_object(self, index: int):
         obj = self.objects[index]
         cls = self.typeids.get(obj.typeid)

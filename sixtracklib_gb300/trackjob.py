@@ -18,9 +18,10 @@ import ctypes as C
 import numpy as np
 
 from . import _native
+from .beam_elements import TYPE_BEAM_MONITOR
 from .buffer import (ARCH_BEAM_ELEMENTS_BUFFER_ID, ARCH_ILLEGAL_BUFFER_ID,
                      ARCH_MIN_USER_DEFINED_BUFFER_ID, ARCH_PARTICLES_BUFFER_ID,
-                     AddressAssignments, CBufferHandle)
+                     AddressAssignments, Buffer, CBufferHandle)
 from .cbuffer import CBuffer
 from .particles import TYPE_PARTICLE, Particles
 
@@ -83,6 +84,8 @@ class TrackJob:
             cfg.encode())
         if not self.ptr_st_track_job:
             raise RuntimeError("unable to create TrackJob: " + _native.last_error())
+        # set-up writes into the beam elements (monitors' particle-id ranges)
+        self._c_elements.pull_into(self._beam_elements_buffer)
         if self._lib.st_TrackJob_has_output_buffer(self.ptr_st_track_job):
             self._refresh_output()
 
@@ -218,6 +221,7 @@ class TrackJob:
         return self
 
     def collect_beam_elements(self):
+        self._c_elements.pull_into(self._beam_elements_buffer)
         return self
 
     def collect_output(self):
@@ -293,8 +297,15 @@ class TrackJob:
         return self._stored[buffer_id][0]
 
     def stored_buffer(self, buffer_id):
+        """A :class:`~sixtracklib_gb300.buffer.Buffer` view of the stored
+        buffer (C-side copy and the Python buffer), or None."""
         entry = self._stored.get(buffer_id)
-        return entry[0] if entry is not None else None
+        return Buffer(entry[0], entry[1]) if entry is not None else None
+
+    def ptr_stored_buffer(self, buffer_id):
+        """The C-side st_Buffer of a stored buffer, or None."""
+        entry = self._stored.get(buffer_id)
+        return entry[1].ptr if entry is not None else None
 
     def push_stored_buffer(self, buffer_id):
         """Send the stored buffer's current contents (same structure)."""
@@ -307,9 +318,35 @@ class TrackJob:
         return self
 
     def collect_stored_buffer(self, buffer_id):
-        """The engine does not write stored buffers: nothing to collect."""
+        """Bring the stored buffer up to date.  The engine writes a stored
+        buffer only through BeamMonitors whose ``out_address`` was assigned
+        from it: their turn-by-turn records (the job's own monitor output,
+        the reference's layout) are copied into the assigned particle sets,
+        as many particles as both hold."""
         if buffer_id not in self._stored:
             raise RuntimeError(f"Unable to collect stored buffer {buffer_id}")
+        items = [it for it in self._assign.items
+                 if it.src_buffer_id == buffer_id and
+                 it.dest_buffer_id == ARCH_BEAM_ELEMENTS_BUFFER_ID and
+                 it.dest_elem_type_id == TYPE_BEAM_MONITOR]
+        if items and self._assigned and self.has_beam_monitor_output:
+            self.collect_output()
+            monitors = [i for i, o in enumerate(self._beam_elements_buffer.objects)
+                        if o.typeid == TYPE_BEAM_MONITOR]
+            cb, h, _own = self._stored[buffer_id]
+            cb.typeids[TYPE_PARTICLE] = Particles
+            for it in items:
+                k = monitors.index(int(it.dest_elem_index))
+                out = self.output_particles(self.beam_monitor_output_offset + k)
+                dst = cb.get_object(int(it.src_elem_index))
+                if not isinstance(dst, Particles):
+                    continue
+                n = min(dst.num_particles, out.num_particles)
+                cols = dst.block.copy()
+                cols[:, :n] = out.block[:, :n]
+                dst.set_block(cols)
+            cb.touch()
+            h.refresh(cb)
         return self
 
     # ------------------------ address assignment (trackjob.py:1833-2035)

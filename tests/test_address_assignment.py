@@ -182,3 +182,28 @@ def test_trackjob_host_logic_without_engine(oracle):
         job.add_assign_address_item(dest_buffer_id=2)
     for h in (job._c_particles, job._c_elements):
         h.free()
+
+
+def test_pull_into_brings_back_c_side_writes():
+    """What the engine writes into its lattice copy (a monitor's particle-id
+    range at job set-up) comes back into the Python lattice; pointer fields
+    keep their Python form, so the lattice still serialises the same way."""
+    import ctypes as C
+
+    from sixtracklib_gb300.buffer import CBufferHandle
+
+    e = lattices.fodo_ring()
+    bm = len(e)
+    e.BeamMonitor(num_stores=4, start=0, skip=1)
+    h = CBufferHandle(e.cbuffer)
+    b, t, s = h.object_info(bm)
+    w = C.cast(C.c_void_p(b), C.POINTER(C.c_uint64))
+    w[4], w[5] = 99, 3  # max / min particle id
+    img0 = e.cbuffer.to_image().copy()
+    h.pull_into(e.cbuffer)
+    m = e.get(bm)
+    assert (m.max_particle_id, m.min_particle_id) == (99, 3)
+    diff = np.nonzero(e.cbuffer.to_image() != img0)[0]
+    assert diff.size == 2  # only the two id fields changed
+    np.testing.assert_array_equal(e.get(1).bal, lattices.fodo_ring().get(1).bal)
+    h.free()

@@ -441,7 +441,8 @@ def test_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
     p.set_block(q.block)
     job = TrackJob(e, ps, config_str="mode=exact")
     bid = job.add_stored_buffer(cbuffer=tables)
-    assert bid == 1024 and job.num_stored_buffers == 1 and job.stored_buffer(bid) is tables.cbuffer
+    assert bid == 1024 and job.num_stored_buffers == 1
+    assert job.stored_buffer(bid).cbuffer is tables.cbuffer
     for k in range(6):
         assert LineDensityProfileData_create_buffer_assignment(job, first + k, bid, k % 2)
     assert not LineDensityProfileData_create_buffer_assignment(job, first, bid, 0)
@@ -605,3 +606,40 @@ def capi_columns(c_buffer):
     from sixtracklib_gb300 import _native
 
     return _c_columns(_native.load(), c_buffer, 0)
+
+
+def test_trackjob_monitor_output_into_stored_buffer(torch_cuda):
+    """A BeamMonitor whose out_address is assigned from a particle set in a
+    stored buffer (tests/python/test_track_job_cpu_assign_address_items.py):
+    after tracking, collect_stored_buffer leaves the monitor's turn-by-turn
+    records there, equal to the job's own monitor output."""
+    from sixtracklib_gb300 import ParticlesSet
+    from sixtracklib_gb300.beam_elements import TYPE_BEAM_MONITOR
+    from sixtracklib_gb300.particles import TYPE_PARTICLE
+    from sixtracklib_gb300.trackjob import TrackJob
+
+    e = lattices.fodo_ring()
+    bm = len(e)
+    e.BeamMonitor(num_stores=4, start=0, skip=1, is_rolling=0, is_turn_ordered=1)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=64)
+    p.set_block(lattices.gaussian_particles(64, seed=19).block)
+    out = ParticlesSet()
+    out.Particles(num_particles=4 * 64)
+    job = TrackJob(e, ps, config_str="mode=exact")
+    oid = job.add_stored_buffer(cbuffer=out)
+    assert job.stored_buffer(oid).num_objects == 1 and job.ptr_stored_buffer(oid)
+    job.add_assign_address_item(
+        dest_elem_type_id=TYPE_BEAM_MONITOR, dest_buffer_id=2, dest_elem_index=bm,
+        dest_pointer_offset=24, src_elem_type_id=TYPE_PARTICLE, src_buffer_id=oid,
+        src_elem_index=0, src_pointer_offset=0)
+    job.commit_address_assignments()
+    job.assign_all_addresses()
+    assert e.get(bm).out_address != 0
+    job.track_until(4)
+    job.collect_stored_buffer(oid)
+    job.collect_output()
+    mon = job.output_particles(job.beam_monitor_output_offset)
+    got = out.particles[0]
+    assert np.array_equal(got.block, mon.block)
+    assert np.count_nonzero(got.x) > 200 and set(np.unique(got.at_turn)) == {0, 1, 2, 3}
