@@ -286,9 +286,13 @@ int64_t st_ElemByElemConfig_get_stored_num_particles(const st_ElemByElemConfig *
  * "gb300", "gpu"); the reference's "cpu" / "opencl" backends are not part
  * of this engine and are rejected with NULL.  `config_str` accepts
  * whitespace-separated key=value pairs (see st_TrackJob_get_config_str):
- *   mode=exact|fast  threads_per_block=N  device=N  aperture=always|never|
- *   conditional  aperture_min_length=L  x_limit=X  y_limit=Y
- * and the reference's TOML form "[cuda]\n track_threads_per_block = N". */
+ *   mode=exact|fast  threads_per_block=N  track_threads_per_block=N
+ *   device=N  aperture=always|never|conditional  aperture_min_length=L
+ *   x_limit=X  y_limit=Y
+ * and the reference's TOML forms ("[cuda]\n track_threads_per_block = N",
+ * "cuda.threads_per_block = N").  Block sizes are multiples of 32 up to
+ * 1024, as in the reference; the tracking kernel (track_threads_per_block,
+ * else threads_per_block) runs with at most 256 threads per block. */
 st_TrackJob *st_TrackJob_create(const char *arch, const char *config_str);
 st_TrackJob *st_TrackJob_new(const char *arch, st_Buffer *particles_buffer,
                              st_Buffer *beam_elements_buffer, const char *config_str);
@@ -473,6 +477,8 @@ void st_TrackJobNew_set_collect_flags(st_TrackJobBaseNew *job, uint16_t flags);
 bool st_TrackJobNew_is_collecting_particles(const st_TrackJobBaseNew *job);
 void st_TrackJobNew_enable_collect_particles(st_TrackJobBaseNew *job);
 void st_TrackJobNew_disable_collect_particles(st_TrackJobBaseNew *job);
+/* cuda/track_job.h: the tracking kernel's block size as it runs, and the
+ * configured threads_per_block. */
 uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *job);
 uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *job);
 

@@ -53,6 +53,9 @@ _SIGNATURES = {
     "st_TrackJob_push_output": ([vp], None),
     "st_TrackJob_has_output_buffer": ([vp], cbool),
     "st_TrackJob_owns_output_buffer": ([vp], cbool),
+    "st_TrackJob_is_collecting_particles": ([vp], cbool),
+    "st_CudaTrackJob_default_threads_per_block": ([vp], u64),
+    "st_CudaTrackJob_default_track_threads_per_block": ([vp], u64),
     "st_TrackJob_get_output_buffer": ([vp], vp),
     "st_TrackJob_has_elem_by_elem_output": ([vp], cbool),
     "st_TrackJob_has_beam_monitor_output": ([vp], cbool),

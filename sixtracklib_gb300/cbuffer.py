@@ -120,9 +120,11 @@ class CBuffer:
         """Size of the buffer's image in bytes."""
         return int(self.to_image().nbytes)
 
-    def get_object(self, index: int):
+    def get_object(self, index: int, cls=None):
+        """Object ``index`` decoded as ``cls`` (default: the class registered
+        for its type id), or the raw CObject."""
         obj = self.objects[index]
-        cls = self.typeids.get(obj.typeid)
+        cls = cls if cls is not None else self.typeids.get(obj.typeid)
         if cls is not None and hasattr(cls, "_from_cobject"):
             return cls._from_cobject(obj, self, index)
         return obj

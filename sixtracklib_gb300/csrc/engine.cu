@@ -35,7 +35,9 @@ namespace stg {
 // ------------------------------------------------------------- options
 struct Options {
     bool fast = false;
-    int threads = 128;
+    int threads = 128;           // tracking kernel's block size (effective)
+    int threads_general = 128;   // the reference's cuda.threads_per_block
+    int track_threads_req = 0;   // cuda.track_threads_per_block as given (0: unset)
     int device = 0;
     int aperture_mode = 2;
     double aperture_min_length = 0.0;
@@ -88,16 +90,18 @@ static bool parse_options(const char *cfg, Options *o, std::string *err)
                 if (err) *err = "config: expected key=value, got '" + it + "'";
                 return false;
             }
-            std::string const k = trim(it.substr(0, eq));
+            std::string k = trim(it.substr(0, eq));
             std::string const v = trim(it.substr(eq + 1));
+            if (k.rfind("cuda.", 0) == 0) k = k.substr(5);  // dotted TOML keys
             try {
                 if (k == "mode") {
                     if (v == "fast") o->fast = true;
                     else if (v == "exact") o->fast = false;
                     else throw std::invalid_argument(v);
-                } else if (k == "threads_per_block" || k == "track_threads_per_block" ||
-                           k == "threads") {
-                    o->threads = std::stoi(v);
+                } else if (k == "threads_per_block" || k == "threads") {
+                    o->threads_general = std::stoi(v);
+                } else if (k == "track_threads_per_block") {
+                    o->track_threads_req = std::stoi(v);
                 } else if (k == "device" || k == "device_id") {
                     o->device = std::stoi(v);
                 } else if (k == "aperture") {
@@ -127,10 +131,18 @@ static bool parse_options(const char *cfg, Options *o, std::string *err)
             }
         }
     }
-    if (o->threads < 32 || o->threads > kMaxThreads || o->threads % 32 != 0) {
-        if (err) *err = "config: threads_per_block must be a multiple of 32 in [32, 256]";
-        return false;
+    // The tracking kernel's block size: track_threads_per_block, else
+    // threads_per_block.  The reference accepts up to 1024; this kernel's
+    // register budget allows at most kMaxThreads, so larger requests run
+    // with kMaxThreads threads per block.
+    int const req = o->track_threads_req > 0 ? o->track_threads_req : o->threads_general;
+    for (int t : {req, o->threads_general}) {
+        if (t < 32 || t > 1024 || t % 32 != 0) {
+            if (err) *err = "config: threads_per_block must be a multiple of 32 in [32, 1024]";
+            return false;
+        }
     }
+    o->threads = req < kMaxThreads ? req : kMaxThreads;
     if (o->stages < 2 || o->stages > 8) {
         if (err) *err = "config: stages must be in [2, 8]";
         return false;
@@ -1548,7 +1560,7 @@ uint64_t st_CudaTrackJob_default_track_threads_per_block(const st_CudaTrackJob *
 }
 uint64_t st_CudaTrackJob_default_threads_per_block(const st_CudaTrackJob *j)
 {
-    return j ? (uint64_t)j->opt.threads : 0;
+    return j ? (uint64_t)j->opt.threads_general : 0;
 }
 
 }  // extern "C"

@@ -23,7 +23,7 @@ from .buffer import (ARCH_BEAM_ELEMENTS_BUFFER_ID, ARCH_ILLEGAL_BUFFER_ID,
                      ARCH_MIN_USER_DEFINED_BUFFER_ID, ARCH_PARTICLES_BUFFER_ID,
                      AddressAssignments, Buffer, CBufferHandle)
 from .cbuffer import CBuffer
-from .particles import TYPE_PARTICLE, Particles
+from .particles import TYPE_PARTICLE, Particles, ParticlesSet
 
 
 def get_cbuffer_from_obj(obj) -> CBuffer:
@@ -129,6 +129,30 @@ class TrackJob:
     last_track_status = last_status
 
     @property
+    def last_status_success(self):
+        return self._last_status == 0
+
+    last_track_status_success = last_status_success
+
+    @property
+    def is_in_debug_mode(self):
+        """The engine has no debug mode (kernel-side status words are always
+        read back)."""
+        return False
+
+    @property
+    def is_collecting_particles(self):
+        return bool(self._lib.st_TrackJob_is_collecting_particles(self.ptr_st_track_job))
+
+    @property
+    def num_particle_sets(self):
+        return len(self._pset_indices)
+
+    @property
+    def owns_output_buffer(self):
+        return bool(self._lib.st_TrackJob_owns_output_buffer(self.ptr_st_track_job))
+
+    @property
     def arch(self):
         return self._arch
 
@@ -153,7 +177,8 @@ class TrackJob:
 
     @property
     def output(self):
-        return self._output_buffer
+        """The output buffer as a particle-set container (trackjob.py:571)."""
+        return ParticlesSet(self._output_buffer) if self._output_buffer is not None else None
 
     @property
     def has_output_buffer(self):
@@ -235,6 +260,11 @@ class TrackJob:
             blk = self._particles_buffer.get_object(i).block
             _c_columns(self._lib, self._c_particles.ptr, i, write=blk)
         self._lib.st_TrackJob_push_particles(self.ptr_st_track_job)
+        return self
+
+    def _push_output(self):
+        """Send the host output buffer to the device copy (trackjob.py:1582)."""
+        self._lib.st_TrackJob_push_output(self.ptr_st_track_job)
         return self
 
     def push_beam_elements(self):
@@ -493,11 +523,31 @@ def _c_columns(lib, c_buffer, index, write=None):
 
 
 class CudaTrackJob(TrackJob):
-    """cuda/track_job.h:42-66 / python/sixtracklib/cuda.py:565: a TrackJob
-    bound to a CUDA node id ("platform.device")."""
+    """cuda/track_job.h:42-66 / python/sixtracklib/cuda.py:565-710: a TrackJob
+    bound to a CUDA node id ("platform.device"); arguments in the
+    reference's order (the third is the particle set's index)."""
 
-    def __init__(self, beam_elements_buffer, particles_buffer, until_turn_elem_by_elem=0,
-                 node_id_str=None, output_buffer=None, config_str=None, **kw):
+    def __init__(self, beam_elements_buffer, particles_buffer, particle_set_index=0,
+                 until_turn_elem_by_elem=0, output_buffer=None, node_id_str=None,
+                 config_str=None, **kw):
+        kw.setdefault("particle_set_indices", [int(particle_set_index)])
         super().__init__(beam_elements_buffer, particles_buffer, until_turn_elem_by_elem,
                          arch="cuda", device=node_id_str, output_buffer=output_buffer,
                          config_str=config_str, **kw)
+
+    @property
+    def default_threads_per_block(self):
+        return int(self._lib.st_CudaTrackJob_default_threads_per_block(self.ptr_st_track_job))
+
+    @property
+    def default_track_threads_per_block(self):
+        return int(self._lib.st_CudaTrackJob_default_track_threads_per_block(
+            self.ptr_st_track_job))
+
+    # The reference's CUDA job keeps device-side arguments for the particles,
+    # the beam elements and the particle addresses and a controller for its
+    # node; this job holds the same data on its device.
+    has_controller = property(lambda self: self.ptr_st_track_job is not None)
+    has_particles_arg = property(lambda self: self.ptr_st_track_job is not None)
+    has_beam_elements_arg = property(lambda self: self.ptr_st_track_job is not None)
+    has_particles_addr_arg = property(lambda self: self.ptr_st_track_job is not None)

@@ -488,7 +488,7 @@ def test_trackjob_beam_monitor_and_elem_by_elem_output(torch_cuda, oracle):
     job.track_elem_by_elem(2)
     job.track_until(12)
     job.collect()
-    out = job.output
+    out = job.output.cbuffer
     ebe = out.get_object(0).block.copy()
     mon = out.get_object(1).block.copy()
     # oracle with the same configuration
@@ -643,3 +643,41 @@ def test_trackjob_monitor_output_into_stored_buffer(torch_cuda):
     got = out.particles[0]
     assert np.array_equal(got.block, mon.block)
     assert np.count_nonzero(got.x) > 200 and set(np.unique(got.at_turn)) == {0, 1, 2, 3}
+
+
+def test_cuda_trackjob_properties_and_track_line(torch_cuda, oracle):
+    """CudaTrackJob as the reference's CUDA tests drive it
+    (tests/python/cuda/test_track_job_threads_per_block.py,
+    test_track_job_track_line.py): particle-set index as the third
+    argument, dotted TOML keys, the job's properties, and tracking line by
+    line, element after element, until a full turn."""
+    from sixtracklib_gb300 import ParticlesSet
+    from sixtracklib_gb300.trackjob import CudaTrackJob
+
+    e = lattices.fodo_ring()
+    ps = ParticlesSet()
+    ps.Particles(num_particles=10)  # set 0: not tracked
+    p = ps.Particles(num_particles=200)
+    q = lattices.gaussian_particles(200, seed=23)
+    p.set_block(q.block)
+    cfg = "cuda.threads_per_block = 256\r\ncuda.track_threads_per_block = 512\r\n"
+    job = CudaTrackJob(e, ps, 1, config_str=cfg)
+    assert job.arch_str == "cuda" and job.is_collecting_particles and job.requires_collecting
+    assert job.has_controller and job.has_particles_arg and job.has_beam_elements_arg
+    assert not job.is_in_debug_mode and not job.has_output_buffer and not job.owns_output_buffer
+    assert job.num_particle_sets == 1
+    assert job.default_threads_per_block == 256
+    assert job.default_track_threads_per_block == 256  # 512 requested: the kernel's maximum
+    n = len(e)
+    for k in range(n):
+        job.track_line(k, k + 1, finish_turn=(k == n - 1))
+        assert job.last_track_status_success
+    job.collect_particles()
+    exp = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp, 1)
+    got = ps.particles[1].block.copy()
+    assert_parity(got, exp, tol=1e-13)
+    assert np.all(got[19].view(np.int64) == 1) and np.all(got[18].view(np.int64) == 0)
+    np.testing.assert_array_equal(ps.particles[0].x, 0.0)  # the other set is untouched
+    with pytest.raises(RuntimeError):
+        CudaTrackJob(e, ps, 0, config_str="cuda.threads_per_block = 48")
