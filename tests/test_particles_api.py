@@ -80,3 +80,33 @@ def test_pysixtrack_transfer():
         if name != "particle_id":
             assert getattr(q, name)[0] == getattr(p, name)[1], name
     assert q.particle_id[0] == 1
+
+
+def test_stcommon_q_gauss_helpers():
+    """As the reference's tests/python/test_qgauss.py: for q = 1 the
+    q-Gaussian is the normal density (rms sigma) to 1e-16; for q != 1 it
+    integrates to 1 over its support."""
+    from sixtracklib_gb300 import stcommon as sc
+
+    for sigma in (1.0, 2.37):
+        sb = sc.Math_sqrt_beta_from_gauss_sigma(sigma)
+        xs = np.linspace(-4 * sigma, 4 * sigma, 101)
+        ref = np.exp(-0.5 * (xs / sigma) ** 2) / np.sqrt(2 * np.pi * sigma * sigma)
+        got = np.array([sc.Math_q_gauss(x, 1.0, sb) for x in xs])
+        assert np.allclose(ref, got, 1e-16, 1e-16)
+        shifted = np.array([sc.Math_q_gauss(x + 0.3, 1.0, sb, mu=0.3) for x in xs])
+        np.testing.assert_allclose(shifted, got, rtol=1e-12)  # (x + 0.3) - 0.3 != x
+    for q in (0.7, 1.3, 2.0):
+        sb = 1.5
+        lo = max(sc.Math_q_gauss_min_support(q, sb), -200.0)
+        hi = min(sc.Math_q_gauss_max_support(q, sb), 200.0)
+        xs = np.linspace(lo, hi, 400001)
+        vals = np.array([sc.Math_q_gauss(x, q, sb) for x in xs[::50]])
+        integral = np.trapezoid(vals, xs[::50])
+        # q = 2 has 1 / x^2 tails: 2e-3 of it lies beyond +-200
+        assert abs(integral - 1.0) < (5e-3 if q >= 2.0 else 1e-4), (q, integral)
+    assert sc.st_ARCH_BEAM_ELEMENTS_BUFFER_ID.value == 2
+    assert sc.st_ARCH_MIN_USER_DEFINED_BUFFER_ID.value == 1024
+    assert sc.st_Buffer_new is not None and sc.st_NullBuffer is None
+    with pytest.raises(AttributeError):
+        sc.st_Not_a_function
