@@ -420,6 +420,35 @@ int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
+/* Device addresses of a particle set's columns
+ * (particles/particles_addr.h:27-55): num_particles, then the address of
+ * each of the 21 columns in NS(Particles) order. */
+typedef struct st_ParticlesAddr {
+    int64_t num_particles;
+    uint64_t q0, mass0, beta0, gamma0, p0c, s, x, y, px, py, zeta, psigma, delta, rpp, rvv,
+        chi, charge_ratio, particle_id, at_element_id, at_turn, state;
+} st_ParticlesAddr;
+/* common/track_job.h:266-289 and track/track_job_base.h:150-175: the
+ * device addresses of the job's particle sets, for kernels of the caller's
+ * own that work on them in place.  `index` is the object index of a
+ * particle set in the particles buffer; objects the job does not track
+ * have no addresses (NULL).  The addresses stay valid until the job is
+ * reset or deleted.  Status 0 on success, -1 otherwise. */
+bool st_TrackJob_can_fetch_particles_addr(const st_TrackJob *job);
+bool st_TrackJob_has_particles_addr(const st_TrackJob *job);
+int32_t st_TrackJob_fetch_particle_addresses(st_TrackJob *job);
+int32_t st_TrackJob_clear_particle_addresses(st_TrackJob *job, st_buffer_size_t index);
+int32_t st_TrackJob_clear_all_particle_addresses(st_TrackJob *job);
+const st_ParticlesAddr *st_TrackJob_particle_addresses(const st_TrackJob *job,
+                                                        st_buffer_size_t index);
+bool st_TrackJobNew_can_fetch_particle_addresses(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_particle_addresses(const st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_fetch_particle_addresses(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_clear_particle_addresses(st_TrackJobBaseNew *job,
+                                                st_buffer_size_t particle_set_index);
+int32_t st_TrackJobNew_clear_all_particle_addresses(st_TrackJobBaseNew *job);
+const st_ParticlesAddr *st_TrackJobNew_get_particle_addresses(const st_TrackJobBaseNew *job,
+                                                               st_buffer_size_t particle_set_index);
 /* The rest of the TrackJobNew set that maps onto this job
  * (track/track_job_base.h:70-420): construction, reset (0 on success, -1 on
  * failure), buffers and output layout, collect / push flags. */

@@ -54,6 +54,12 @@ _SIGNATURES = {
     "st_TrackJob_has_output_buffer": ([vp], cbool),
     "st_TrackJob_owns_output_buffer": ([vp], cbool),
     "st_TrackJob_is_collecting_particles": ([vp], cbool),
+    "st_TrackJob_can_fetch_particles_addr": ([vp], cbool),
+    "st_TrackJob_has_particles_addr": ([vp], cbool),
+    "st_TrackJob_fetch_particle_addresses": ([vp], i32),
+    "st_TrackJob_clear_particle_addresses": ([vp, u64], i32),
+    "st_TrackJob_clear_all_particle_addresses": ([vp], i32),
+    "st_TrackJob_particle_addresses": ([vp, u64], vp),
     "st_CudaTrackJob_default_threads_per_block": ([vp], u64),
     "st_CudaTrackJob_default_track_threads_per_block": ([vp], u64),
     "st_TrackJob_get_output_buffer": ([vp], vp),

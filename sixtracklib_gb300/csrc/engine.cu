@@ -738,6 +738,9 @@ struct st_TrackJob {
     // the particle buffer's memory, page-locked for direct DMA (or null)
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
+    // device column addresses of the particle sets (fetch_particle_addresses)
+    std::vector<st_ParticlesAddr> paddr;
+    std::vector<bool> paddr_set;
 
     ~st_TrackJob() { release(); }
     void release()
@@ -745,6 +748,8 @@ struct st_TrackJob {
         if (pinned) cudaHostUnregister(pinned);
         pinned = nullptr;
         pinned_bytes = 0;
+        paddr.clear();
+        paddr_set.clear();
         if (d_cols) cudaFree(d_cols);
         if (d_out) cudaFree(d_out);
         d_cols = nullptr;
@@ -1408,6 +1413,84 @@ int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *j)
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *j)
 {
     return (j && transfer_outputs(j, true)) ? 0 : -1;
+}
+bool st_TrackJob_can_fetch_particles_addr(const st_TrackJob *j) { return j && j->d_cols; }
+bool st_TrackJob_has_particles_addr(const st_TrackJob *j)
+{
+    if (!j) return false;
+    for (bool b : j->paddr_set)
+        if (b) return true;
+    return false;
+}
+// The device block holds column c of all tracked particles contiguously:
+// set k's column c starts at d_cols + c * n_total + pset_off[k].
+int32_t st_TrackJob_fetch_particle_addresses(st_TrackJob *j)
+{
+    if (!j || !j->d_cols) return -1;
+    j->paddr.assign(j->psets.size(), st_ParticlesAddr{});
+    j->paddr_set.assign(j->psets.size(), true);
+    for (size_t k = 0; k < j->psets.size(); ++k) {
+        st_ParticlesAddr &a = j->paddr[k];
+        a.num_particles = j->pset_cnt[k];
+        uint64_t *cols = &a.q0;
+        for (int c = 0; c < 21; ++c)
+            cols[c] = (uint64_t)(uintptr_t)(j->d_cols + (size_t)c * j->n_total + j->pset_off[k]);
+    }
+    return 0;
+}
+static int pset_position(const st_TrackJob *j, st_buffer_size_t index)
+{
+    for (size_t k = 0; k < j->psets.size(); ++k)
+        if (j->psets[k] == index) return (int)k;
+    return -1;
+}
+int32_t st_TrackJob_clear_particle_addresses(st_TrackJob *j, st_buffer_size_t index)
+{
+    if (!j) return -1;
+    int const k = pset_position(j, index);
+    if (k < 0 || (size_t)k >= j->paddr_set.size()) return -1;
+    j->paddr_set[k] = false;
+    return 0;
+}
+int32_t st_TrackJob_clear_all_particle_addresses(st_TrackJob *j)
+{
+    if (!j) return -1;
+    j->paddr.clear();
+    j->paddr_set.clear();
+    return 0;
+}
+const st_ParticlesAddr *st_TrackJob_particle_addresses(const st_TrackJob *j,
+                                                        st_buffer_size_t index)
+{
+    if (!j) return nullptr;
+    int const k = pset_position(j, index);
+    if (k < 0 || (size_t)k >= j->paddr_set.size() || !j->paddr_set[k]) return nullptr;
+    return &j->paddr[k];
+}
+bool st_TrackJobNew_can_fetch_particle_addresses(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_can_fetch_particles_addr(j);
+}
+bool st_TrackJobNew_has_particle_addresses(const st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_has_particles_addr(j);
+}
+int32_t st_TrackJobNew_fetch_particle_addresses(st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_fetch_particle_addresses(j);
+}
+int32_t st_TrackJobNew_clear_particle_addresses(st_TrackJobBaseNew *j, st_buffer_size_t i)
+{
+    return st_TrackJob_clear_particle_addresses(j, i);
+}
+int32_t st_TrackJobNew_clear_all_particle_addresses(st_TrackJobBaseNew *j)
+{
+    return st_TrackJob_clear_all_particle_addresses(j);
+}
+const st_ParticlesAddr *st_TrackJobNew_get_particle_addresses(const st_TrackJobBaseNew *j,
+                                                               st_buffer_size_t i)
+{
+    return st_TrackJob_particle_addresses(j, i);
 }
 st_TrackJobBaseNew *st_TrackJobNew_create(const char *arch, const char *cfg)
 {

@@ -262,6 +262,47 @@ class TrackJob:
         self._lib.st_TrackJob_push_particles(self.ptr_st_track_job)
         return self
 
+    # ----------------------- particle addresses (trackjob.py, cuda.py:650-700)
+    @property
+    def can_fetch_particle_addresses(self):
+        return bool(self._lib.st_TrackJob_can_fetch_particles_addr(self.ptr_st_track_job))
+
+    @property
+    def has_particle_addresses(self):
+        return bool(self._lib.st_TrackJob_has_particles_addr(self.ptr_st_track_job))
+
+    def fetch_particle_addresses(self):
+        """Make the device addresses of the job's particle columns
+        available (get_particle_addresses)."""
+        self._last_status = int(
+            self._lib.st_TrackJob_fetch_particle_addresses(self.ptr_st_track_job))
+        if self._last_status != 0:
+            raise RuntimeError("unable to fetch particle addresses")
+        return self
+
+    def clear_particle_addresses(self, particle_set_index=0):
+        self._last_status = int(self._lib.st_TrackJob_clear_particle_addresses(
+            self.ptr_st_track_job, int(particle_set_index)))
+        return self
+
+    def clear_all_particle_addresses(self):
+        self._last_status = int(
+            self._lib.st_TrackJob_clear_all_particle_addresses(self.ptr_st_track_job))
+        return self
+
+    def get_particle_addresses(self, particle_set_index=0):
+        """A copy of the st_ParticlesAddr of particle set
+        ``particle_set_index`` (its object index in the particles buffer):
+        ``num_particles`` and the device address of each column; None when
+        not fetched or not tracked by this job."""
+        ptr = self._lib.st_TrackJob_particle_addresses(self.ptr_st_track_job,
+                                                       int(particle_set_index))
+        if not ptr:
+            return None
+        out = ParticlesAddr()
+        C.memmove(C.addressof(out), ptr, C.sizeof(ParticlesAddr))
+        return out
+
     def _push_output(self):
         """Send the host output buffer to the device copy (trackjob.py:1582)."""
         self._lib.st_TrackJob_push_output(self.ptr_st_track_job)
@@ -498,6 +539,16 @@ class TrackJob:
     def output_particles(self, index) -> Particles:
         """Particles object ``index`` of the output buffer."""
         return self._output_buffer.get_object(index)
+
+
+class ParticlesAddr(C.Structure):
+    """st_ParticlesAddr (particles/particles_addr.h:27-55)."""
+
+    _fields_ = [("num_particles", C.c_int64)] + [
+        (f"{name}_addr", C.c_uint64) for name in (
+            "q0", "mass0", "beta0", "gamma0", "p0c", "s", "x", "y", "px", "py", "zeta",
+            "psigma", "delta", "rpp", "rvv", "chi", "charge_ratio", "particle_id",
+            "at_element_id", "at_turn", "state")]
 
 
 class _StParticles(C.Structure):

@@ -681,3 +681,40 @@ def test_cuda_trackjob_properties_and_track_line(torch_cuda, oracle):
     np.testing.assert_array_equal(ps.particles[0].x, 0.0)  # the other set is untouched
     with pytest.raises(RuntimeError):
         CudaTrackJob(e, ps, 0, config_str="cuda.threads_per_block = 48")
+
+
+def test_trackjob_particle_addresses(torch_cuda, oracle):
+    """Device addresses of the job's particle columns
+    (tests/python/cuda/test_track_job_fetch_particle_addr.py): consistent
+    with the column layout, and usable in place -- tracking the fetched
+    block with the device-resident entry point changes what the job
+    collects."""
+    from sixtracklib_gb300 import ParticlesSet, _native
+    from sixtracklib_gb300.device import DeviceTracker
+    from sixtracklib_gb300.trackjob import CudaTrackJob
+
+    e = lattices.fodo_ring()
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=300)
+    q = lattices.gaussian_particles(300, seed=27)
+    p.set_block(q.block)
+    job = CudaTrackJob(e, ps, 0, config_str="mode=exact")
+    assert job.can_fetch_particle_addresses and not job.has_particle_addresses
+    assert job.get_particle_addresses(0) is None
+    job.fetch_particle_addresses()
+    assert job.last_status_success and job.has_particle_addresses
+    a = job.get_particle_addresses(0)
+    assert a.num_particles == 300 and job.get_particle_addresses(1) is None
+    cols = [getattr(a, f) for f, _ in a._fields_[1:]]
+    assert all(c2 - c1 == 300 * 8 for c1, c2 in zip(cols, cols[1:]))
+    job.track_until(2)
+    trk = DeviceTracker(e, config="mode=exact")
+    lib = _native.load()
+    assert lib.st_DeviceLattice_track_until(trk._ptr, C.c_void_p(a.q0_addr), 300, 5, None) == 0
+    torch_cuda.cuda.synchronize()
+    job.collect_particles()
+    exp = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp, 5)
+    assert_parity(ps.particles[0].block.copy(), exp, tol=1e-13)
+    job.clear_particle_addresses(0)
+    assert not job.has_particle_addresses and job.get_particle_addresses(0) is None
