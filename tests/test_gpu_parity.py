@@ -468,6 +468,18 @@ def test_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
     job.collect_particles()
     assert oracle.track_until(e.cbuffer.to_image(), exp, 10) == 0
     assert_parity(p.block.copy(), exp, tol=1e-12)
+    # reset on fresh particles: the stored tables and their assignment stay
+    ps2 = ParticlesSet()
+    p2 = ps2.Particles(num_particles=256)
+    q2 = lattices.gaussian_particles(256, seed=7, sz=0.12)
+    p2.set_block(q2.block)
+    job.reset(e, ps2)
+    assert job.num_stored_buffers == 1 and job.total_num_assign_items == 6
+    assert job.track_until(4) == 0
+    job.collect_particles()
+    exp2 = q2.block.copy()
+    assert oracle.track_until(e.cbuffer.to_image(), exp2, 4) == 0
+    assert_parity(p2.block.copy(), exp2, tol=1e-13)
 
 
 def test_trackjob_beam_monitor_and_elem_by_elem_output(torch_cuda, oracle):
