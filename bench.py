@@ -55,6 +55,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-element-turns/s"
 WORKLOAD = "synthetic 20k-element ring, 1M particles polar grid, FP64, 1 turn per step"
+# DRAM bytes (read + write) of one tracking launch of the default workload
+# (1M particles, fast, 128 threads, 2 CTAs/SM), measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass; two launches after
+# the warm-up: 120.6 and 118.6 MB; profiles/track_kernel_synthetic_ring_20k.md)
+TRACK_TRAFFIC_BYTES = 1.196e8
 
 
 def parse():
@@ -587,7 +592,11 @@ def run_ours(args):
                    "parallelism": f"particles sharded, {world} independent GPU(s)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak and peak > 0 else None, "traffic": None,
+                     "frac": achieved / peak if peak and peak > 0 else None,
+                     "traffic": (TRACK_TRAFFIC_BYTES if (args.particles, args.mode, args.threads,
+                                                        args.blocks_per_sm) ==
+                                 (1_000_000, "fast", 128, 2) else None),
+                     "traffic_unit": "bytes per launch (ncu capture of this configuration)",
                      "peak_source": "measured in-process: dense DFMA loop (csrc/probe.cu), "
                                     "FMA = 2 flops",
                      "flops_per_pet": flops_per_pet, "launch_ms": avg_launch * 1e3,
