@@ -251,6 +251,32 @@ def test_beam_beam_space_charge_ring(torch_cuda, oracle, elliptic):
             assert_parity(got, exp, tol=tol)
 
 
+@pytest.mark.parametrize("elliptic,turns", [(False, 100), (True, 20)])
+def test_beam_beam_space_charge_full_size(torch_cuda, oracle, elliptic, turns):
+    """The beam-beam and space-charge mix at its full size, 262,144 Gaussian
+    protons: a strided sample of 1,024 agrees with the oracle within 1e-10
+    (loss flags and counters identical), and a particle's result does not
+    depend on its slot (a permuted block gives the permuted result, bit for
+    bit)."""
+    torch = torch_cuda
+    from sixtracklib_gb300.device import DeviceTracker
+
+    e = lattices.bb_sc_ring(elliptic=elliptic)
+    trk = DeviceTracker(e, config="mode=exact")
+    p = lattices.gaussian_particles(262144, seed=41)
+    base = torch.from_numpy(p.block.copy().view(np.int64)).cuda()
+    a = base.clone()
+    assert trk.track_until(a, turns) == 0
+    perm = torch.randperm(base.shape[1], device=base.device)
+    c = base[:, perm].contiguous()
+    assert trk.track_until(c, turns) == 0
+    assert torch.equal(c, a[:, perm])
+    idx = np.arange(0, 262144, 256)
+    sample = p.block[:, idx].copy()
+    assert oracle.track_until(e.cbuffer.to_image(), sample, turns) == 0
+    assert_parity(a.cpu().numpy().view(np.uint64)[:, idx], sample, tol=1e-10)
+
+
 @pytest.mark.parametrize("sigmas", [(2e-3, 1e-3), (1e-3, 2.5e-3), (1.5e-3, 1.5e-3)])
 def test_gaussian_field_kicks(torch_cuda, oracle, sigmas):
     """The Gaussian field itself, one 4D beam-beam element with a strong
