@@ -420,6 +420,70 @@ int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
+/* Stored buffers and address assignment (common/track_job.h: stored
+ * buffers, NS(AssignAddressItem) of buffer/assign_address_item.h).  A stored
+ * buffer is a caller's st_Buffer kept by the job under an id >= 1024
+ * (owned if take_ownership).  An item names a destination pointer field
+ * (buffer id -- 2 for the beam elements, or a stored buffer --, object
+ * index and type id, byte offset) and a source (buffer id -- 1 particles,
+ * 2 beam elements or a stored buffer --, object index and type id, byte
+ * offset); assigning writes the source object's address plus its offset
+ * into the field, after the reference's checks (type ids, sizes, 8-byte
+ * alignment), and recompiles the lattice when the beam elements changed.
+ * The engine reads such an address when it compiles the lattice (an
+ * SCInterpolatedProfile's line-density table), so a stored buffer must
+ * live as long as the job.  Beam monitors write into the job's own output
+ * buffer whatever their out_address says.  Status 0 on success, -1
+ * otherwise; ids / indices are 0 on failure. */
+typedef struct st_AssignAddressItem {
+    uint64_t dest_buffer_id, src_buffer_id, dest_elem_type_id, src_elem_type_id;
+    uint64_t dest_elem_index, src_elem_index, dest_pointer_offset, src_pointer_offset;
+} st_AssignAddressItem;
+st_buffer_size_t st_TrackJob_add_stored_buffer(st_TrackJob *job, st_Buffer *buffer,
+                                               bool take_ownership, bool delete_ptr_after_move);
+st_buffer_size_t st_TrackJob_create_stored_buffer(st_TrackJob *job,
+                                                  st_buffer_size_t buffer_capacity);
+int32_t st_TrackJob_remove_stored_buffer(st_TrackJob *job, st_buffer_size_t buffer_id);
+bool st_TrackJob_has_stored_buffers(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_num_stored_buffers(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_min_stored_buffer_id(const st_TrackJob *job);
+st_buffer_size_t st_TrackJob_max_stored_buffer_id(const st_TrackJob *job);
+bool st_TrackJob_owns_stored_buffer(const st_TrackJob *job, st_buffer_size_t buffer_id);
+st_Buffer *st_TrackJob_stored_buffer(st_TrackJob *job, st_buffer_size_t buffer_id);
+const st_Buffer *st_TrackJob_const_stored_buffer(const st_TrackJob *job,
+                                                 st_buffer_size_t buffer_id);
+int32_t st_TrackJob_push_stored_buffer(st_TrackJob *job, st_buffer_size_t buffer_id);
+int32_t st_TrackJob_collect_stored_buffer(st_TrackJob *job, st_buffer_size_t buffer_id);
+st_AssignAddressItem *st_TrackJob_add_assign_address_item(st_TrackJob *job,
+                                                          const st_AssignAddressItem *item);
+st_AssignAddressItem *st_TrackJob_add_assign_address_item_detailed(
+    st_TrackJob *job, st_object_type_id_t dest_type_id, st_buffer_size_t dest_buffer_id,
+    st_buffer_size_t dest_elem_index, st_buffer_size_t dest_pointer_offset,
+    st_object_type_id_t src_type_id, st_buffer_size_t src_buffer_id,
+    st_buffer_size_t src_elem_index, st_buffer_size_t src_pointer_offset);
+bool st_TrackJob_has_assign_address_item(const st_TrackJob *job,
+                                         const st_AssignAddressItem *item);
+bool st_TrackJob_has_assign_item_by_index(const st_TrackJob *job, st_buffer_size_t dest_buffer_id,
+                                          st_buffer_size_t src_buffer_id,
+                                          st_buffer_size_t assign_item_index);
+bool st_TrackJob_has_assign_items(const st_TrackJob *job, st_buffer_size_t dest_buffer_id,
+                                  st_buffer_size_t src_buffer_id);
+st_buffer_size_t st_TrackJob_index_of_assign_address_item(const st_TrackJob *job,
+                                                          const st_AssignAddressItem *item);
+st_buffer_size_t st_TrackJob_num_assign_items(const st_TrackJob *job,
+                                              st_buffer_size_t dest_buffer_id,
+                                              st_buffer_size_t src_buffer_id);
+st_buffer_size_t st_TrackJob_total_num_assign_items(const st_TrackJob *job);
+const st_AssignAddressItem *st_TrackJob_ptr_assign_address_item(
+    const st_TrackJob *job, const st_AssignAddressItem *item);
+const st_AssignAddressItem *st_TrackJob_ptr_assign_address_item_by_index(
+    const st_TrackJob *job, st_buffer_size_t dest_buffer_id, st_buffer_size_t src_buffer_id,
+    st_buffer_size_t assign_address_item_index);
+int32_t st_TrackJob_commit_address_assignments(st_TrackJob *job);
+int32_t st_TrackJob_assign_all_addresses(st_TrackJob *job);
+int32_t st_TrackJob_assign_addresses(st_TrackJob *job, st_buffer_size_t dest_buffer_id,
+                                     st_buffer_size_t src_buffer_id);
+
 /* Device addresses of a particle set's columns
  * (particles/particles_addr.h:27-55): num_particles, then the address of
  * each of the 21 columns in NS(Particles) order. */

@@ -60,6 +60,30 @@ _SIGNATURES = {
     "st_TrackJob_clear_particle_addresses": ([vp, u64], i32),
     "st_TrackJob_clear_all_particle_addresses": ([vp], i32),
     "st_TrackJob_particle_addresses": ([vp, u64], vp),
+    "st_TrackJob_add_stored_buffer": ([vp, vp, cbool, cbool], u64),
+    "st_TrackJob_create_stored_buffer": ([vp, u64], u64),
+    "st_TrackJob_remove_stored_buffer": ([vp, u64], i32),
+    "st_TrackJob_has_stored_buffers": ([vp], cbool),
+    "st_TrackJob_num_stored_buffers": ([vp], u64),
+    "st_TrackJob_min_stored_buffer_id": ([vp], u64),
+    "st_TrackJob_max_stored_buffer_id": ([vp], u64),
+    "st_TrackJob_owns_stored_buffer": ([vp, u64], cbool),
+    "st_TrackJob_stored_buffer": ([vp, u64], vp),
+    "st_TrackJob_push_stored_buffer": ([vp, u64], i32),
+    "st_TrackJob_collect_stored_buffer": ([vp, u64], i32),
+    "st_TrackJob_add_assign_address_item": ([vp, vp], vp),
+    "st_TrackJob_add_assign_address_item_detailed": ([vp] + [u64] * 8, vp),
+    "st_TrackJob_has_assign_address_item": ([vp, vp], cbool),
+    "st_TrackJob_has_assign_item_by_index": ([vp, u64, u64, u64], cbool),
+    "st_TrackJob_has_assign_items": ([vp, u64, u64], cbool),
+    "st_TrackJob_index_of_assign_address_item": ([vp, vp], u64),
+    "st_TrackJob_num_assign_items": ([vp, u64, u64], u64),
+    "st_TrackJob_total_num_assign_items": ([vp], u64),
+    "st_TrackJob_ptr_assign_address_item": ([vp, vp], vp),
+    "st_TrackJob_ptr_assign_address_item_by_index": ([vp, u64, u64, u64], vp),
+    "st_TrackJob_commit_address_assignments": ([vp], i32),
+    "st_TrackJob_assign_all_addresses": ([vp], i32),
+    "st_TrackJob_assign_addresses": ([vp, u64, u64], i32),
     "st_CudaTrackJob_default_threads_per_block": ([vp], u64),
     "st_CudaTrackJob_default_track_threads_per_block": ([vp], u64),
     "st_TrackJob_get_output_buffer": ([vp], vp),

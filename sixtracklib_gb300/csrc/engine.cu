@@ -17,6 +17,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdlib>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -741,8 +742,19 @@ struct st_TrackJob {
     // device column addresses of the particle sets (fetch_particle_addresses)
     std::vector<st_ParticlesAddr> paddr;
     std::vector<bool> paddr_set;
+    // stored buffers (id -> buffer, owned) and assignment items; kept
+    // across reset, freed with the job
+    std::map<uint64_t, std::pair<st_Buffer *, bool>> stored;
+    uint64_t next_stored_id = 1024;
+    std::deque<st_AssignAddressItem> assign_items;
 
-    ~st_TrackJob() { release(); }
+    ~st_TrackJob()
+    {
+        release();
+        for (auto &kv : stored)
+            if (kv.second.second && kv.second.first) st_Buffer_delete(kv.second.first);
+        stored.clear();
+    }
     void release()
     {
         if (pinned) cudaHostUnregister(pinned);
@@ -1414,6 +1426,245 @@ int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *j)
 {
     return (j && transfer_outputs(j, true)) ? 0 : -1;
 }
+// ------------------------------------------ stored buffers, address items
+st_buffer_size_t st_TrackJob_add_stored_buffer(st_TrackJob *j, st_Buffer *b, bool own, bool)
+{
+    if (!j || !b) return 0;
+    uint64_t const id = j->next_stored_id++;
+    j->stored[id] = {b, own};
+    return id;
+}
+st_buffer_size_t st_TrackJob_create_stored_buffer(st_TrackJob *j, st_buffer_size_t cap)
+{
+    if (!j) return 0;
+    st_Buffer *b = st_Buffer_new(cap);
+    if (!b) return 0;
+    return st_TrackJob_add_stored_buffer(j, b, true, true);
+}
+int32_t st_TrackJob_remove_stored_buffer(st_TrackJob *j, st_buffer_size_t id)
+{
+    if (!j) return -1;
+    auto it = j->stored.find(id);
+    if (it == j->stored.end()) return -1;
+    if (it->second.second && it->second.first) st_Buffer_delete(it->second.first);
+    j->stored.erase(it);
+    return 0;
+}
+bool st_TrackJob_has_stored_buffers(const st_TrackJob *j) { return j && !j->stored.empty(); }
+st_buffer_size_t st_TrackJob_num_stored_buffers(const st_TrackJob *j)
+{
+    return j ? j->stored.size() : 0;
+}
+st_buffer_size_t st_TrackJob_min_stored_buffer_id(const st_TrackJob *j)
+{
+    return (j && !j->stored.empty()) ? j->stored.begin()->first : 0;
+}
+st_buffer_size_t st_TrackJob_max_stored_buffer_id(const st_TrackJob *j)
+{
+    return (j && !j->stored.empty()) ? j->stored.rbegin()->first : 0;
+}
+bool st_TrackJob_owns_stored_buffer(const st_TrackJob *j, st_buffer_size_t id)
+{
+    if (!j) return false;
+    auto it = j->stored.find(id);
+    return it != j->stored.end() && it->second.second;
+}
+st_Buffer *st_TrackJob_stored_buffer(st_TrackJob *j, st_buffer_size_t id)
+{
+    if (!j) return nullptr;
+    auto it = j->stored.find(id);
+    return it != j->stored.end() ? it->second.first : nullptr;
+}
+const st_Buffer *st_TrackJob_const_stored_buffer(const st_TrackJob *j, st_buffer_size_t id)
+{
+    return st_TrackJob_stored_buffer(const_cast<st_TrackJob *>(j), id);
+}
+
+static bool same_item(const st_AssignAddressItem &a, const st_AssignAddressItem &b)
+{
+    return std::memcmp(&a, &b, sizeof(a)) == 0;
+}
+static bool pair_of(const st_AssignAddressItem &a, uint64_t dest, uint64_t src)
+{
+    return a.dest_buffer_id == dest && a.src_buffer_id == src;
+}
+// The st_Buffer a buffer id names: 1 particles, 2 beam elements, 3 output,
+// >= 1024 stored.
+static st_Buffer *buffer_of(st_TrackJob *j, uint64_t id)
+{
+    if (id == 1) return j->pbuf;
+    if (id == 2) return j->ebuf;
+    if (id == 3) return j->obuf;
+    auto it = j->stored.find(id);
+    return it != j->stored.end() ? it->second.first : nullptr;
+}
+// Address of (object `index`, byte `off`) of buffer `b` if the object has
+// the type `tid` and holds 8 bytes at `off`; 0 otherwise
+// (buffer/assign_address_item.h: *_from_managed_buffer).
+static uint64_t field_addr(st_Buffer *b, uint64_t index, uint64_t tid, uint64_t off)
+{
+    if (!b || index >= st_Buffer_get_num_of_objects(b)) return 0;
+    const st_Object &o = st_Buffer_get_const_objects_begin(b)[index];
+    uint64_t const a = o.begin_addr + off;
+    if (o.begin_addr == 0 || o.type_id != tid || o.size < off + 8 || a % 8 != 0) return 0;
+    return a;
+}
+
+st_AssignAddressItem *st_TrackJob_add_assign_address_item(st_TrackJob *j,
+                                                          const st_AssignAddressItem *item)
+{
+    if (!j || !item) return nullptr;
+    for (auto &it : j->assign_items)
+        if (same_item(it, *item)) return &it;
+    j->assign_items.push_back(*item);
+    return &j->assign_items.back();
+}
+st_AssignAddressItem *st_TrackJob_add_assign_address_item_detailed(
+    st_TrackJob *j, st_object_type_id_t dt, st_buffer_size_t db, st_buffer_size_t di,
+    st_buffer_size_t doff, st_object_type_id_t stid, st_buffer_size_t sb, st_buffer_size_t si,
+    st_buffer_size_t soff)
+{
+    st_AssignAddressItem const it{db, sb, dt, stid, di, si, doff, soff};
+    return st_TrackJob_add_assign_address_item(j, &it);
+}
+const st_AssignAddressItem *st_TrackJob_ptr_assign_address_item(const st_TrackJob *j,
+                                                                 const st_AssignAddressItem *item)
+{
+    if (!j || !item) return nullptr;
+    for (auto const &it : j->assign_items)
+        if (same_item(it, *item)) return &it;
+    return nullptr;
+}
+bool st_TrackJob_has_assign_address_item(const st_TrackJob *j, const st_AssignAddressItem *item)
+{
+    return st_TrackJob_ptr_assign_address_item(j, item) != nullptr;
+}
+st_buffer_size_t st_TrackJob_num_assign_items(const st_TrackJob *j, st_buffer_size_t dest,
+                                              st_buffer_size_t src)
+{
+    if (!j) return 0;
+    st_buffer_size_t n = 0;
+    for (auto const &it : j->assign_items) n += pair_of(it, dest, src) ? 1 : 0;
+    return n;
+}
+bool st_TrackJob_has_assign_items(const st_TrackJob *j, st_buffer_size_t dest,
+                                  st_buffer_size_t src)
+{
+    return st_TrackJob_num_assign_items(j, dest, src) > 0;
+}
+st_buffer_size_t st_TrackJob_total_num_assign_items(const st_TrackJob *j)
+{
+    return j ? j->assign_items.size() : 0;
+}
+const st_AssignAddressItem *st_TrackJob_ptr_assign_address_item_by_index(
+    const st_TrackJob *j, st_buffer_size_t dest, st_buffer_size_t src, st_buffer_size_t index)
+{
+    if (!j) return nullptr;
+    st_buffer_size_t k = 0;
+    for (auto const &it : j->assign_items)
+        if (pair_of(it, dest, src) && k++ == index) return &it;
+    return nullptr;
+}
+bool st_TrackJob_has_assign_item_by_index(const st_TrackJob *j, st_buffer_size_t dest,
+                                          st_buffer_size_t src, st_buffer_size_t index)
+{
+    return st_TrackJob_ptr_assign_address_item_by_index(j, dest, src, index) != nullptr;
+}
+// Index among the items of the item's (dest, src) pair; that pair's count
+// when the item is not there.
+st_buffer_size_t st_TrackJob_index_of_assign_address_item(const st_TrackJob *j,
+                                                          const st_AssignAddressItem *item)
+{
+    if (!j || !item) return 0;
+    st_buffer_size_t k = 0;
+    for (auto const &it : j->assign_items) {
+        if (!pair_of(it, item->dest_buffer_id, item->src_buffer_id)) continue;
+        if (same_item(it, *item)) return k;
+        ++k;
+    }
+    return k;
+}
+int32_t st_TrackJob_commit_address_assignments(st_TrackJob *j)
+{
+    if (!j) return -1;
+    clear_error();
+    for (auto const &it : j->assign_items) {
+        st_Buffer *d = buffer_of(j, it.dest_buffer_id), *s = buffer_of(j, it.src_buffer_id);
+        if (!d || !s || it.dest_elem_index >= st_Buffer_get_num_of_objects(d) ||
+            it.src_elem_index >= st_Buffer_get_num_of_objects(s)) {
+            set_error("TrackJob: an assignment item names a missing buffer or object");
+            return -1;
+        }
+    }
+    return 0;
+}
+static int32_t assign(st_TrackJob *j, bool all, uint64_t dest, uint64_t src)
+{
+    if (!j) return -1;
+    clear_error();
+    bool lattice = false;
+    for (auto const &it : j->assign_items) {
+        if (!all && !pair_of(it, dest, src)) continue;
+        uint64_t const sa = field_addr(buffer_of(j, it.src_buffer_id), it.src_elem_index,
+                                       it.src_elem_type_id, it.src_pointer_offset);
+        uint64_t const da = field_addr(buffer_of(j, it.dest_buffer_id), it.dest_elem_index,
+                                       it.dest_elem_type_id, it.dest_pointer_offset);
+        if (!sa || !da || it.dest_buffer_id == 1) {
+            set_error("TrackJob: an assignment item does not match its objects");
+            return -1;
+        }
+        *(uint64_t *)(uintptr_t)da = sa;
+        lattice = lattice || it.dest_buffer_id == 2;
+    }
+    if (lattice && !compile_job_lattice(j)) return -1;
+    return 0;
+}
+int32_t st_TrackJob_assign_all_addresses(st_TrackJob *j) { return assign(j, true, 0, 0); }
+int32_t st_TrackJob_assign_addresses(st_TrackJob *j, st_buffer_size_t dest, st_buffer_size_t src)
+{
+    return assign(j, false, dest, src);
+}
+// The engine reads stored buffers from host memory when it compiles the
+// lattice: a push recompiles when an item reads this buffer.
+int32_t st_TrackJob_push_stored_buffer(st_TrackJob *j, st_buffer_size_t id)
+{
+    if (!j || !st_TrackJob_stored_buffer(j, id)) return -1;
+    for (auto const &it : j->assign_items)
+        if (it.src_buffer_id == id && it.dest_buffer_id == 2)
+            return compile_job_lattice(j) ? 0 : -1;
+    return 0;
+}
+// The engine writes a stored buffer only through BeamMonitors whose
+// out_address was assigned from it: the monitor's turn-by-turn records (the
+// job's own monitor output, in the reference's layout) are copied into the
+// assigned particle set, as many particles as both hold.
+int32_t st_TrackJob_collect_stored_buffer(st_TrackJob *j, st_buffer_size_t id)
+{
+    st_Buffer *sb = j ? st_TrackJob_stored_buffer(j, id) : nullptr;
+    if (!sb) return -1;
+    bool collected = false;
+    for (auto const &it : j->assign_items) {
+        if (it.src_buffer_id != id || it.dest_buffer_id != 2 ||
+            it.dest_elem_type_id != ST_OBJECT_TYPE_BEAM_MONITOR)
+            continue;
+        auto mb = j->monitor_block.find(it.dest_elem_index);
+        if (mb == j->monitor_block.end()) continue;
+        if (!collected) {
+            st_TrackJob_collect_output(j);
+            collected = true;
+        }
+        const st_Particles *src =
+            st_Particles_buffer_get_particles(j->obuf, j->outs[mb->second].obj_index);
+        st_Particles *dst = st_Particles_buffer_get_particles(sb, it.src_elem_index);
+        if (!src || !dst) continue;
+        int64_t const n = std::min(src->num_particles, dst->num_particles);
+        std::vector<uint64_t> blk((size_t)n * 21);
+        gather(src, 0, n, blk.data());
+        scatter(dst, 0, n, blk.data());
+    }
+    return 0;
+}
+
 bool st_TrackJob_can_fetch_particles_addr(const st_TrackJob *j) { return j && j->d_cols; }
 bool st_TrackJob_has_particles_addr(const st_TrackJob *j)
 {

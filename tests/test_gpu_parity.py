@@ -756,3 +756,132 @@ def test_trackjob_particle_addresses(torch_cuda, oracle):
     assert_parity(ps.particles[0].block.copy(), exp, tol=1e-13)
     job.clear_particle_addresses(0)
     assert not job.has_particle_addresses and job.get_particle_addresses(0) is None
+
+
+class _StAssignItem(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "dest_buffer_id", "src_buffer_id", "dest_elem_type_id", "src_elem_type_id",
+        "dest_elem_index", "src_elem_index", "dest_pointer_offset", "src_pointer_offset")]
+
+
+def _c_image(lib, ptr):
+    n = lib.st_Buffer_get_size(ptr)
+    data = lib.st_Buffer_get_const_data_begin(ptr)
+    return np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint64)), shape=(n // 8,)).copy()
+
+
+def test_c_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
+    """The C functions for stored buffers and assignment items
+    (common/track_job.h, NS(TrackJob_add_stored_buffer) ...
+    NS(TrackJob_assign_all_addresses)) on one C TrackJob: ids and
+    ownership, item bookkeeping, line-density tables assigned from a stored
+    buffer to interpolated space-charge kicks (tracked result equal to the
+    oracle on the job's lattice, different from the fallback density),
+    refused items, and a BeamMonitor writing into a stored particle set."""
+    from sixtracklib_gb300 import ParticlesSet, _native
+    from sixtracklib_gb300.beam_elements import (TYPE_BEAM_MONITOR, TYPE_LINE_DENSITY_PROF_DATA,
+                                                 TYPE_SC_INTERPOLATED_PROF)
+    from sixtracklib_gb300.particles import TYPE_PARTICLE
+    from tests import capi
+
+    L = _native.load()
+    z = np.linspace(-0.3, 0.3, 41)
+    prof = np.exp(-0.5 * (z / 0.1) ** 2) * 1e12
+    tables = Elements()
+    tables.LineDensityProfileData(values=prof, z0=-0.3, dz=float(z[1] - z[0]), method="linear")
+    tables.LineDensityProfileData(values=prof * 1.1, z0=-0.3, dz=float(z[1] - z[0]),
+                                  method="cubic")
+    e = lattices.fodo_ring()
+    first = len(e)
+    for k in range(6):
+        e.SCInterpolatedProfile(number_of_particles=1e11, length=0.5, sigma_x=1e-3,
+                                sigma_y=1.2e-3 if k % 2 else 1e-3, interpol_data_addr=0,
+                                line_density_prof_fallback=5e11, min_sigma_diff=1e-10)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=256)
+    q = lattices.gaussian_particles(256, seed=31, sz=0.12)
+    p.set_block(q.block)
+    pb = capi.c_buffer_from_image(ps.cbuffer.to_image())
+    eb = capi.c_buffer_from_image(e.cbuffer.to_image())
+    sb = capi.c_buffer_from_image(tables.cbuffer.to_image())
+    idx = (C.c_uint64 * 1)(0)
+    job = L.st_TrackJob_new_detailed(b"cuda", pb, 1, idx, eb, None, 0, b"mode=exact")
+    assert job, _native.last_error()
+
+    assert not L.st_TrackJob_has_stored_buffers(job) and L.st_TrackJob_min_stored_buffer_id(job) == 0
+    bid = L.st_TrackJob_add_stored_buffer(job, sb, False, False)
+    assert bid == 1024 and L.st_TrackJob_create_stored_buffer(job, 256) == 1025
+    assert L.st_TrackJob_owns_stored_buffer(job, 1025) and not L.st_TrackJob_owns_stored_buffer(job, 1024)
+    assert L.st_TrackJob_stored_buffer(job, 1024) == sb and L.st_TrackJob_num_stored_buffers(job) == 2
+    assert L.st_TrackJob_remove_stored_buffer(job, 1025) == 0
+    assert L.st_TrackJob_remove_stored_buffer(job, 1025) == -1
+    assert (L.st_TrackJob_min_stored_buffer_id(job), L.st_TrackJob_max_stored_buffer_id(job)) == (1024, 1024)
+
+    ptrs = [L.st_TrackJob_add_assign_address_item_detailed(
+        job, TYPE_SC_INTERPOLATED_PROF, 2, first + k, 48, TYPE_LINE_DENSITY_PROF_DATA, bid, k % 2, 0)
+        for k in range(6)]
+    assert all(ptrs)
+    again = _StAssignItem(2, bid, TYPE_SC_INTERPOLATED_PROF, TYPE_LINE_DENSITY_PROF_DATA,
+                          first + 3, 1, 48, 0)
+    assert L.st_TrackJob_add_assign_address_item(job, C.byref(again)) == ptrs[3]
+    assert L.st_TrackJob_total_num_assign_items(job) == 6
+    assert L.st_TrackJob_num_assign_items(job, 2, bid) == 6 and L.st_TrackJob_has_assign_items(job, 2, bid)
+    assert not L.st_TrackJob_has_assign_items(job, 2, 1)
+    assert L.st_TrackJob_has_assign_item_by_index(job, 2, bid, 5)
+    assert not L.st_TrackJob_has_assign_item_by_index(job, 2, bid, 6)
+    assert L.st_TrackJob_has_assign_address_item(job, C.byref(again))
+    assert L.st_TrackJob_index_of_assign_address_item(job, C.byref(again)) == 3
+    assert L.st_TrackJob_ptr_assign_address_item_by_index(job, 2, bid, 3) == ptrs[3]
+    assert L.st_TrackJob_commit_address_assignments(job) == 0
+    assert L.st_TrackJob_assign_all_addresses(job) == 0, _native.last_error()
+    obj = C.cast(L.st_Buffer_get_const_object(sb, 1), C.POINTER(C.c_uint64))
+    sc = C.cast(L.st_Buffer_get_const_object(eb, first + 3), C.POINTER(C.c_uint64))
+    assert C.cast(sc[0] + 48, C.POINTER(C.c_uint64))[0] == obj[0]
+
+    assert L.st_TrackJob_track_until(job, 5) == 0
+    L.st_TrackJob_collect_particles(job)
+    img = _c_image(L, eb)
+    exp = q.block.copy()
+    assert oracle.track_until(img, exp, 5) == 0
+    assert_parity(capi_columns(pb), exp, tol=1e-13)
+    fallback = q.block.copy()
+    assert oracle.track_until(e.cbuffer.to_image(), fallback, 5) == 0
+    assert not np.array_equal(exp, fallback)
+
+    # an item whose source object does not exist is refused at commit and assignment
+    L.st_TrackJob_add_assign_address_item_detailed(
+        job, TYPE_SC_INTERPOLATED_PROF, 2, first, 48, TYPE_LINE_DENSITY_PROF_DATA, bid, 7, 0)
+    assert L.st_TrackJob_commit_address_assignments(job) == -1
+    assert L.st_TrackJob_assign_addresses(job, 2, bid) == -1
+    L.st_TrackJob_delete(job)
+
+    # a BeamMonitor writing into a particle set of a stored buffer
+    e2 = lattices.fodo_ring()
+    bm = len(e2)
+    e2.BeamMonitor(num_stores=4, start=0, skip=1, is_rolling=0, is_turn_ordered=1)
+    out = ParticlesSet()
+    out.Particles(num_particles=4 * 256)
+    pb2 = capi.c_buffer_from_image(ps.cbuffer.to_image())
+    eb2 = capi.c_buffer_from_image(e2.cbuffer.to_image())
+    ob = capi.c_buffer_from_image(out.cbuffer.to_image())
+    job = L.st_TrackJob_new_detailed(b"cuda", pb2, 1, idx, eb2, None, 0, b"mode=exact")
+    assert job, _native.last_error()
+    oid = L.st_TrackJob_add_stored_buffer(job, ob, True, True)
+    assert L.st_TrackJob_owns_stored_buffer(job, oid)
+    assert L.st_TrackJob_add_assign_address_item_detailed(
+        job, TYPE_BEAM_MONITOR, 2, bm, 24, TYPE_PARTICLE, oid, 0, 0)
+    assert L.st_TrackJob_assign_addresses(job, 2, oid) == 0, _native.last_error()
+    assert L.st_TrackJob_track_until(job, 4) == 0
+    assert L.st_TrackJob_collect_stored_buffer(job, oid) == 0
+    got = capi_columns(ob)
+    outb = L.st_TrackJob_get_output_buffer(job)
+    off = L.st_TrackJob_get_beam_monitor_output_buffer_offset(job)
+    from sixtracklib_gb300.trackjob import _c_columns
+
+    mon = _c_columns(L, outb, off)
+    assert np.array_equal(got, mon)
+    assert set(np.unique(got[19].view(np.int64))) == {0, 1, 2, 3}  # at_turn
+    assert np.count_nonzero(got[6]) > 800  # x
+    L.st_TrackJob_delete(job)  # frees the owned stored buffer
+    for b in (pb, eb, sb, pb2, eb2):
+        L.st_Buffer_delete(b)
