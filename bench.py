@@ -196,10 +196,27 @@ def cpu_baseline(ring, parts, seconds, threads=None):
     st1 = b[20].view(np.int64)
     e1 = b[18].view(np.int64)
     pet = int((alive0 * t1 * n_elem).sum() + ((alive0 & (st1 == 0)) * (e1 + 1)).sum())
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": pet / dt, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"{n} particles (strided) x {turns} turns of the same ring, "
-                      f"{pet:.3e} PET in {dt:.2f} s; oracle/oracle.c, OpenMP over particles"}
+    cores = orc.set_num_threads(0)
+    out = {"value": pet / dt, "unit": METRIC, "cores": cores, "kind": "port",
+           "sample": f"{n} particles (strided) x {turns} turns of the same ring, "
+                     f"{pet:.3e} PET in {dt:.2f} s; oracle/oracle.c, OpenMP over particles"}
+    # one host thread on the first 1,024 particles of the sample, one turn
+    one = sample[:, :1024].copy()
+    orc.set_num_threads(1)
+    try:
+        t = time.perf_counter()
+        orc.track_until(lat, one, 1)
+        dt1 = time.perf_counter() - t
+    finally:
+        orc.set_num_threads(cores)
+    alive1 = sample[20, :1024].view(np.int64) == 1
+    st = one[20].view(np.int64)
+    pet1 = int((alive1 * one[19].view(np.int64) * n_elem).sum() +
+               ((alive1 & (st == 0)) * (one[18].view(np.int64) + 1)).sum())
+    out["single_thread"] = {"value": pet1 / dt1, "cores": 1,
+                            "sample": f"{one.shape[1]} particles x 1 turn, {pet1:.3e} PET "
+                                      f"in {dt1:.2f} s"}
+    return out
 
 
 # ------------------------------------------------------------------- e2e

@@ -13,6 +13,22 @@
 #include <math.h>
 #include <stddef.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Host threads of the particle loops (all cores by default); returns the
+ * number the loops will use. */
+int orc_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
 
 /* ---------------------------------------------------------------- consts */
 /* sixtracklib/common/constants.h:10-35, internal/physics_constants.h:28-70 */

@@ -52,6 +52,9 @@ typedef struct orc_monitor_outputs {
 
 /* Global aperture mode after Drift/DriftExact: 2 always, 1 conditional on
  * length >= min_length, 0 never (SIXTRL_APERTURE_CHECK_AT_DRIFT). */
+/* Host threads of the particle loops; returns the number in use. */
+int orc_set_num_threads(int n);
+
 void orc_set_aperture_mode(int mode, double min_length, double x_limit,
                            double y_limit);
 

@@ -121,6 +121,12 @@ class Oracle:
         mo = MonitorOutputs(len(arrs), cols, caps)
         return mo, (arrs, cols, caps)
 
+    def set_num_threads(self, n: int) -> int:
+        """Host threads of the oracle's particle loops; returns the number in use."""
+        fn = self.lib.orc_set_num_threads
+        fn.argtypes, fn.restype = [C.c_int], C.c_int
+        return int(fn(int(n)))
+
     def set_aperture_mode(self, mode=2, min_length=0.0, x_limit=1.0, y_limit=1.0):
         self.lib.orc_set_aperture_mode(int(mode), float(min_length), float(x_limit),
                                        float(y_limit))
