@@ -885,3 +885,61 @@ def test_c_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
     L.st_TrackJob_delete(job)  # frees the owned stored buffer
     for b in (pb, eb, sb, pb2, eb2):
         L.st_Buffer_delete(b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("aperture,min_length,limits", [
+    ("always", 0.0, (1.0, 1.0)), ("conditional", 5.0, (1.0, 1.0)),
+    ("conditional", 11.0, (1.0, 1.0)), ("never", 0.0, (1.0, 1.0)),
+    ("always", 0.0, (0.5, 0.8))])
+def test_global_aperture_over_drifts(torch_cuda, oracle, aperture, min_length, limits):
+    """100 particles over 10,000 drifts of 10 m
+    (common/test_particles_aperture_c99.cpp:30-122): with the global
+    aperture checked after a drift, a particle is lost exactly at the first
+    drift that takes |x| or |y| beyond the limit, and never otherwise; the
+    same for the conditional check (drifts at least `aperture_min_length`
+    long) and custom limits.  Bit-identical to the oracle set up alike."""
+    from sixtracklib_gb300.device import DeviceTracker
+
+    e = Elements()
+    for _ in range(10_000):
+        e.Drift(length=10.0)
+    rng = np.random.default_rng(30)
+    p = lattices.gaussian_particles(100, seed=30)
+    p.x[:], p.y[:] = rng.normal(0, 1e-3, 100), rng.normal(0, 1e-3, 100)
+    p.px[:], p.py[:] = rng.uniform(-2e-5, 2e-5, 100), rng.uniform(-1.5e-5, 1.5e-5, 100)
+    lat = e.cbuffer.to_image()
+    xl, yl = limits
+    mode = {"always": 2, "conditional": 1, "never": 0}[aperture]
+    oracle.set_aperture_mode(mode, min_length, xl, yl)
+    try:
+        exp = p.block.copy()
+        s0 = oracle.track_until(lat, exp, 1)
+    finally:
+        oracle.set_aperture_mode()
+    trk = DeviceTracker(lat, config=f"mode=exact aperture={aperture} "
+                                    f"aperture_min_length={min_length} x_limit={xl} y_limit={yl}")
+    cols = torch_cuda.from_numpy(p.block.copy().view(np.int64)).cuda()
+    st = trk.track_until(cols, 1)
+    torch_cuda.cuda.synchronize()
+    got = cols.cpu().numpy().view(np.uint64)
+    assert st == s0 == 0
+    assert_parity(got, exp, 0.0, bit_exact=True)
+    state = got[20].view(np.int64)
+    checked = mode == 2 or (mode == 1 and 10.0 >= min_length)
+    if not checked:
+        assert np.all(state == 1)
+        return
+    lost = state == 0
+    assert 10 < lost.sum() < 100
+    x, y = got[6].view(np.float64), got[7].view(np.float64)
+    px, py = p.px * p.rpp, p.py * p.rpp
+    # lost particles keep the coordinates past the limit at their drift
+    assert np.all((np.abs(x[lost]) > xl) | (np.abs(y[lost]) > yl))
+    assert np.all((np.abs(x[~lost]) <= xl) & (np.abs(y[~lost]) <= yl))
+    # ... and the first drift to cross it, from the straight-line orbit
+    k = got[18].view(np.int64)[lost]
+    x0, y0 = p.x[lost], p.y[lost]
+    before = (k * 10.0)
+    assert np.all((np.abs(x0 + px[lost] * before) <= xl * (1 + 1e-9)) &
+                  (np.abs(y0 + py[lost] * before) <= yl * (1 + 1e-9)))
