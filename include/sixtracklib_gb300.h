@@ -422,8 +422,11 @@ int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
 /* Stored buffers and address assignment (common/track_job.h: stored
  * buffers, NS(AssignAddressItem) of buffer/assign_address_item.h).  A stored
- * buffer is a caller's st_Buffer kept by the job under an id >= 1024
- * (owned if take_ownership).  An item names a destination pointer field
+ * buffer is a caller's st_Buffer kept by the job under an id >= 1024.  With
+ * take_ownership its contents move into a buffer of the job's (object
+ * addresses unchanged; st_TrackJob_stored_buffer returns the new handle),
+ * the caller's buffer is left empty and is deleted if
+ * delete_ptr_after_move; owned buffers are deleted with the job.  An item names a destination pointer field
  * (buffer id -- 2 for the beam elements, or a stored buffer --, object
  * index and type id, byte offset) and a source (buffer id -- 1 particles,
  * 2 beam elements or a stored buffer --, object index and type id, byte

@@ -397,6 +397,24 @@ uint64_t stg_buffer_generation(const st_Buffer *b) { return b ? b->generation : 
 
 }  // extern "C"
 
+st_Buffer *stg::buffer_take_contents(st_Buffer *b)
+{
+    if (!b) return nullptr;
+    st_Buffer *empty = st_Buffer_new(0);
+    if (!empty) return nullptr;
+    st_Buffer *n = new (std::nothrow) st_Buffer(*b);
+    if (!n) {
+        st_Buffer_delete(empty);
+        return nullptr;
+    }
+    uint64_t const gen = b->generation;
+    *b = *empty;  // b takes the fresh empty layout; `empty` gives up its memory
+    b->generation = gen + 1;
+    empty->mem = nullptr;
+    delete empty;
+    return n;
+}
+
 // ------------------------------------------------------------ elements
 namespace {
 

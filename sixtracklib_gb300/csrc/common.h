@@ -14,6 +14,11 @@ namespace stg {
 void set_error(const std::string &msg);
 void clear_error();
 
+// A new st_Buffer holding b's contents (same memory, so object addresses
+// are unchanged); b is left a valid empty buffer.  Null on failure, with b
+// untouched (buffer.hpp: MAKE_FROM_CBUFFER_AND_TAKE_OWNERSHIP).
+st_Buffer *buffer_take_contents(st_Buffer *b);
+
 inline double w2d(uint64_t w)
 {
     double d;

@@ -1427,11 +1427,22 @@ int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *j)
     return (j && transfer_outputs(j, true)) ? 0 : -1;
 }
 // ------------------------------------------ stored buffers, address items
-st_buffer_size_t st_TrackJob_add_stored_buffer(st_TrackJob *j, st_Buffer *b, bool own, bool)
+// Without ownership the job keeps the caller's pointer.  With ownership the
+// contents move into a buffer of the job's (object addresses unchanged), the
+// caller's buffer is left empty and is deleted if delete_ptr_after_move
+// (track_job_buffer_store.cpp:255-283).
+st_buffer_size_t st_TrackJob_add_stored_buffer(st_TrackJob *j, st_Buffer *b, bool own,
+                                               bool delete_ptr_after_move)
 {
     if (!j || !b) return 0;
+    st_Buffer *kept = b;
+    if (own) {
+        kept = buffer_take_contents(b);
+        if (!kept) return 0;
+        if (delete_ptr_after_move) st_Buffer_delete(b);
+    }
     uint64_t const id = j->next_stored_id++;
-    j->stored[id] = {b, own};
+    j->stored[id] = {kept, own};
     return id;
 }
 st_buffer_size_t st_TrackJob_create_stored_buffer(st_TrackJob *j, st_buffer_size_t cap)
@@ -1439,7 +1450,9 @@ st_buffer_size_t st_TrackJob_create_stored_buffer(st_TrackJob *j, st_buffer_size
     if (!j) return 0;
     st_Buffer *b = st_Buffer_new(cap);
     if (!b) return 0;
-    return st_TrackJob_add_stored_buffer(j, b, true, true);
+    uint64_t const id = j->next_stored_id++;
+    j->stored[id] = {b, true};
+    return id;
 }
 int32_t st_TrackJob_remove_stored_buffer(st_TrackJob *j, st_buffer_size_t id)
 {

@@ -815,6 +815,15 @@ def test_c_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
     assert L.st_TrackJob_stored_buffer(job, 1024) == sb and L.st_TrackJob_num_stored_buffers(job) == 2
     assert L.st_TrackJob_remove_stored_buffer(job, 1025) == 0
     assert L.st_TrackJob_remove_stored_buffer(job, 1025) == -1
+    # taking ownership without deleting: the contents move, the caller's buffer is empty
+    moved = capi.c_buffer_from_image(tables.cbuffer.to_image())
+    first_obj = int(C.cast(L.st_Buffer_get_const_object(moved, 0), C.POINTER(C.c_uint64))[0])
+    mid = L.st_TrackJob_add_stored_buffer(job, moved, True, False)
+    kept = L.st_TrackJob_stored_buffer(job, mid)
+    assert mid == 1026 and kept != moved and L.st_Buffer_get_num_of_objects(moved) == 0
+    assert int(C.cast(L.st_Buffer_get_const_object(kept, 0), C.POINTER(C.c_uint64))[0]) == first_obj
+    L.st_Buffer_delete(moved)
+    assert L.st_TrackJob_remove_stored_buffer(job, mid) == 0
     assert (L.st_TrackJob_min_stored_buffer_id(job), L.st_TrackJob_max_stored_buffer_id(job)) == (1024, 1024)
 
     ptrs = [L.st_TrackJob_add_assign_address_item_detailed(
@@ -866,8 +875,10 @@ def test_c_trackjob_stored_buffers_and_address_assignment(torch_cuda, oracle):
     ob = capi.c_buffer_from_image(out.cbuffer.to_image())
     job = L.st_TrackJob_new_detailed(b"cuda", pb2, 1, idx, eb2, None, 0, b"mode=exact")
     assert job, _native.last_error()
-    oid = L.st_TrackJob_add_stored_buffer(job, ob, True, True)
+    oid = L.st_TrackJob_add_stored_buffer(job, ob, True, True)  # `ob` is deleted
     assert L.st_TrackJob_owns_stored_buffer(job, oid)
+    ob = L.st_TrackJob_stored_buffer(job, oid)
+    assert L.st_Buffer_get_num_of_objects(ob) == 1
     assert L.st_TrackJob_add_assign_address_item_detailed(
         job, TYPE_BEAM_MONITOR, 2, bm, 24, TYPE_PARTICLE, oid, 0, 0)
     assert L.st_TrackJob_assign_addresses(job, 2, oid) == 0, _native.last_error()
