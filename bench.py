@@ -602,7 +602,9 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded lattice and particles)",
-        "config": {"workload": WORKLOAD, "particles_per_gpu": args.particles,
+        "config": {"workload": (WORKLOAD if args.particles == 1_000_000 else
+                                WORKLOAD.replace("1M particles", f"{args.particles} particles")),
+                   "particles_per_gpu": args.particles,
                    "lattice_elements": n_elem, "turns_per_step": 1, "mode": args.mode,
                    "threads_per_block": args.threads, "blocks_per_sm": args.blocks_per_sm,
                    "l2": "inputs larger than L2: 168 MB particle columns per GPU",

@@ -53,6 +53,24 @@ def build_reference(ref_root: str | None = None) -> str | None:
     return REF_LIB
 
 
+def build_reference_cuda(ref_root: str | None = None) -> str | None:
+    """Run oracle/build_ref_cuda.sh (the reference's CUDA kernels as an
+    sm_103a cubin) when the reference sources are present and the cubin is
+    missing or older than its recipe."""
+    root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
+    if not os.path.exists(os.path.join(root, "sixtracklib/cuda/kernels/track_particles.cu")):
+        return None
+    out = os.path.join(HERE, "_ref", "ref_track_sm103a.cubin")
+    deps = [os.path.join(HERE, f) for f in ("build_ref_cuda.sh", "ref_cuda_kernels.cu",
+                                            "build_ref.sh")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    env = dict(os.environ, REF_ROOT=root)
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref_cuda.sh")], env=env,
+                          stdout=subprocess.DEVNULL)
+    return out
+
+
 class EbeConfig(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "order", "num_particles_to_store", "num_elements_to_store",
