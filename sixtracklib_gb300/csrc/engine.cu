@@ -160,7 +160,7 @@ struct Device {
     int id = -1;
     cudaStream_t stream = nullptr;
     int32_t *d_flags = nullptr;  // [0] status, [1] error
-    int32_t *h_flags = nullptr;  // pinned
+    int32_t *h_flags = nullptr;  // pinned: [0..1] the flags, [2..3] an int64 count
     // scratch for the active-particle selection (grown on demand, kept)
     uint64_t *scratch = nullptr;
     int64_t scratch_words = 0;
@@ -196,7 +196,7 @@ static Device *get_device(int id)
     d->id = id;
     if (!cuda_ok(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaMalloc(&d->d_flags, 2 * sizeof(int32_t)), "cudaMalloc") ||
-        !cuda_ok(cudaMallocHost(&d->h_flags, 2 * sizeof(int32_t)), "cudaMallocHost")) {
+        !cuda_ok(cudaMallocHost(&d->h_flags, 4 * sizeof(int32_t)), "cudaMallocHost")) {
         delete d;
         return nullptr;
     }
@@ -253,7 +253,25 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     return s;
 }
 
+// Particle-element-turns per launch of a segmented until-turn call: long
+// calls are cut into launches of about this much work, and the particles
+// still alive are re-packed densely between them (lanes of particles lost
+// during a launch stay idle until its end).  ~55 ms of tracking on a GB300.
+constexpr double kSegmentPet = 2e9;
+
+static int64_t segment_turns(int64_t active, int64_t num_elements)
+{
+    double const per_turn = (double)std::max<int64_t>(active, 1) *
+                            (double)std::max<int64_t>(num_elements, 1);
+    double const t = std::ceil(kSegmentPet / per_turn);
+    return t >= 2147483647.0 ? 2147483647 : std::max<int64_t>(1, (int64_t)t);
+}
+
 // Run one tracking pass and wait for it; returns the OR-ed status (0/-1).
+// An until-turn call that waits is run as a sequence of launches of at most
+// segment_turns() turns each, with the particles that still have work
+// selected again before every launch; the per-particle arithmetic is the
+// same as in one launch, so results are bit-identical.
 static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, uint64_t *d_cols,
                          int64_t n, int64_t i0, int64_t i1, int mode, int64_t until_turn,
                          bool finish_turn, uint64_t *ebe_out, int64_t ebe_cap,
@@ -307,13 +325,42 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
         prm.idx = idx;
         prm.count = count;
     }
-    if (i1 > i0) {
+    // until-turn calls that wait: capped launches while work is left (an
+    // until_turn within the first segment needs one launch, as the start
+    // turns are >= 0 for any particle that can have work)
+    int64_t seg = segment_turns(i1 - i0, prm.num_elements);
+    bool const segmented = wait && mode == MODE_UNTIL && i1 > i0 && seg < until_turn;
+    while (i1 > i0) {
+        prm.turn_cap = segmented ? (int32_t)std::min<int64_t>(seg, 2147483647) : 0;
         int const rc = launch_track(prm, opt.fast, opt.threads, opt.blocks_per_sm, stream);
         if (rc != 0) {
             set_error(std::string("track kernel launch: ") + cudaGetErrorString((cudaError_t)rc));
             return -1;
         }
         g_launches.fetch_add(1);
+        if (!segmented) break;
+        int64_t *idx = nullptr, *count = nullptr;
+        int const rs = launch_select(d_cols, n, i0, i1, mode, until_turn, dev->scratch, &idx,
+                                     &count, stream);
+        if (rs != 0) {
+            set_error(std::string("particle selection launch: ") +
+                      cudaGetErrorString((cudaError_t)rs));
+            return -1;
+        }
+        g_launches.fetch_add(3);
+        int64_t *h_count = reinterpret_cast<int64_t *>(dev->h_flags + 2);
+        if (!cuda_ok(cudaMemcpyAsync(h_count, count, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                     stream),
+                     "cudaMemcpyAsync(count)") ||
+            !cuda_ok(cudaMemcpyAsync(dev->h_flags, dev->d_flags, 2 * sizeof(int32_t),
+                                     cudaMemcpyDeviceToHost, stream),
+                     "cudaMemcpyAsync(status)") ||
+            !cuda_ok(cudaStreamSynchronize(stream), "track kernel"))
+            return -1;
+        if (*h_count == 0 || dev->h_flags[1] != 0) break;  // done, or a pipeline timeout
+        prm.idx = idx;
+        prm.count = count;
+        seg = segment_turns(*h_count, prm.num_elements);
     }
     if (!wait) return 0;
     if (!cuda_ok(cudaMemcpyAsync(dev->h_flags, dev->d_flags, 2 * sizeof(int32_t),

@@ -32,7 +32,7 @@ struct TrackParams {
     int64_t i0, i1;          // particle index range
     int64_t until_turn;
     int32_t finish_turn;
-    int32_t pad_;
+    int32_t turn_cap;        // MODE_UNTIL: a block stops after this many turns (0: none)
     uint64_t xlim_bits, ylim_bits;  // global aperture limits as IEEE bits
     int32_t *status;         // device: OR of per-particle status
     int32_t *error;          // device: ErrorBits

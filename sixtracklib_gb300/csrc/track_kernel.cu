@@ -430,6 +430,10 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
         }
         ++turn;
         any = __syncthreads_or(active);
+        // every particle of the block is at a turn boundary here: a capped
+        // launch may stop, the next launch resumes from the stored state
+        if (prm.mode == MODE_UNTIL && prm.turn_cap > 0 && turn >= (int64_t)s_tmin + prm.turn_cap)
+            any = false;
     }
 
     // drain bulk copies still in flight before the CTA exits
