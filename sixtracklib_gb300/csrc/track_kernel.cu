@@ -350,10 +350,13 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
             issued = first;
         }
         if (resident) {  // the whole lattice stays in shared memory
-            bool ok = true;
-            for (int g = 0; g < nch; ++g) ok = mbar_wait_bounded(&bars[g], 0u) && ok;
-            consumed = nch;
-            timed_out = __syncthreads_or(!ok);
+            // consumed = the first chunk not seen complete: after a timeout
+            // the drain below waits for it and every later one
+            int first_bad = nch;
+            for (int g = 0; g < nch; ++g)
+                if (!mbar_wait_bounded(&bars[g], 0u) && first_bad == nch) first_bad = g;
+            consumed = first_bad;
+            timed_out = __syncthreads_or(first_bad < nch);
         }
     }
 
@@ -369,7 +372,7 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
                 buf = (int)(consumed % stages);
                 uint32_t const parity = (uint32_t)((consumed / stages) & 1);
                 bool const ok = mbar_wait_bounded(&bars[buf], parity);
-                ++consumed;
+                if (ok) ++consumed;  // a chunk that timed out is left to the drain
                 if (__syncthreads_or(!ok)) {
                     timed_out = true;
                     break;
@@ -436,8 +439,9 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
             any = false;
     }
 
-    // drain bulk copies still in flight before the CTA exits
-    if (threadIdx.x == 0 && !resident) {
+    // drain bulk copies still in flight before the CTA exits (a resident
+    // lattice has none left unless a wait timed out)
+    if (threadIdx.x == 0 && (!resident || timed_out)) {
         while (consumed < issued) {
             int const buf = (int)(consumed % stages);
             uint32_t const parity = (uint32_t)((consumed / stages) & 1);
