@@ -346,6 +346,7 @@ bool st_TrackJob_is_collecting_output(const st_TrackJob *job);
 uint16_t st_TrackJob_get_collect_flags(const st_TrackJob *job);
 void st_TrackJob_set_collect_flags(st_TrackJob *job, uint16_t flags);
 bool st_TrackJob_requires_collecting(const st_TrackJob *job);
+/* 3, SIXTRL_ARCHITECTURE_CUDA (control/definitions.h:84-86) */
 int64_t st_TrackJob_get_type_id(const st_TrackJob *job);
 const char *st_TrackJob_get_type_str(const st_TrackJob *job);
 bool st_TrackJob_has_device_id_str(const st_TrackJob *job);
@@ -566,6 +567,15 @@ bool st_TrackJobNew_has_beam_monitors(const st_TrackJobBaseNew *job);
 st_buffer_size_t st_TrackJobNew_get_num_particle_sets(const st_TrackJobBaseNew *job);
 st_buffer_size_t st_TrackJobNew_get_total_num_of_particles(const st_TrackJobBaseNew *job);
 const char *st_TrackJobNew_get_arch_string(const st_TrackJobBaseNew *job);
+/* track/track_job_base.h: NS(TrackJobNew_get_arch_id), _has_arch_string;
+ * the arch id is 3, SIXTRL_ARCHITECTURE_CUDA */
+uint32_t st_TrackJobNew_get_arch_id(const st_TrackJobBaseNew *job);
+bool st_TrackJobNew_has_arch_string(const st_TrackJobBaseNew *job);
+/* cuda/track_job.h:27-38: the CUDA devices this process can use (node
+ * index k = CUDA device k); the index list returns how many it wrote. */
+st_buffer_size_t st_CudaTrackJob_get_num_available_nodes(void);
+st_buffer_size_t st_CudaTrackJob_get_available_node_indices_list(st_buffer_size_t max_num_node_indices,
+                                                                 int64_t *node_indices_begin);
 bool st_TrackJobNew_has_config_str(const st_TrackJobBaseNew *job);
 const char *st_TrackJobNew_get_config_str(const st_TrackJobBaseNew *job);
 uint16_t st_TrackJobNew_get_collect_flags(const st_TrackJobBaseNew *job);

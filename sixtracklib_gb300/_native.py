@@ -84,6 +84,8 @@ _SIGNATURES = {
     "st_TrackJob_commit_address_assignments": ([vp], i32),
     "st_TrackJob_assign_all_addresses": ([vp], i32),
     "st_TrackJob_assign_addresses": ([vp, u64, u64], i32),
+    "st_CudaTrackJob_get_num_available_nodes": ([], u64),
+    "st_TrackJob_get_type_id": ([vp], i64),
     "st_CudaTrackJob_default_threads_per_block": ([vp], u64),
     "st_CudaTrackJob_default_track_threads_per_block": ([vp], u64),
     "st_TrackJob_get_output_buffer": ([vp], vp),

@@ -1291,7 +1291,28 @@ uint16_t st_TrackJob_get_collect_flags(const st_TrackJob *j) { return j ? j->col
 void st_TrackJob_set_collect_flags(st_TrackJob *j, uint16_t f) { if (j) j->collect_flags = f; }
 bool st_TrackJob_requires_collecting(const st_TrackJob *j) { return j != nullptr; }
 
-int64_t st_TrackJob_get_type_id(const st_TrackJob *j) { return j ? 2 : -1; }
+// SIXTRL_ARCHITECTURE_CUDA (control/definitions.h:84-86): the id a CUDA
+// track job reports (cuda/track/track_job.cpp:129)
+int64_t st_TrackJob_get_type_id(const st_TrackJob *j) { return j ? 3 : -1; }
+uint32_t st_TrackJobNew_get_arch_id(const st_TrackJobBaseNew *j) { return j ? 3u : 0u; }
+bool st_TrackJobNew_has_arch_string(const st_TrackJobBaseNew *j) { return j != nullptr; }
+st_buffer_size_t st_CudaTrackJob_get_num_available_nodes(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (st_buffer_size_t)n;
+}
+st_buffer_size_t st_CudaTrackJob_get_available_node_indices_list(st_buffer_size_t max_num,
+                                                                 int64_t *indices)
+{
+    st_buffer_size_t const n = st_CudaTrackJob_get_num_available_nodes();
+    st_buffer_size_t k = 0;
+    for (; indices && k < n && k < max_num; ++k) indices[k] = (int64_t)k;
+    return k;
+}
 const char *st_TrackJob_get_type_str(const st_TrackJob *j) { return j ? "cuda" : ""; }
 bool st_TrackJob_has_device_id_str(const st_TrackJob *j) { return j && !j->device_id_str.empty(); }
 const char *st_TrackJob_get_device_id_str(const st_TrackJob *j)

@@ -163,6 +163,50 @@ class TrackJob:
     def type_str(self):
         return self._lib.st_TrackJob_get_type_str(self.ptr_st_track_job).decode()
 
+    def type(self):
+        """The architecture id of the job: 3, SIXTRL_ARCHITECTURE_CUDA
+        (trackjob.py:1622-1632)."""
+        return int(self._lib.st_TrackJob_get_type_id(self.ptr_st_track_job))
+
+    @property
+    def arch_id(self):
+        return self.type()
+
+    # ---------------------------------- nodes (trackjob.py:1215-1290)
+    @staticmethod
+    def enabled_archs():
+        """The architectures this engine tracks on: CUDA only (the reference
+        lists its compiled modules plus "cpu")."""
+        return ["cuda"]
+
+    @staticmethod
+    def num_available_nodes(arch_str=None, env_var_name=None, filter_str=None):
+        """CUDA devices this process can use for arch "cuda" (the reference
+        counts OpenCL nodes only and answers 0 otherwise); 0 for other archs."""
+        if arch_str is None or arch_str.strip().lower() != "cuda":
+            return 0
+        return int(_native.load().st_CudaTrackJob_get_num_available_nodes())
+
+    @staticmethod
+    def num_all_nodes(arch_str=None):
+        return TrackJob.num_available_nodes(arch_str)
+
+    @staticmethod
+    def print_nodes(arch_str, all=False, filter_str=None, env_var_name=None):
+        """Print the CUDA devices (node index = device index) for arch "cuda"."""
+        n = TrackJob.num_available_nodes(arch_str)
+        if n == 0:
+            print(f"no nodes available for arch {arch_str!r}")
+            return
+        try:
+            import torch
+
+            names = [torch.cuda.get_device_name(k) for k in range(n)]
+        except Exception:  # the names are cosmetic; the count comes from the driver
+            names = ["CUDA device"] * n
+        for k, name in enumerate(names):
+            print(f"cuda node {k}: {name}")
+
     @property
     def particles_buffer(self):
         return self._particles_buffer

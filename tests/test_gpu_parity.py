@@ -704,6 +704,10 @@ def test_cuda_trackjob_properties_and_track_line(torch_cuda, oracle):
     assert job.has_controller and job.has_particles_arg and job.has_beam_elements_arg
     assert not job.is_in_debug_mode and not job.has_output_buffer and not job.owns_output_buffer
     assert job.num_particle_sets == 1
+    assert job.type() == job.arch_id == 3  # SIXTRL_ARCHITECTURE_CUDA
+    assert CudaTrackJob.enabled_archs() == ["cuda"]
+    assert CudaTrackJob.num_available_nodes("cuda") >= 1
+    assert CudaTrackJob.num_available_nodes("opencl") == 0
     assert job.default_threads_per_block == 256
     assert job.default_track_threads_per_block == 256  # 512 requested: the kernel's maximum
     n = len(e)

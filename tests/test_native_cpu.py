@@ -174,3 +174,17 @@ def test_line_density_link_survives_buffer_adoption():
     finally:
         lib.st_Buffer_delete(buf)
 
+
+
+def test_node_queries_without_gpu(lib, capsys):
+    """Node queries answer without a device: no CUDA node here, and no
+    other architecture is served (trackjob.py:1215-1290)."""
+    from sixtracklib_gb300.trackjob import TrackJob
+
+    assert TrackJob.enabled_archs() == ["cuda"]
+    assert TrackJob.num_available_nodes("opencl") == 0
+    assert TrackJob.num_available_nodes() == 0
+    assert TrackJob.num_available_nodes("cuda") == lib.st_CudaTrackJob_get_num_available_nodes()
+    TrackJob.print_nodes("opencl")
+    assert "no nodes" in capsys.readouterr().out
+    assert lib.st_TrackJob_get_type_id(None) == -1
