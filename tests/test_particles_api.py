@@ -110,3 +110,18 @@ def test_stcommon_q_gauss_helpers():
     assert sc.st_Buffer_new is not None and sc.st_NullBuffer is None
     with pytest.raises(AttributeError):
         sc.st_Not_a_function
+
+
+def test_package_exports_the_reference_names():
+    """The names python/sixtracklib/__init__.py exports for this path."""
+    import sixtracklib_gb300 as st
+
+    for name in ("Particles", "ParticlesSet", "ParticlesAddr", "makeCopy",
+                 "calcParticlesDifference", "compareParticlesDifference", "Buffer",
+                 "get_cbuffer_from_obj", "AssignAddressItem", "CudaTrackJob", "TrackJob",
+                 "supports", "LineDensityProfileData",
+                 "LineDensityProfileData_create_buffer_assignment", "TriCub", "TriCubData",
+                 "TriCub_buffer_create_assign_address_item", "Elements", "Drift", "Multipole",
+                 "BeamBeam6D", "SCQGaussProfile", "BeamMonitor"):
+        assert hasattr(st, name), name
+    assert st.supports("cuda") and not st.supports("opencl") and not st.supports("cpu")
