@@ -106,6 +106,38 @@ class _Element:
     def _array_len(self, expr):
         return int(eval(expr, {}, dict(self.__dict__)))
 
+    def __setattr__(self, name, value):
+        """Fields of an element that belongs to a lattice buffer are views of
+        it, as the reference's CObject fields are: assigning one writes the
+        buffer in place (an array field keeps its length)."""
+        object.__setattr__(self, name, value)
+        cb = self.__dict__.get("_cbuffer")
+        index = self.__dict__.get("_index")
+        if cb is None or index is None:
+            return
+        for fi, (fname, kind) in enumerate(self._fields):
+            if fname == name:
+                break
+        else:
+            return
+        obj = cb.objects[index]
+        if kind == "f":
+            obj.words[fi] = np.float64(value).view(np.uint64)
+        elif kind == "i":
+            obj.words[fi] = np.int64(value).view(np.uint64)
+        elif kind == "u":
+            obj.words[fi] = np.uint64(int(value))
+        else:
+            arr = np.ascontiguousarray(value, dtype=np.float64).ravel()
+            off = int(obj.words[fi])
+            n = self._array_len(self, kind[1])
+            if arr.size != n:
+                raise ValueError(f"{type(self).__name__}.{name}: {arr.size} values for an "
+                                 f"array of {n} in the buffer (its layout is fixed)")
+            obj.words[off:off + n] = arr.view(np.uint64)
+            object.__setattr__(self, name, arr.copy())
+        cb.touch()
+
     def _set_array_entry(self, name, i, value):
         """array field ``name``[i] = value, here and in the lattice buffer
         the element belongs to (the reference's elements are views of their
@@ -265,6 +297,12 @@ class SRotation(_Element):
         super().__init__(cbuffer=cbuffer, **kw)
 
     @property
+    def angle(self):
+        """The rotation angle in radians (beam_elements.py:293-295; the
+        constructor takes degrees)."""
+        return float(np.arctan2(self.sin_z, self.cos_z))
+
+    @property
     def angle_deg(self):
         return float(np.arctan2(self.sin_z, self.cos_z) * 180.0 / np.pi)
 
@@ -283,6 +321,38 @@ class BeamMonitor(_Element):
     )
     _default_skip = 1
     _default_is_turn_ordered = 1
+
+
+def append_beam_monitors_to_lattice(beam_elements_buffer, until_turn_elem_by_elem,
+                                    until_turn_turn_by_turn, until_turn, skip_turns=1,
+                                    min_particle_id=0, max_particle_id=0, initial_at_turn=0):
+    """Append the turn-by-turn and the periodic output monitors
+    (beam_elements.py:314-367): a turn-ordered monitor storing every turn
+    from max(initial_at_turn, until_turn_elem_by_elem) up to
+    until_turn_turn_by_turn, then a rolling one storing every `skip_turns`-th
+    turn up to until_turn.  Returns the number of monitors added."""
+    cb = beam_elements_buffer
+    if not isinstance(cb, CBuffer):
+        cb = getattr(cb, "cbuffer", cb)
+    added = 0
+    start_tbt = max(initial_at_turn, until_turn_elem_by_elem)
+    if until_turn_turn_by_turn > start_tbt:
+        BeamMonitor(start=start_tbt, num_stores=until_turn_turn_by_turn - start_tbt, skip=1,
+                    out_address=0, min_particle_id=min_particle_id,
+                    max_particle_id=max_particle_id, is_rolling=0, is_turn_ordered=1,
+                    cbuffer=cb)
+        added += 1
+    start_out = max(start_tbt, until_turn_turn_by_turn)
+    if until_turn > start_out:
+        skip = skip_turns if skip_turns > 0 else 1
+        num_stores, rem = divmod(until_turn - start_out, skip)
+        if rem > 0:
+            num_stores += 1
+        BeamMonitor(start=start_out, num_stores=num_stores, skip=skip, out_address=0,
+                    min_particle_id=min_particle_id, max_particle_id=max_particle_id,
+                    is_rolling=1, is_turn_ordered=1, cbuffer=cb)
+        added += 1
+    return added
 
 
 class LimitRect(_Element):
@@ -318,6 +388,17 @@ class LimitEllipse(_Element):
         kw.pop("a_b_squ", None)
         super().__init__(cbuffer=cbuffer, a_squ=a_squ, b_squ=b_squ, a_b_squ=a_squ * b_squ, **kw)
 
+    def set_half_axes(self, a, b):
+        return self.set_half_axes_squ(a * a, b * b)
+
+    def set_half_axes_squ(self, a_squ, b_squ):
+        """beam_elements.py:460-467 / 647-654 (written into the lattice
+        buffer the element belongs to)."""
+        self.a_squ = a_squ
+        self.b_squ = b_squ
+        self.a_b_squ = a_squ * b_squ
+        return self
+
 
 class LimitRectEllipse(_Element):
     _typeid = TYPE_LIMIT_RECT_ELLIPSE
@@ -334,6 +415,17 @@ class LimitRectEllipse(_Element):
         kw.pop("a_b_squ", None)
         super().__init__(cbuffer=cbuffer, max_x=max_x, max_y=max_y, a_squ=a_squ,
                          b_squ=b_squ, a_b_squ=a_squ * b_squ, **kw)
+
+    def set_half_axes(self, a, b):
+        return self.set_half_axes_squ(a * a, b * b)
+
+    def set_half_axes_squ(self, a_squ, b_squ):
+        """beam_elements.py:460-467 / 647-654 (written into the lattice
+        buffer the element belongs to)."""
+        self.a_squ = a_squ
+        self.b_squ = b_squ
+        self.a_b_squ = a_squ * b_squ
+        return self
 
 
 class DipoleEdge(_Element):

@@ -1764,7 +1764,7 @@ int32_t st_TrackJob_fetch_particle_addresses(st_TrackJob *j)
     for (size_t k = 0; k < j->psets.size(); ++k) {
         st_ParticlesAddr &a = j->paddr[k];
         a.num_particles = j->pset_cnt[k];
-        uint64_t *cols = &a.q0;
+        uint64_t *cols = &a.q0_addr;
         for (int c = 0; c < 21; ++c)
             cols[c] = (uint64_t)(uintptr_t)(j->d_cols + (size_t)c * j->n_total + j->pset_off[k]);
     }

@@ -253,6 +253,30 @@ def compareParticlesDifference(lhs, rhs, abs_treshold=None):
     return 0
 
 
+TYPE_PARTICLES_ADDR = 512
+
+
+def _particles_addr_class():
+    from .beam_elements import _Element
+
+    class ParticlesAddr(_Element):
+        """NS(ParticlesAddr) as a buffer object (particles.py:490-513, type
+        id 512): the particle count and the address of each of the 21
+        columns, in NS(Particles) order."""
+
+        _typeid = TYPE_PARTICLES_ADDR
+        _fields = (("num_particles", "i"),) + tuple(
+            (name, "u") for name in (
+                "q0", "mass0", "beta0", "gamma0", "p0c", "s", "x", "y", "px", "py", "zeta",
+                "psigma", "delta", "rpp", "rvv", "chi", "charge_ratio", "particle_id",
+                "at_element", "at_turn", "state"))
+
+    return ParticlesAddr
+
+
+ParticlesAddr = _particles_addr_class()
+
+
 class ParticlesSet:
     """Container of particle sets in one CObjects buffer
     (python/sixtracklib/particles.py:417-489)."""
@@ -268,6 +292,33 @@ class ParticlesSet:
     def particles(self):
         return [self.cbuffer.get_object(i) for i in range(self.cbuffer.n_objects)
                 if self.cbuffer.objects[i].typeid == TYPE_PARTICLE]
+
+    @classmethod
+    def fromSixDump101(cls, input_folder, st_dump_file, **kwargs):
+        """Particle sets from a SixTrack DUMP format-101 file, one set per
+        dump location (particles.py:443-488).  Like the reference this needs
+        sixtracktools and pysixtrack to read the SixTrack input and the dump;
+        it raises ImportError where they are not installed."""
+        import pysixtrack
+        import sixtracktools
+
+        six = sixtracktools.SixInput(input_folder)
+        line, rest, iconv = six.expand_struct(convert=pysixtrack.element_types)
+        sixdump = sixtracktools.SixDump101(st_dump_file)
+        num_iconv, num_belem, num_dumps = len(iconv), len(line), len(sixdump.particles)
+        if not (num_iconv > 0 and num_belem > iconv[-1] and num_dumps >= num_iconv and
+                num_dumps % num_iconv == 0):
+            raise ValueError("SixTrack dump and input do not match")
+        n = num_dumps // num_iconv
+        self = cls(**kwargs)
+        for ii, elem_id in enumerate(iconv):
+            p = self.Particles(num_particles=n)
+            for jj in range(n):
+                p.from_pysixtrack(pysixtrack.Particles(**sixdump[n * ii + jj].get_minimal_beam()),
+                                  jj)
+                p.state[jj] = 1
+                p.at_element[jj] = elem_id
+        return self
 
     @classmethod
     def fromfile(cls, filename):

@@ -18,7 +18,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native
-from .beam_elements import Elements
+from .beam_elements import Elements, LineDensityProfileData  # noqa: F401  (sc_line_density.py)
 
 
 class LineDensityBuffer:

@@ -22,6 +22,7 @@ import numpy as np
 
 from . import buffer as _buffer
 from .beam_elements import q_gauss_cq as _q_gauss_cq
+from .trackjob import st_ParticlesAddr  # noqa: F401  (stcommon.py:517-542)
 
 SIXTRL_MATH_QGAUSSIAN_Q_EPS = 1e-6
 

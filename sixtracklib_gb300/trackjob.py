@@ -343,8 +343,8 @@ class TrackJob:
                                                        int(particle_set_index))
         if not ptr:
             return None
-        out = ParticlesAddr()
-        C.memmove(C.addressof(out), ptr, C.sizeof(ParticlesAddr))
+        out = st_ParticlesAddr()
+        C.memmove(C.addressof(out), ptr, C.sizeof(st_ParticlesAddr))
         return out
 
     def _push_output(self):
@@ -585,14 +585,16 @@ class TrackJob:
         return self._output_buffer.get_object(index)
 
 
-class ParticlesAddr(C.Structure):
-    """st_ParticlesAddr (particles/particles_addr.h:27-55)."""
+class st_ParticlesAddr(C.Structure):
+    """st_ParticlesAddr (particles/particles_addr.h:27-55) with the field
+    names of the reference's ctypes binding (stcommon.py:517-542)."""
 
+    _pack_ = 8
     _fields_ = [("num_particles", C.c_int64)] + [
-        (f"{name}_addr", C.c_uint64) for name in (
+        (name, C.c_uint64) for name in (
             "q0", "mass0", "beta0", "gamma0", "p0c", "s", "x", "y", "px", "py", "zeta",
             "psigma", "delta", "rpp", "rvv", "chi", "charge_ratio", "particle_id",
-            "at_element_id", "at_turn", "state")]
+            "at_element", "at_turn", "state")]
 
 
 class _StParticles(C.Structure):

@@ -752,7 +752,7 @@ def test_trackjob_particle_addresses(torch_cuda, oracle):
     job.track_until(2)
     trk = DeviceTracker(e, config="mode=exact")
     lib = _native.load()
-    assert lib.st_DeviceLattice_track_until(trk._ptr, C.c_void_p(a.q0_addr), 300, 5, None) == 0
+    assert lib.st_DeviceLattice_track_until(trk._ptr, C.c_void_p(a.q0), 300, 5, None) == 0
     torch_cuda.cuda.synchronize()
     job.collect_particles()
     exp = q.block.copy()

@@ -125,3 +125,66 @@ def test_package_exports_the_reference_names():
                  "BeamBeam6D", "SCQGaussProfile", "BeamMonitor"):
         assert hasattr(st, name), name
     assert st.supports("cuda") and not st.supports("opencl") and not st.supports("cpu")
+
+
+def test_element_fields_are_buffer_views(oracle):
+    """Assigning a field of an element that belongs to a lattice writes the
+    lattice buffer in place (the reference's CObject fields are views), so
+    the edit reaches tracking; an array keeps its length."""
+    import pytest
+
+    from sixtracklib_gb300 import lattices
+
+    e = lattices.fodo_ring()
+    img0 = e.cbuffer.to_image().copy()
+    d = e.get(0)
+    d.length = 2.5
+    assert e.get(0).length == 2.5
+    assert np.count_nonzero(e.cbuffer.to_image() != img0) == 1
+    m = e.get(1)
+    m.bal = np.array([0.0, 0.0, 0.06, 0.0])
+    assert np.allclose(e.get(1).bal, [0.0, 0.0, 0.06, 0.0])
+    with pytest.raises(ValueError):
+        m.bal = np.zeros(6)
+    fresh = lattices.fodo_ring()
+    fresh.get(0).length, fresh.get(1).bal = 2.5, np.array([0.0, 0.0, 0.06, 0.0])
+    p = lattices.gaussian_particles(32, seed=1).block
+    a, b = p.copy(), p.copy()
+    oracle.track_until(e.cbuffer.to_image(), a, 2)
+    oracle.track_until(fresh.cbuffer.to_image(), b, 2)
+    assert np.array_equal(a, b)
+
+
+def test_reference_element_helpers():
+    """SRotation.angle (radians), the half-axes setters, the output monitors
+    helper (beam_elements.py:293-299, 314-367, 460-467) and the
+    ParticlesAddr buffer object (particles.py:490-513)."""
+    import pytest
+
+    from sixtracklib_gb300.beam_elements import (Elements, LimitEllipse,
+                                                 append_beam_monitors_to_lattice)
+    from sixtracklib_gb300.particles import ParticlesAddr, ParticlesSet
+
+    e = Elements()
+    r = e.SRotation(angle=30.0)
+    assert abs(r.angle - np.pi / 6) < 1e-15 and abs(r.angle_deg - 30.0) < 1e-12
+    el = e.LimitEllipse(a=0.02, b=0.01)
+    el.set_half_axes(0.03, 0.015)
+    got = e.get(1)
+    assert (got.a_squ, got.b_squ, got.a_b_squ) == (0.03 * 0.03, 0.015 * 0.015,
+                                                   (0.03 * 0.03) * (0.015 * 0.015))
+    rel = e.LimitRectEllipse(max_x=0.02, max_y=0.02, a=0.02, b=0.02).set_half_axes_squ(4e-4, 1e-4)
+    assert e.get(2).a_b_squ == 4e-4 * 1e-4 and rel.b_squ == 1e-4
+    assert isinstance(LimitEllipse(a=1.0, b=2.0).set_half_axes(2.0, 3.0), LimitEllipse)
+    n0 = len(e)
+    assert append_beam_monitors_to_lattice(e, 2, 10, 107, skip_turns=10, max_particle_id=99) == 2
+    tbt, out = e.get(n0), e.get(n0 + 1)
+    assert (tbt.start, tbt.num_stores, tbt.skip, tbt.is_rolling) == (2, 8, 1, 0)
+    assert (out.start, out.num_stores, out.skip, out.is_rolling) == (10, 10, 10, 1)
+    assert out.max_particle_id == 99
+    assert append_beam_monitors_to_lattice(e, 0, 0, 0) == 0
+    ps = ParticlesSet()
+    a = ParticlesAddr(cbuffer=ps.cbuffer, num_particles=4, x=4096)
+    assert ps.cbuffer.objects[0].typeid == 512 and a.x == 4096
+    with pytest.raises(ImportError):  # needs sixtracktools and pysixtrack, as the reference
+        ParticlesSet.fromSixDump101("input", "dump.dat")
