@@ -147,6 +147,39 @@ st_Buffer *st_Buffer_new_on_data(const unsigned char *data, st_buffer_size_t siz
 void st_Buffer_delete(st_Buffer *buffer);
 int32_t st_Buffer_write_to_file(const st_Buffer *buffer, const char *path);
 int32_t st_Buffer_reset(st_Buffer *buffer);
+/* buffer.h:263-400: sized creation, capacity management and the header
+ * queries.  Objects are never freed individually, so there are no garbage
+ * ranges (0); a buffer of this library lives at its stored base address,
+ * so it never needs remapping (remap / refresh succeed).  Status 0 on
+ * success, -1 otherwise; clear removes every object. */
+st_Buffer *st_Buffer_new_detailed(st_buffer_size_t max_num_objects,
+                                  st_buffer_size_t max_num_slots,
+                                  st_buffer_size_t max_num_dataptrs,
+                                  st_buffer_size_t max_num_garbage_ranges, uint64_t flags);
+int32_t st_Buffer_reserve(st_Buffer *buffer, st_buffer_size_t max_num_objects,
+                          st_buffer_size_t max_num_slots, st_buffer_size_t max_num_dataptrs,
+                          st_buffer_size_t max_num_garbage_ranges);
+int32_t st_Buffer_clear(st_Buffer *buffer, bool set_data_to_zero);
+int32_t st_Buffer_reset_detailed(st_Buffer *buffer, st_buffer_size_t max_num_objects,
+                                 st_buffer_size_t max_num_slots,
+                                 st_buffer_size_t max_num_dataptrs,
+                                 st_buffer_size_t max_num_garbage_ranges);
+int32_t st_Buffer_reserve_capacity(st_Buffer *buffer, st_buffer_size_t capacity);
+/* Replace the buffer's content with a CObjects file's. */
+int32_t st_Buffer_read_from_file(st_Buffer *buffer, const char *path_to_file);
+/* Write the image with its stored addresses moved to `norm_base_addr`. */
+int32_t st_Buffer_write_to_file_normalized_addr(const st_Buffer *buffer, const char *path_to_file,
+                                                st_buffer_addr_t norm_base_addr);
+bool st_Buffer_needs_remapping(const st_Buffer *buffer);
+int32_t st_Buffer_remap(st_Buffer *buffer);
+int32_t st_Buffer_refresh(st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_header_size(const st_Buffer *buffer);
+st_buffer_addr_t st_Buffer_get_data_end_addr(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_max_num_of_objects(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_max_num_of_slots(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_max_num_of_dataptrs(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_num_of_garbage_ranges(const st_Buffer *buffer);
+st_buffer_size_t st_Buffer_get_max_num_of_garbage_ranges(const st_Buffer *buffer);
 st_buffer_size_t st_Buffer_get_size(const st_Buffer *buffer);
 st_buffer_size_t st_Buffer_get_capacity(const st_Buffer *buffer);
 st_buffer_size_t st_Buffer_get_slot_size(const st_Buffer *buffer);
@@ -493,8 +526,9 @@ int32_t st_TrackJob_assign_addresses(st_TrackJob *job, st_buffer_size_t dest_buf
  * each of the 21 columns in NS(Particles) order. */
 typedef struct st_ParticlesAddr {
     int64_t num_particles;
-    uint64_t q0, mass0, beta0, gamma0, p0c, s, x, y, px, py, zeta, psigma, delta, rpp, rvv,
-        chi, charge_ratio, particle_id, at_element_id, at_turn, state;
+    uint64_t q0_addr, mass0_addr, beta0_addr, gamma0_addr, p0c_addr, s_addr, x_addr, y_addr,
+        px_addr, py_addr, zeta_addr, psigma_addr, delta_addr, rpp_addr, rvv_addr, chi_addr,
+        charge_ratio_addr, particle_id_addr, at_element_id_addr, at_turn_addr, state_addr;
 } st_ParticlesAddr;
 /* common/track_job.h:266-289 and track/track_job_base.h:150-175: the
  * device addresses of the job's particle sets, for kernels of the caller's

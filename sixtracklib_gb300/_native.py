@@ -36,6 +36,27 @@ _SIGNATURES = {
     "st_Buffer_get_num_of_dataptrs": ([vp], u64),
     "st_Buffer_get_const_data_begin": ([vp], vp),
     "st_Buffer_get_const_object": ([vp, u64], vp),
+    "st_Buffer_new_detailed": ([u64, u64, u64, u64, u64], vp),
+    "st_Buffer_reserve": ([vp, u64, u64, u64, u64], i32),
+    "st_Buffer_reserve_capacity": ([vp, u64], i32),
+    "st_Buffer_reset": ([vp], i32),
+    "st_Buffer_reset_detailed": ([vp, u64, u64, u64, u64], i32),
+    "st_Buffer_clear": ([vp, cbool], i32),
+    "st_Buffer_needs_remapping": ([vp], cbool),
+    "st_Buffer_remap": ([vp], i32),
+    "st_Buffer_refresh": ([vp], i32),
+    "st_Buffer_read_from_file": ([vp, cstr], i32),
+    "st_Buffer_write_to_file_normalized_addr": ([vp, cstr, u64], i32),
+    "st_Buffer_get_capacity": ([vp], u64),
+    "st_Buffer_get_slot_size": ([vp], u64),
+    "st_Buffer_get_header_size": ([vp], u64),
+    "st_Buffer_get_data_begin_addr": ([vp], u64),
+    "st_Buffer_get_data_end_addr": ([vp], u64),
+    "st_Buffer_get_max_num_of_objects": ([vp], u64),
+    "st_Buffer_get_max_num_of_slots": ([vp], u64),
+    "st_Buffer_get_max_num_of_dataptrs": ([vp], u64),
+    "st_Buffer_get_num_of_garbage_ranges": ([vp], u64),
+    "st_Buffer_get_max_num_of_garbage_ranges": ([vp], u64),
     "st_Drift_add": ([vp, C.c_double], vp),
     "st_Multipole_add": ([vp, i64, vp, C.c_double, C.c_double, C.c_double], vp),
     "st_Particles_new": ([vp, u64], vp),

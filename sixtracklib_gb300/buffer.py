@@ -130,27 +130,201 @@ class CBufferHandle:
 
 
 class Buffer:
-    """The view of a stored buffer that ``TrackJob.stored_buffer`` returns
-    (buffer.py:92-200): the job's C-side copy (``pointer``), its object
-    count and size, and the Python buffer it copies (``cbuffer``)."""
+    """A C-side NS(Buffer) (buffer.py:92-430).
 
-    maps_to_cbuffer = True
+    Made from a Python buffer (``cbuffer``: a C-side copy of its image, which
+    ``refresh`` brings up to date after Python-side edits -- the reference
+    maps the same memory instead), an existing ``st_Buffer`` pointer
+    (``ptr_ext_buffer``, owned only if asked), a CObjects file, raw image
+    data, or empty with a byte ``size`` or with object / slot / dataptr
+    capacities.  A TrackJob's stored buffer is returned as a Buffer over the
+    job's copy (owned by the job)."""
 
-    def __init__(self, cbuffer: CBuffer, handle: CBufferHandle):
-        self.cbuffer = cbuffer
-        self._handle = handle
+    maps_to_cbuffer = property(lambda self: self._cbuffer is not None and bool(self.pointer))
 
+    def __init__(self, cbuffer=None, ptr_ext_buffer=None, owns_pointer=None, owns_buffer=None,
+                 ptr_data=None, path_to_file=None, size=0, num_objects=None, num_slots=None,
+                 num_dataptrs=None, num_garbage_ranges=None, buffer_flags=None, slot_size=8,
+                 _handle=None):
+        self._lib = _native.load()
+        self._last_status = 0
+        self._owns_buffer = self._owns_pointer = True
+        self._cbuffer = get_cbuffer_from_obj(cbuffer)
+        self._handle = _handle
+        self._frees_handle = False
+        self._ptr = None
+        if _handle is not None:  # a TrackJob's copy: the job owns it
+            self._owns_buffer = self._owns_pointer = False
+        elif self._cbuffer is not None:
+            # the Python buffer owns the data, as with the reference's mapping
+            self._handle = CBufferHandle(self._cbuffer)
+            self._frees_handle = True
+            self._owns_buffer = False
+        elif ptr_ext_buffer:
+            self._ptr = ptr_ext_buffer
+            self._owns_pointer = owns_pointer is True
+            self._owns_buffer = owns_buffer is True
+        elif path_to_file:
+            self._ptr = self._lib.st_Buffer_new_from_file(str(path_to_file).encode())
+        elif ptr_data:
+            nbytes = C.cast(ptr_data, C.POINTER(C.c_uint64))[1]  # header word 1: the size
+            self._ptr = self._lib.st_Buffer_new_on_data(ptr_data, int(nbytes))
+        elif num_objects is not None and num_slots is not None and num_dataptrs is not None:
+            self._ptr = self._lib.st_Buffer_new_detailed(
+                int(num_objects), int(num_slots), int(num_dataptrs),
+                int(num_garbage_ranges or 0), int(buffer_flags or 0))
+        else:
+            self._ptr = self._lib.st_Buffer_new(int(size or 0))
+        if not self.pointer:
+            raise RuntimeError("unable to create the buffer: " + _native.last_error())
+
+    @classmethod
+    def from_cbuffer(cls, obj, owns_buffer=False, owns_pointer=True, **kwargs):
+        cb = get_cbuffer_from_obj(obj)
+        if cb is None:
+            raise ValueError(f"Unable to obtain cbuffer for {obj}")
+        return cls(cbuffer=cb, owns_buffer=owns_buffer, owns_pointer=owns_pointer, **kwargs)
+
+    def __del__(self):
+        try:
+            if self._frees_handle:
+                self._handle.free()
+                self._frees_handle = False
+            elif self._ptr and self._owns_pointer:
+                self._lib.st_Buffer_delete(self._ptr)
+            self._ptr = None
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ queries
     @property
     def pointer(self):
-        return self._handle.ptr
+        return self._handle.ptr if self._handle is not None else self._ptr
 
     @property
-    def num_objects(self):
-        return int(self._handle._lib.st_Buffer_get_num_of_objects(self._handle.ptr))
+    def cbuffer(self):
+        return self._cbuffer
 
     @property
-    def size(self):
-        return int(self._handle._lib.st_Buffer_get_size(self._handle.ptr))
+    def last_status(self):
+        return self._last_status
+
+    @property
+    def last_status_success(self):
+        return self._last_status == 0
+
+    @property
+    def owns_buffer(self):
+        return self._owns_buffer
+
+    @property
+    def owns_pointer(self):
+        return self._owns_pointer
+
+    @property
+    def is_owner(self):
+        return self._owns_buffer and self._owns_pointer
+
+    def _q(self, name):
+        return int(getattr(self._lib, name)(self.pointer))
+
+    slot_size = property(lambda self: self._q("st_Buffer_get_slot_size"))
+    size = property(lambda self: self._q("st_Buffer_get_size"))
+    capacity = property(lambda self: self._q("st_Buffer_get_capacity"))
+    num_objects = property(lambda self: self._q("st_Buffer_get_num_of_objects"))
+    max_num_objects = property(lambda self: self._q("st_Buffer_get_max_num_of_objects"))
+    num_slots = property(lambda self: self._q("st_Buffer_get_num_of_slots"))
+    max_num_slots = property(lambda self: self._q("st_Buffer_get_max_num_of_slots"))
+    num_dataptrs = property(lambda self: self._q("st_Buffer_get_num_of_dataptrs"))
+    max_num_dataptrs = property(lambda self: self._q("st_Buffer_get_max_num_of_dataptrs"))
+    num_garbage_ranges = property(lambda self: self._q("st_Buffer_get_num_of_garbage_ranges"))
+    max_num_garbage_ranges = property(
+        lambda self: self._q("st_Buffer_get_max_num_of_garbage_ranges"))
+    header_size = property(lambda self: self._q("st_Buffer_get_header_size"))
+    data_begin_addr = property(lambda self: self._q("st_Buffer_get_data_begin_addr"))
+    data_end_addr = property(lambda self: self._q("st_Buffer_get_data_end_addr"))
+
+    @property
+    def needs_remapping(self):
+        return bool(self._lib.st_Buffer_needs_remapping(self.pointer))
+
+    @property
+    def ptr_data_begin(self):
+        return C.cast(self.data_begin_addr, C.POINTER(C.c_ubyte))
+
+    @property
+    def ptr_data_end(self):
+        return C.cast(self.data_end_addr, C.POINTER(C.c_ubyte))
+
+    # ------------------------------------------------------------ changes
+    def _status(self, st, what):
+        self._last_status = int(st)
+        if self._last_status != 0:
+            raise RuntimeError(f"unsuccessful {what} op; status:{self._last_status}")
+        return self
+
+    def clear(self, clear_data=False):
+        return self._status(self._lib.st_Buffer_clear(self.pointer, bool(clear_data)), "clear")
+
+    def refresh(self):
+        """Bring the C-side copy of a Python buffer up to date (the
+        structure must be unchanged); otherwise the reference's refresh."""
+        if self._cbuffer is not None and self._handle is not None:
+            self._handle.refresh(self._cbuffer)
+            return self._status(0, "refresh")
+        return self._status(self._lib.st_Buffer_refresh(self.pointer), "refresh")
+
+    def remap(self):
+        return self._status(self._lib.st_Buffer_remap(self.pointer), "remap")
+
+    def write_to_file(self, path_to_file, normalized_base_addr=None):
+        if not path_to_file:
+            self._last_status = -1
+            raise RuntimeError("illegal path supplied")
+        p = str(path_to_file).encode()
+        if normalized_base_addr is not None and normalized_base_addr > 0:
+            st = self._lib.st_Buffer_write_to_file_normalized_addr(self.pointer, p,
+                                                                     int(normalized_base_addr))
+        else:
+            st = self._lib.st_Buffer_write_to_file(self.pointer, p)
+        return self._status(st, "write_to_file")
+
+    def read_from_file(self, path_to_file):
+        if path_to_file:
+            self._status(self._lib.st_Buffer_read_from_file(self.pointer,
+                                                            str(path_to_file).encode()),
+                         "read_from_file")
+        return self
+
+    def reserve_capacity(self, capacity):
+        if capacity is not None and capacity >= 0:
+            self._status(self._lib.st_Buffer_reserve_capacity(self.pointer, int(capacity)),
+                         "reserve capacity")
+        return self
+
+    def reserve(self, max_num_objects, max_num_slots, max_num_dataptrs,
+                max_num_garbage_ranges):
+        return self._status(self._lib.st_Buffer_reserve(
+            self.pointer, int(max_num_objects), int(max_num_slots), int(max_num_dataptrs),
+            int(max_num_garbage_ranges)), "reserve")
+
+    def reset(self, max_num_objects=None, max_num_slots=None, max_num_dataptrs=None,
+              max_num_garbage_ranges=None):
+        if (max_num_objects, max_num_slots, max_num_dataptrs,
+                max_num_garbage_ranges) == (None, None, None, None):
+            return self._status(self._lib.st_Buffer_reset(self.pointer), "reset")
+        return self._status(self._lib.st_Buffer_reset_detailed(
+            self.pointer,
+            int(self.max_num_objects if max_num_objects is None else max_num_objects),
+            int(self.max_num_slots if max_num_slots is None else max_num_slots),
+            int(self.max_num_dataptrs if max_num_dataptrs is None else max_num_dataptrs),
+            int(max_num_garbage_ranges or 0)), "reset")
+
+    def image(self) -> np.ndarray:
+        """A copy of the buffer's CObjects image."""
+        n = self.size
+        data = self._lib.st_Buffer_get_const_data_begin(self.pointer)
+        return np.ctypeslib.as_array(C.cast(data, C.POINTER(C.c_uint64)), shape=(n // 8,)).copy()
 
 
 class AssignAddressItem(_Element):

@@ -10,6 +10,7 @@
 // in the reference.  Growth re-lays the sections out with doubled capacity
 // and shifts every stored address; pointers returned earlier become invalid,
 // as they do in the reference.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -310,6 +311,138 @@ int32_t st_Buffer_reset(st_Buffer *b)
     if (!b) return -1;
     return relayout(b, nullptr, b->slots_cap, b->objs_cap, b->dptr_cap) ? 0 : -1;
 }
+
+st_Buffer *st_Buffer_new_detailed(st_buffer_size_t max_num_objects,
+                                  st_buffer_size_t max_num_slots,
+                                  st_buffer_size_t max_num_dataptrs,
+                                  st_buffer_size_t max_num_garbage_ranges, uint64_t flags)
+{
+    (void)max_num_garbage_ranges;  // no garbage ranges are kept: objects are never freed
+    (void)flags;
+    st_Buffer *b = new (std::nothrow) st_Buffer();
+    if (!b) return nullptr;
+    if (!relayout(b, nullptr, max_num_slots, max_num_objects, max_num_dataptrs)) {
+        delete b;
+        return nullptr;
+    }
+    return b;
+}
+
+int32_t st_Buffer_reserve(st_Buffer *b, st_buffer_size_t max_num_objects,
+                          st_buffer_size_t max_num_slots, st_buffer_size_t max_num_dataptrs,
+                          st_buffer_size_t max_num_garbage_ranges)
+{
+    (void)max_num_garbage_ranges;
+    if (!b) return -1;
+    if (max_num_objects <= b->objs_cap && max_num_slots <= b->slots_cap &&
+        max_num_dataptrs <= b->dptr_cap)
+        return 0;
+    stg::ImageView v;
+    std::string err;
+    if (!v.open(b->mem, b->cap_words * 8, &err)) {
+        set_error(err);
+        return -1;
+    }
+    return relayout(b, &v, std::max<uint64_t>(b->slots_cap, max_num_slots),
+                    std::max<uint64_t>(b->objs_cap, max_num_objects),
+                    std::max<uint64_t>(b->dptr_cap, max_num_dataptrs))
+               ? 0
+               : -1;
+}
+
+int32_t st_Buffer_reset_detailed(st_Buffer *b, st_buffer_size_t max_num_objects,
+                                 st_buffer_size_t max_num_slots,
+                                 st_buffer_size_t max_num_dataptrs,
+                                 st_buffer_size_t max_num_garbage_ranges)
+{
+    (void)max_num_garbage_ranges;
+    if (!b) return -1;
+    return relayout(b, nullptr, max_num_slots, max_num_objects, max_num_dataptrs) ? 0 : -1;
+}
+
+int32_t st_Buffer_reserve_capacity(st_Buffer *b, st_buffer_size_t capacity)
+{
+    if (!b) return -1;
+    if (capacity <= b->cap_words * 8) return 0;
+    uint64_t const more = (capacity - b->cap_words * 8 + 7) / 8;
+    return st_Buffer_reserve(b, b->objs_cap, b->slots_cap + more, b->dptr_cap, 0);
+}
+
+int32_t st_Buffer_read_from_file(st_Buffer *b, const char *path)
+{
+    if (!b) return -1;
+    st_Buffer *n = st_Buffer_new_from_file(path);
+    if (!n) return -1;
+    uint64_t const gen = b->generation;
+    std::free(b->mem);
+    *b = *n;
+    b->generation = gen + 1;
+    n->mem = nullptr;
+    delete n;
+    return 0;
+}
+
+// The image with every stored address moved to `norm_base` (header, object
+// table, dataptr table, the pointer fields the dataptrs name, and an
+// interpolated space-charge kick's table address when it points into the
+// buffer), written to `path` (buffer.h:334-337).
+int32_t st_Buffer_write_to_file_normalized_addr(const st_Buffer *b, const char *path,
+                                                st_buffer_addr_t norm_base)
+{
+    if (!b || !path) return -1;
+    uint64_t const base = base_of(b), size = b->mem[1], nw = size / 8;
+    auto inside = [&](uint64_t a) { return a >= base && a < base + size; };
+    auto moved = [&](uint64_t a) { return a - base + norm_base; };
+    std::vector<uint64_t> img(b->mem, b->mem + nw);
+    img[0] = norm_base;
+    for (int k = 3; k <= 6; ++k) img[k] = moved(b->mem[k]);
+    uint64_t const no = nobjs(b), nd = ndptrs(b);
+    for (uint64_t i = 0; i < no; ++i) {
+        uint64_t const e = b->objs_w + 2 + 3 * i;
+        img[e] = moved(b->mem[e]);
+        if (b->mem[e + 1] == ST_OBJECT_TYPE_SC_INTERPOLATED_PROF && b->mem[e + 2] >= 56) {
+            uint64_t const w = (b->mem[e] - base) / 8 + 6;
+            if (w < nw && inside(b->mem[w])) img[w] = moved(b->mem[w]);
+        }
+    }
+    for (uint64_t k = 0; k < nd; ++k) {
+        uint64_t const e = b->dptr_w + 2 + k;
+        uint64_t const field = b->mem[e];
+        img[e] = moved(field);
+        if (inside(field)) {
+            uint64_t const w = (field - base) / 8;
+            if (w < nw && inside(b->mem[w])) img[w] = moved(b->mem[w]);
+        }
+    }
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return -1;
+    size_t const put = std::fwrite(img.data(), 1, (size_t)size, f);
+    std::fclose(f);
+    return put == size ? 0 : -1;
+}
+
+int32_t st_Buffer_clear(st_Buffer *b, bool set_data_to_zero)
+{
+    (void)set_data_to_zero;  // the new layout is zero-filled
+    return st_Buffer_reset(b);
+}
+
+// A buffer of this library is always mapped at its own address: its stored
+// base address equals where it lives, so remapping has nothing to do.
+bool st_Buffer_needs_remapping(const st_Buffer *b) { return b && b->mem[0] != base_of(b); }
+int32_t st_Buffer_remap(st_Buffer *b) { return (b && !st_Buffer_needs_remapping(b)) ? 0 : -1; }
+int32_t st_Buffer_refresh(st_Buffer *b) { return st_Buffer_remap(b); }
+
+st_buffer_size_t st_Buffer_get_header_size(const st_Buffer *b) { return b ? b->mem[2] : 0; }
+st_buffer_addr_t st_Buffer_get_data_end_addr(const st_Buffer *b)
+{
+    return b ? base_of(b) + b->mem[1] : 0;
+}
+st_buffer_size_t st_Buffer_get_max_num_of_objects(const st_Buffer *b) { return b ? b->objs_cap : 0; }
+st_buffer_size_t st_Buffer_get_max_num_of_slots(const st_Buffer *b) { return b ? b->slots_cap : 0; }
+st_buffer_size_t st_Buffer_get_max_num_of_dataptrs(const st_Buffer *b) { return b ? b->dptr_cap : 0; }
+st_buffer_size_t st_Buffer_get_num_of_garbage_ranges(const st_Buffer *) { return 0; }
+st_buffer_size_t st_Buffer_get_max_num_of_garbage_ranges(const st_Buffer *) { return 0; }
 
 st_buffer_size_t st_Buffer_get_size(const st_Buffer *b) { return b ? b->mem[1] : 0; }
 st_buffer_size_t st_Buffer_get_capacity(const st_Buffer *b) { return b ? b->cap_words * 8 : 0; }

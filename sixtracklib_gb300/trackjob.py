@@ -415,7 +415,7 @@ class TrackJob:
         """A :class:`~sixtracklib_gb300.buffer.Buffer` view of the stored
         buffer (C-side copy and the Python buffer), or None."""
         entry = self._stored.get(buffer_id)
-        return Buffer(entry[0], entry[1]) if entry is not None else None
+        return Buffer(cbuffer=entry[0], _handle=entry[1]) if entry is not None else None
 
     def ptr_stored_buffer(self, buffer_id):
         """The C-side st_Buffer of a stored buffer, or None."""

@@ -207,3 +207,54 @@ def test_pull_into_brings_back_c_side_writes():
     assert diff.size == 2  # only the two id fields changed
     np.testing.assert_array_equal(e.get(1).bal, lattices.fodo_ring().get(1).bal)
     h.free()
+
+
+def test_buffer_class(tmp_path):
+    """The C-side buffer wrapper (buffer.py:92-430): construction from a
+    Python buffer, a size, capacities, a file and raw data; capacities,
+    reserve / reset / clear; file round trips, with normalized addresses
+    giving the Python writer's bytes."""
+    import ctypes as Ct
+
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.buffer import Buffer
+    from sixtracklib_gb300.cbuffer import CBuffer
+
+    e = lattices.fodo_ring()
+    b = Buffer.from_cbuffer(e)
+    assert b.maps_to_cbuffer and not b.owns_buffer and b.owns_pointer
+    assert b.num_objects == len(e) and b.slot_size == 8 and b.header_size == 64
+    assert b.data_end_addr - b.data_begin_addr == b.size <= b.capacity
+    assert not b.needs_remapping and b.remap() is b and b.last_status_success
+    assert b.num_garbage_ranges == 0 and b.max_num_objects >= b.num_objects
+    e.get(0).length = 3.25  # a Python-side edit reaches the copy on refresh
+    b.refresh()
+    assert np.array_equal(CBuffer.from_image(b.image()).objects[0].words,
+                          e.cbuffer.objects[0].words)
+    path = str(tmp_path / "lattice.bin")
+    b.write_to_file(path, normalized_base_addr=4096)
+    raw = np.fromfile(path, dtype=np.uint64)
+    assert raw[0] == 4096 and all(4096 <= raw[k] < 4096 + raw[1] for k in (3, 4, 5, 6))
+    back = CBuffer.fromfile(path)
+    assert [o.typeid for o in back.objects] == [o.typeid for o in e.cbuffer.objects]
+    assert all(np.array_equal(x.words, y.words) for x, y in zip(back.objects, e.cbuffer.objects))
+    f = Buffer(path_to_file=path)
+    assert f.num_objects == len(e) and f.owns_buffer and f.is_owner
+    g = Buffer(size=0).read_from_file(path)
+    assert g.num_objects == len(e)
+    img = e.cbuffer.to_image()
+    r = Buffer(ptr_data=Ct.c_void_p(img.ctypes.data))
+    assert r.num_objects == len(e)
+    d = Buffer(num_objects=10, num_slots=100, num_dataptrs=5)
+    assert (d.max_num_objects, d.max_num_slots, d.max_num_dataptrs) == (10, 100, 5)
+    d.reserve(20, 200, 8, 0)
+    assert (d.max_num_objects, d.max_num_slots, d.max_num_dataptrs) == (20, 200, 8)
+    cap = d.capacity
+    d.reserve_capacity(cap + 4096)
+    assert d.capacity >= cap + 4096
+    f.clear()
+    assert f.num_objects == 0
+    g.reset(max_num_objects=4)
+    assert g.num_objects == 0 and g.max_num_objects == 4
+    with pytest.raises(RuntimeError):
+        g.write_to_file("")
