@@ -112,3 +112,24 @@ def test_beam_beam_space_charge(torch_cuda, ref_kernels, elliptic):
             st, got = run_device(torch_cuda, lat, p.block, until=turns, mode=mode)
             assert st == 0
             assert_parity(got, ref, tol=tol)
+
+
+def test_benchmark_workload_full_size_bit_identical(torch_cuda, ref_kernels):
+    """The benchmark workload at full size -- 1,000,000 protons of the polar
+    grid on the 20,000-element ring, 2 turns -- tracked by the reference's
+    kernel and by the engine's exact mode: every column of every particle
+    bit-identical, losses included."""
+    from sixtracklib_gb300.device import DeviceTracker
+
+    torch = torch_cuda
+    e = lattices.synthetic_ring()
+    p = lattices.polar_grid_particles(1_000_000)
+    ref = _ref_until(ref_kernels, torch, e.cbuffer.to_image(), p.block, 2)
+    trk = DeviceTracker(e, config="mode=exact")
+    cols = torch.from_numpy(p.block.copy().view(np.int64)).cuda()
+    assert trk.track_until(cols, 2) == 0
+    got = cols.cpu().numpy().view(np.uint64)
+    lost = int((ref[20].view(np.int64) == 0).sum())
+    assert 0 < lost < 1_000_000
+    diff = np.nonzero((got != ref).any(axis=1))[0]
+    assert diff.size == 0, f"columns {diff} differ"
