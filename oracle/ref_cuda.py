@@ -155,9 +155,10 @@ def _pet(before: np.ndarray, after: np.ndarray, n_elem: int) -> int:
 
 def main(argv=None):
     """Time the reference's CUDA kernel on the synthetic 20,000-element ring
-    and the polar-grid protons (the engine's benchmark workload): one warm-up
-    turn, then `turns` turns in one launch timed with CUDA events; prints one
-    JSON line."""
+    and the polar-grid protons (the engine's benchmark workload), or on the
+    beam-beam and space-charge mix (round or elliptic strong beams, Gaussian
+    protons): one warm-up turn, then `turns` turns in one launch timed with
+    CUDA events; prints one JSON line."""
     import argparse
     import json
 
@@ -168,9 +169,20 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--turns", type=int, default=2)
+    ap.add_argument("--workload", default="synthetic",
+                    choices=["synthetic", "bbsc", "bbsc_elliptic"])
     args = ap.parse_args(argv)
-    ring = lattices.synthetic_ring()
-    parts = lattices.polar_grid_particles(args.particles)
+    if args.workload == "synthetic":
+        ring = lattices.synthetic_ring()
+        parts = lattices.polar_grid_particles(args.particles)
+        name = f"synthetic 20k-element ring, {args.particles} particles polar grid"
+    else:
+        elliptic = args.workload == "bbsc_elliptic"
+        ring = lattices.bb_sc_ring(elliptic=elliptic)
+        parts = lattices.gaussian_particles(args.particles, seed=3)
+        name = (f"FODO ring + 4 BeamBeam6D (21 slices) + 4 BeamBeam4D + 200 SCQGaussProfile, "
+                f"{'elliptic' if elliptic else 'round'} strong beams, {args.particles} "
+                f"Gaussian protons")
     k = RefCudaKernels(torch)
     d_lat = k.to_device(ring.cbuffer.to_image())
     d_p = k.to_device(particles_image(parts.block))
@@ -188,8 +200,8 @@ def main(argv=None):
     pet = _pet(before, after, len(ring))
     print(json.dumps({
         "kernel": "st_Track_particles_until_turn_cuda (reference, sm_103a, -fmad=false)",
-        "workload": f"synthetic 20k-element ring, {n} particles polar grid, {args.turns} turns "
-                    f"after 1 warm-up turn, {THREADS_PER_BLOCK} threads per block",
+        "workload": f"{name}, {args.turns} turns after 1 warm-up turn, "
+                    f"{THREADS_PER_BLOCK} threads per block",
         "ms": ms, "pet": pet, "value": pet / (ms * 1e-3),
         "unit": "particle-element-turns/s"}))
 
