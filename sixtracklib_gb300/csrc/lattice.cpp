@@ -18,6 +18,7 @@ namespace {
 
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751;
 constexpr double kClight = 299792458.0;
+constexpr double kEps0 = 8.854187817620e-12;
 
 struct Emitter {
     std::vector<uint64_t> recs;     // records, unchunked
@@ -205,6 +206,14 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                 for (double v : {sqrt_beta, sqrt_beta * sqrt_beta, sqrt_beta / w2d(w[9]),
                                  abs_omq >= 1e-6 ? 1.0 / omq : 0.0})
                     p.push_back(d2w(v));
+                // the round field's constants (gauss_fields.h:138-148), used
+                // by the fast arithmetic policy in place of two divisions
+                double const sx = w2d(w[2]), sy = w2d(w[3]), msd = w2d(w[7]);
+                double const sigma = 0.5 * (sx + sy);
+                bool const round = std::fabs(sx - sy) < msd;
+                p.push_back(d2w(round ? 0.5 / (sigma * sigma) : 0.0));
+                p.push_back(d2w(round ? 1.0 / (2.0 * kPi * kEps0 * sigma) : 0.0));
+                if (round) aux |= SC_ROUND;
             }
             break;
         case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {

@@ -551,6 +551,26 @@ static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, dou
 // second exponential, exp(-(x^2 + y^2) / (2 sigma^2)), is the same number as
 // the first, exp(-0.5 r2 / sigma^2) (both arguments are r2 / sigma^2 scaled
 // by -1/2 exactly), so it is evaluated once.
+// The same field and G terms from sigma^2 with two divisions and no square
+// root (the fast arithmetic policy; within a few ulp of fields_round_g).
+__device__ __forceinline__ void fields_round_g_fast(double x, double y, double sigma2, double *ex,
+                                                    double *ey, double *gx, double *gy)
+{
+    constexpr double k = 1.0 / (2. * kPiD * kEps0D);
+    double const inv_s2 = 1.0 / sigma2;
+    double const r2 = x * x + y * y;
+    double const inv_r2 = 1.0 / r2;
+    double const e = exp(-0.5 * r2 * inv_s2);
+    double const t = (r2 < 1e-20) ? k * sqrt(r2 * inv_s2) : (1 - e) * k * inv_r2;
+    double const exv = t * x, eyv = t * y;
+    double const c = k * inv_s2;
+    double const h = 0.5 * inv_r2;
+    *ex = exv;
+    *ey = eyv;
+    *gx = h * (y * eyv - x * exv + c * x * x * e);
+    *gy = h * (x * exv - y * eyv + c * y * y * e);
+}
+
 __device__ __forceinline__ void fields_round_g(double x, double y, double sigma, double *ex,
                                                double *ey, double *gx, double *gy)
 {
@@ -573,7 +593,7 @@ __device__ __forceinline__ void fields_round_g(double x, double y, double sigma,
 // propagation's singular branch reduces to Sig_11_hat = Sig_33_hat = W / 2,
 // cos theta = 1, sin theta = 0, no theta derivative, and the field is the
 // round one -- the same values as the general code for such a beam.
-template <bool ROUND>
+template <bool ROUND, bool FAST>
 static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec, int n_slices)
 {
     const uint64_t *d = rec + 1;
@@ -637,7 +657,10 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
             double const s_hat = 0.5 * (S11 + S33);
             double const ds_hat = 0.5 * dS_W;
             double ex, ey, gx, gy;
-            fields_round_g(xb, yb, sqrt(s_hat), &ex, &ey, &gx, &gy);
+            if (FAST)
+                fields_round_g_fast(xb, yb, s_hat, &ex, &ey, &gx, &gy);
+            else
+                fields_round_g(xb, yb, sqrt(s_hat), &ex, &ey, &gx, &gy);
             Fx = Ksl * ex;
             Fy = Ksl * ey;
             Fz = 0.5 * (Ksl * gx * ds_hat + Ksl * gy * ds_hat);
@@ -720,14 +743,20 @@ static __device__ __noinline__ PState sc_coasting(PState p, const uint64_t *rec)
 }
 
 // be_beamfields/track.h:203-268 with NS(Math_q_gauss) (internal/math_qgauss.h:114-175)
-static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
+// FAST: the particle's 1 / (pc0 beta) gives 1 / rvv by two products, and
+// a round field (aux SC_ROUND) takes its constants from the record: two
+// divisions instead of four, within a few ulp of the reference's kick.
+template <bool FAST>
+static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, uint32_t aux)
 {
     const uint64_t *c = rec + 1;
     double const charge = kCharge0SiD * p.q0;
     double const beta0 = p.beta0;
     double const beta = beta0 * p.rvv;
     double const pc0 = p.p0c * kCharge0SiD;
-    double const z = p.zeta / p.rvv;
+    double inv_pc0_beta = 0.0;
+    if (FAST) inv_pc0_beta = 1.0 / (pc0 * beta);
+    double const z = FAST ? p.zeta * (inv_pc0_beta * (pc0 * beta0)) : p.zeta / p.rvv;
     double fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
     fk *= W(c[0]);
     // c[11..14]: sqrt_beta = 1 / (sqrt(2) bunchlength_rms), sqrt_beta^2,
@@ -745,9 +774,26 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec)
         e = exp(arg);
     }
     fk *= W(c[13]) * e;
-    fk /= pc0 * beta;
     double ex, ey, gx, gy;
-    fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx, &gy);
+    if (FAST) {
+        fk *= inv_pc0_beta;
+        if (aux & SC_ROUND) {
+            double const x = p.x - W(c[5]), y = p.y - W(c[6]);
+            double const r2 = x * x + y * y;
+            double const t = (r2 < 1e-20) ? sqrt(r2) * W(c[16])
+                                          : (1.0 - exp(-r2 * W(c[15]))) *
+                                                (1.0 / (2. * kPiD * kEps0D)) / r2;
+            ex = t * x;
+            ey = t * y;
+        } else {
+            fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey,
+                         &gx, &gy);
+        }
+    } else {
+        fk /= pc0 * beta;
+        fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey, &gx,
+                     &gy);
+    }
     p.px += fk * ex;
     p.py += fk * ey;
     return p;

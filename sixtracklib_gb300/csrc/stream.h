@@ -33,7 +33,10 @@ enum Op : uint32_t {
     OP_SC_COASTING = 15,    // [9 SCCoasting words]
     OP_SC_QGAUSS = 16,      // [11 SCQGaussProfile words, sqrt_beta = 1 / (sqrt(2)
                             //  bunchlength_rms), sqrt_beta^2, sqrt_beta / cq,
-                            //  1 / (1 - q) (0 when |1 - q| < 1e-6)]
+                            //  1 / (1 - q) (0 when |1 - q| < 1e-6),
+                            //  0.5 / sigma^2, 1 / (2 pi eps0 sigma)]
+                            // aux bit0 (SC_ROUND): |sigma_x - sigma_y| <
+                            //  min_sigma_diff, sigma = (sigma_x + sigma_y) / 2
     OP_MONITOR = 17,        // [num_stores, start, skip, max_pid, min_pid, rolling,
                             //  turn_ordered, out_ptr, out_capacity]
     OP_NOP = 18,            // success, no effect (disabled beam-beam)
@@ -47,6 +50,9 @@ enum Op : uint32_t {
 };
 
 constexpr uint32_t DRIFT_APERTURE = 1u;
+// SC q-Gaussian aux flag: the transverse field is the round one.
+constexpr uint32_t SC_ROUND = 1u;
+
 // BB6D aux flag: the strong beam's Sigma matrix is round and uncoupled
 // (S11 = S33, S12 = S34, S22 = S44, S13 = S14 = S23 = S24 = 0) with
 // threshold_singular > 0 and min_sigma_diff > 0.  Then R = S13 = 0 at every

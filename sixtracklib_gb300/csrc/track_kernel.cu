@@ -234,15 +234,15 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         return 0;
     case OP_BB6D:
         if (aux & BB6D_ROUND)
-            p = beam_beam_6d<true>(p, rec, (int)(aux & BB6D_SLICES));
+            p = beam_beam_6d<true, FAST>(p, rec, (int)(aux & BB6D_SLICES));
         else
-            p = beam_beam_6d<false>(p, rec, (int)aux);
+            p = beam_beam_6d<false, FAST>(p, rec, (int)aux);
         return 0;
     case OP_SC_COASTING:
         p = sc_coasting(p, rec);
         return 0;
     case OP_SC_QGAUSS:
-        p = sc_qgauss(p, rec);
+        p = sc_qgauss<FAST>(p, rec, aux);
         return 0;
     case OP_SC_INTERP:
         p = sc_interpolated(p, rec, aux);
