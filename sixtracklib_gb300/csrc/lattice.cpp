@@ -214,6 +214,16 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                 p.push_back(d2w(round ? 0.5 / (sigma * sigma) : 0.0));
                 p.push_back(d2w(round ? 1.0 / (2.0 * kPi * kEps0 * sigma) : 0.0));
                 if (round) aux |= SC_ROUND;
+                // the elliptic field's constants (gauss_fields.h:150-190)
+                bool const ell = !round && sx != sy && sx > 0.0 && sy > 0.0;
+                double const S = ell ? std::sqrt(2.0 * std::fabs(sx * sx - sy * sy)) : 0.0;
+                double const kSqrtPi = 1.7724538509055160272981674833411451827975494561224;
+                for (double v : {ell ? 1.0 / S : 0.0, ell ? 1.0 / (2.0 * kEps0 * kSqrtPi * S) : 0.0,
+                                 ell ? sy / sx : 0.0, ell ? sx / sy : 0.0,
+                                 ell ? 1.0 / (2.0 * sx * sx) : 0.0,
+                                 ell ? 1.0 / (2.0 * sy * sy) : 0.0})
+                    p.push_back(d2w(v));
+                if (ell) aux |= (sx > sy) ? SC_ELL_X : SC_ELL_Y;
             }
             break;
         case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {

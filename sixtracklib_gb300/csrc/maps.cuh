@@ -785,6 +785,26 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
                                                 (1.0 / (2. * kPiD * kEps0D)) / r2;
             ex = t * x;
             ey = t * y;
+        } else if (aux & (SC_ELL_X | SC_ELL_Y)) {
+            // the elliptic field with its element constants from the record
+            double const x = p.x - W(c[5]), y = p.y - W(c[6]);
+            double const abx = fabs(x), aby = fabs(y);
+            double const is = W(c[17]), fact = W(c[18]);
+            double const e = exp(-(abx * abx * W(c[21])) - aby * aby * W(c[22]));
+            double wz_re, wz_im, we_re, we_im;
+            if (aux & SC_ELL_X) {
+                cerrf(abx * is, aby * is, &wz_re, &wz_im);
+                cerrf(W(c[19]) * abx * is, W(c[20]) * aby * is, &we_re, &we_im);
+                ex = fact * (wz_im - we_im * e);
+                ey = fact * (wz_re - we_re * e);
+            } else {
+                cerrf(aby * is, abx * is, &wz_re, &wz_im);
+                cerrf(W(c[20]) * aby * is, W(c[19]) * abx * is, &we_re, &we_im);
+                ey = fact * (wz_im - we_im * e);
+                ex = fact * (wz_re - we_re * e);
+            }
+            if (x < 0) ex = -ex;
+            if (y < 0) ey = -ey;
         } else {
             fields_gauss(p.x - W(c[5]), p.y - W(c[6]), W(c[2]), W(c[3]), W(c[7]), 1, &ex, &ey,
                          &gx, &gy);

@@ -34,9 +34,14 @@ enum Op : uint32_t {
     OP_SC_QGAUSS = 16,      // [11 SCQGaussProfile words, sqrt_beta = 1 / (sqrt(2)
                             //  bunchlength_rms), sqrt_beta^2, sqrt_beta / cq,
                             //  1 / (1 - q) (0 when |1 - q| < 1e-6),
-                            //  0.5 / sigma^2, 1 / (2 pi eps0 sigma)]
+                            //  0.5 / sigma^2, 1 / (2 pi eps0 sigma),
+                            //  1 / S, 1 / (2 eps0 sqrt(pi) S), sigma_y / sigma_x,
+                            //  sigma_x / sigma_y, 1 / (2 sigma_x^2),
+                            //  1 / (2 sigma_y^2)], S = sqrt(2 |sigma_x^2 - sigma_y^2|)
                             // aux bit0 (SC_ROUND): |sigma_x - sigma_y| <
-                            //  min_sigma_diff, sigma = (sigma_x + sigma_y) / 2
+                            //  min_sigma_diff, sigma = (sigma_x + sigma_y) / 2;
+                            // bit1 / bit2 (SC_ELL_X / SC_ELL_Y): elliptic with
+                            //  sigma_x > sigma_y / sigma_x < sigma_y
     OP_MONITOR = 17,        // [num_stores, start, skip, max_pid, min_pid, rolling,
                             //  turn_ordered, out_ptr, out_capacity]
     OP_NOP = 18,            // success, no effect (disabled beam-beam)
@@ -52,6 +57,8 @@ enum Op : uint32_t {
 constexpr uint32_t DRIFT_APERTURE = 1u;
 // SC q-Gaussian aux flag: the transverse field is the round one.
 constexpr uint32_t SC_ROUND = 1u;
+constexpr uint32_t SC_ELL_X = 2u;
+constexpr uint32_t SC_ELL_Y = 4u;
 
 // BB6D aux flag: the strong beam's Sigma matrix is round and uncoupled
 // (S11 = S33, S12 = S34, S22 = S44, S13 = S14 = S23 = S24 = 0) with
