@@ -233,3 +233,20 @@ void ref_fields_gauss(double x, double y, double sx, double sy, double msd,
 {
     NS(get_Ex_Ey_Gx_Gy_gauss)(x, y, sx, sy, msd, skip, ex, ey, gx, gy);
 }
+
+/* NS(BeamBeam6D_boost) / NS(BeamBeam6D_inv_boost) (be_beamfields.h:
+ * 2101-2230) on one point: `boost` = (sphi, cphi, tphi, salpha, calpha) as
+ * in NS(BB6D_boost_data), `c6` = (x, px, y, py, sigma, delta), in place. */
+void ref_bb6d_boost(const double *boost, double *c6, int inverse)
+{
+    NS(BB6D_boost_data) b;
+    b.sphi = boost[0];
+    b.cphi = boost[1];
+    b.tphi = boost[2];
+    b.salpha = boost[3];
+    b.calpha = boost[4];
+    if (inverse)
+        NS(BeamBeam6D_inv_boost)(&b, &c6[0], &c6[1], &c6[2], &c6[3], &c6[4], &c6[5]);
+    else
+        NS(BeamBeam6D_boost)(&b, &c6[0], &c6[1], &c6[2], &c6[3], &c6[4], &c6[5]);
+}

@@ -886,3 +886,24 @@ def bb6d_data(q_part, phi, alpha, delta_x, delta_y, n_part_per_slice, z_slices,
     words[38 + 2 * n : 38 + 3 * n] = salpha * tphi * z
     words[38 + 3 * n : 38 + 4 * n] = z / cphi
     return words
+
+
+def gaussian_equal_charge_slices(n_part_tot, sigma_z, n_slices):
+    """Slicing of a Gaussian strong bunch into `n_slices` slices of equal
+    charge, as the 6D beam-beam set-up of the reference's Python layer
+    expects them (charge_slices, zeta_slices): the bins are the quantiles
+    k / n_slices of the longitudinal Gaussian, each slice sits at the
+    centroid of its bin, sigma_z sqrt(n_slices^2 / (2 pi)) (exp(-a^2 / 2) -
+    exp(-b^2 / 2)) for the normalised bin edges a < b, head (largest z)
+    first; one slice sits at z = 0.  Returns (charge per slice, z)."""
+    n = int(n_slices)
+    if n < 1:
+        raise ValueError("at least one slice")
+    if n == 1:
+        return np.array([float(n_part_tot)]), np.array([0.0])
+    from scipy.special import ndtri
+
+    edges = ndtri(np.linspace(0.0, 1.0, n + 1))  # -inf .. +inf
+    dens = np.exp(-0.5 * edges * edges)          # 0 at both infinities
+    z = float(sigma_z) * n / np.sqrt(2.0 * np.pi) * (dens[:-1] - dens[1:])
+    return np.full(n, float(n_part_tot) / n), z[::-1].copy()
