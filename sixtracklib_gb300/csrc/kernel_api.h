@@ -3,6 +3,8 @@
 
 #include <cstdint>
 
+#include "stream.h"
+
 namespace stg {
 
 constexpr int kMaxThreads = 256;  // largest block the kernels are built for
@@ -11,6 +13,20 @@ constexpr int kDefaultStages = 4;
 enum TrackMode : int32_t { MODE_UNTIL = 0, MODE_LINE = 1, MODE_EBE = 2 };
 
 enum ErrorBits : int32_t { ERR_PIPELINE_TIMEOUT = 1 };
+
+// Opcodes of the plain-ring kernel instantiation: drifts, multipoles,
+// shifts, rotations, dipole edges, cavities, apertures and monitors.  A
+// lattice with none of the beam-field, space-charge or RF-multipole maps is
+// tracked by a kernel compiled without them, which needs fewer registers
+// (no spills at two CTAs per SM) and keeps the dispatch switch short.
+constexpr uint32_t kPlainOps =
+    (1u << OP_END) | (1u << OP_DRIFT) | (1u << OP_DRIFT_EXACT) | (1u << OP_MULTIPOLE) |
+    (1u << OP_MULTIPOLE_CURV) | (1u << OP_CAVITY) | (1u << OP_XYSHIFT) | (1u << OP_SROTATION) |
+    (1u << OP_LIMIT_RECT) | (1u << OP_LIMIT_ELLIPSE) | (1u << OP_LIMIT_RECT_ELLIPSE) |
+    (1u << OP_DIPEDGE) | (1u << OP_MONITOR) | (1u << OP_NOP) | (1u << OP_FAIL) |
+    (1u << OP_FAIL_LOST);
+
+inline bool plain_lattice(uint32_t op_mask) { return (op_mask & ~kPlainOps) == 0u; }
 
 struct EbeDevConfig {
     int64_t order;
@@ -42,12 +58,15 @@ struct TrackParams {
     const int64_t *idx;      // device: particle indices to track (null: i0..i1)
     const int64_t *count;    // device: number of entries of idx
     const double *s_table;   // device: s before element k when a turn starts at s = 0
+    uint32_t op_mask;        // opcodes present in the compiled range (stream.h)
 };
 
 // Launch one tracking kernel on `stream` (a cudaStream_t).  Returns the CUDA
 // error code of the launch (0 on success).
 // blocks_per_sm selects the register tier: 1 (up to 255 registers, no
 // spills) or 2 (at most 128 registers per thread, two CTAs per SM).
+// prm.op_mask selects the instantiation: the plain-ring kernel when every
+// opcode present is in kPlainOps, the full kernel otherwise.
 int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_sm,
                  void *stream);
 size_t track_smem_bytes(int stages, int chunk_words);
@@ -68,6 +87,7 @@ struct BatchLaunch {
     const int64_t *base_turn;     // device: until_turn = *base_turn + turn_offset
     int64_t turn_offset;
     bool fast;
+    bool plain;                   // every variant is a plain ring (kPlainOps)
     int threads, blocks_per_sm;
     unsigned grid;
     size_t smem;
@@ -75,7 +95,8 @@ struct BatchLaunch {
 
 // Set the kernel's shared-memory limit to `smem` and report how many CTAs
 // of `threads` fit on one SM.  Returns the CUDA error code.
-int batch_ctas_per_sm(bool fast, int threads, int blocks_per_sm, size_t smem, int *per_sm);
+int batch_ctas_per_sm(bool fast, bool plain, int threads, int blocks_per_sm, size_t smem,
+                      int *per_sm);
 int launch_batch(const BatchLaunch &b, void *stream);
 
 // Stable selection of the particles with work left (compact.cu): fills

@@ -10,6 +10,7 @@
 #include "lattice.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 
 namespace stg {
@@ -23,6 +24,9 @@ constexpr double kEps0 = 8.854187817620e-12;
 struct Emitter {
     std::vector<uint64_t> recs;     // records, unchunked
     std::vector<uint64_t> rec_len;  // per record
+    // {record, parameter index, offset in the side data}: parameter words
+    // that receive the device address of out-of-line data
+    std::vector<std::array<uint64_t, 3>> side_refs;
     void push(uint32_t op, uint32_t aux, const std::vector<uint64_t> &params)
     {
         uint32_t const n = (uint32_t)params.size() + 1;
@@ -46,6 +50,8 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
     if (begin > end || end > img.num_objects) return bad(err, end, "line range outside the lattice");
     Emitter em;
     out->monitor_elements.clear();
+    out->side.clear();
+    out->side_fixups.clear();
     out->s_table.assign(1, 0.0);
     uint32_t op_mask = 0;
     for (uint64_t i = begin; i < end; ++i) {
@@ -275,8 +281,13 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                 }
             }
             aux = (method != 255u && nv > 0) ? 1u : 0u;
-            p.insert(p.end(), {method, nv, z0, dz, voff, doff, (uint64_t)data.size()});
-            p.insert(p.end(), data.begin(), data.end());
+            // the table stays in global memory (read through L2), its
+            // address in the last parameter word
+            p.insert(p.end(), {method, nv, z0, dz, voff, doff, (uint64_t)data.size(), 0});
+            em.side_refs.push_back({(uint64_t)em.rec_len.size(), (uint64_t)p.size() - 1,
+                                    (uint64_t)out->side.size()});
+            out->side.insert(out->side.end(), data.begin(), data.end());
+            out->side.resize((out->side.size() + 1) & ~(size_t)1);  // 16-byte aligned tables
             break;
         }
         case ST_OBJECT_TYPE_BEAM_MONITOR: {
@@ -341,6 +352,8 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
         pos += n;
     }
     if (used > 0 || nchunks == 0) close_chunk();
+    for (const auto &r : em.side_refs)
+        out->side_fixups.push_back({(uint64_t)out->elem_offset[r[0]] + 1u + r[1], r[2]});
     out->info.num_elements = (int64_t)(end - begin);
     out->info.num_chunks = nchunks;
     out->info.chunk_words = (int32_t)cw;

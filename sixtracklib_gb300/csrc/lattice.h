@@ -32,6 +32,14 @@ struct CompiledStream {
     std::vector<double> s_table;
     // word offset of each element's record in `words` (num_elements entries)
     std::vector<int64_t> elem_offset;
+    // Data kept out of the records (the line-density tables of interpolated
+    // space charge): records stay small, so the chunk size -- and with it
+    // the shared memory of every stage -- does not grow with a table.  The
+    // uploader places `side` in device memory and writes its address plus
+    // the offset into each word listed in `side_fixups` ({word index in
+    // `words`, offset in `side` in words}).
+    std::vector<uint64_t> side;
+    std::vector<std::pair<uint64_t, uint64_t>> side_fixups;
 };
 
 // Compile elements [begin, end) of the image.  Returns false (and sets the

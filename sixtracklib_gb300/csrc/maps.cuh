@@ -68,13 +68,18 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
 
 // ------------------------------------------------------------------- maps
 // s += L for a particle whose s is accumulated (not read from the s table).
-// `s_live` is block-uniform: false once every particle of the block reads s
-// from the table (every turn after the first).  The add is a volatile PTX
-// instruction so that it cannot be speculated out of the branch (the plain
-// C form is issued for every lane and its result selected).
-__device__ __forceinline__ void add_s(PState &p, double L, bool s_live)
+// S_LIVE is a block-uniform property of the pass: false once every particle
+// of the block reads s from the table (every turn after the first), and the
+// instantiation without it has no s update at all -- a guarded add in the
+// element loop would be issued (predicated off) on the FP64 pipe for every
+// drift.  The add is a volatile PTX instruction so that it cannot be
+// speculated out of the per-particle branch.
+template <bool S_LIVE>
+__device__ __forceinline__ void add_s(PState &p, double L)
 {
-    if (s_live && !p.lazy_s) asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(p.s) : "d"(L));
+    if constexpr (S_LIVE) {
+        if (!p.lazy_s) asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(p.s) : "d"(L));
+    }
 }
 
 // be_drift/track.h:45-67.  FAST keeps the reference's rounding of
@@ -83,8 +88,8 @@ __device__ __forceinline__ void add_s(PState &p, double L, bool s_live)
 // from the reference by its own rounding noise, ~1e-16 m per drift.
 // s is only accumulated when the turn did not start at s = +0 (otherwise it
 // comes from the lattice's s table).
-template <bool FAST>
-__device__ __forceinline__ void drift(PState &p, double L, bool s_live = true)
+template <bool FAST, bool S_LIVE = true>
+__device__ __forceinline__ void drift(PState &p, double L)
 {
     double const xp = p.px * p.rpp;
     double const yp = p.py * p.rpp;
@@ -99,18 +104,19 @@ __device__ __forceinline__ void drift(PState &p, double L, bool s_live = true)
         p.y += yp * L;
         p.zeta += L * dzeta;
     }
-    add_s(p, L, s_live);
+    add_s<S_LIVE>(p, L);
 }
 
 // be_drift/track.h:71-97
-__device__ __forceinline__ void drift_exact(PState &p, double L, bool s_live = true)
+template <bool S_LIVE = true>
+__device__ __forceinline__ void drift_exact(PState &p, double L)
 {
     double const opd = p.delta + 1.0;
     double const lpzi = L / sqrt(opd * opd - (p.px * p.px + p.py * p.py));
     double const dzeta = p.rvv * L - opd * lpzi;
     p.x += p.px * lpzi;
     p.y += p.py * lpzi;
-    add_s(p, L, s_live);
+    add_s<S_LIVE>(p, L);
     p.zeta += dzeta;
 }
 
@@ -293,10 +299,13 @@ static __device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec
 // is U(n) = 0.5 Q(n+1) / Q(n) for the three-term recurrence
 // Q(n) = w0 Q(n+1) + (n / 2) Q(n+2), Q(nu+1) = 1, Q(nu+2) = 0; the series
 // V(n) = U(n) (V(n+1) + h^(1-n)) then telescopes to
-// V(1) = sum_{m=1..nc} h^(1-m) 0.5^m Q(m+1) / Q(1).  One complex division
-// per call instead of two real divisions per term (|Q| stays below ~1e30);
-// the values agree with the term-by-term evaluation to rounding (a few
-// 1e-15 relative).
+// V(1) = sum_{m=1..nc} h^(1-m) 0.5^m Q(m+1) / Q(1)
+//      = 0.5 A(1) / Q(1),  A(m) = Q(m+1) + A(m+1) / (2h),  A(nc) = Q(nc+1),
+// a Horner sum taken along the recurrence (two FMAs per term).  One complex
+// division per call instead of two real divisions per term (|Q| stays below
+// ~1e30); 0.5 / h is taken as 0.5 (3.2 q), the product h = 1 / (3.2 q) was
+// formed from.  The values agree with the term-by-term evaluation to
+// rounding (a few 1e-15 relative).
 static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
 {
     double const a_const = 1.12837916709551;
@@ -306,45 +315,40 @@ static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_
     double q1r = 1.0, q1i = 0.0, q2r = 0.0, q2i = 0.0;  // Q(n+1), Q(n+2)
     if (y < ylim && x < xlim) {
         double const q = (1.0 - y / ylim) * sqrt(1.0 - (x / xlim) * (x / xlim));
-        double const h = 1.0 / (3.2 * q);
+        double const q32 = 3.2 * q;
+        double const inv_2h = 0.5 * q32;  // 0.5 / h
         int const nc = 7 + (int)(23.0 * q);
         int const nu = 10 + (int)(21.0 * q);
-        double const w0r = y + 0.5 / h, w0i = x;
-        // c = h^(1-n) 0.5^n at n = nc: 0.5 (0.5 / h)^(nc - 1)
-        double c = 0.5, r = 0.5 / h;
-        for (int e = nc - 1; e > 0; e >>= 1) {
-            if (e & 1) c *= r;
-            r *= r;
-        }
-        double const c_step = 2.0 * h;
-        double sr = 0.0, si = 0.0;
+        double const w0r = y + inv_2h, w0i = x;
+        double ar = 0.0, ai = 0.0;  // A(n)
+        double hn = 0.5 * nu;       // n / 2, exact in steps of 0.5
         for (int n = nu; n > 0; n--) {
             if (n <= nc) {
-                sr = fma(c, q1r, sr);
-                si = fma(c, q1i, si);
-                c *= c_step;
+                ar = fma(ar, inv_2h, q1r);
+                ai = fma(ai, inv_2h, q1i);
             }
-            double const hn = 0.5 * n;
             double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
             double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
             q2r = q1r;
             q2i = q1i;
             q1r = qr;
             q1i = qi;
+            hn -= 0.5;
         }
-        // w = a_const conj(V(1)), V(1) = s / Q(1)
-        double const inv = a_const / fma(q1r, q1r, q1i * q1i);
-        wx = fma(sr, q1r, si * q1i) * inv;
-        wy = fma(sr, q1i, -si * q1r) * inv;
+        // w = a_const conj(V(1)), V(1) = 0.5 A(1) / Q(1)
+        double const inv = 0.5 * a_const / fma(q1r, q1r, q1i * q1i);
+        wx = fma(ar, q1r, ai * q1i) * inv;
+        wy = fma(ar, q1i, -ai * q1r) * inv;
     } else {
         // |w0| is unbounded here: Q(n) = s^(10-n) Q'(n) with s a power of two
         // near |w0| (exact scaling), Q'(n) = (w0 / s) Q'(n+1) + (n / 2 s^2) Q'(n+2)
         int ex;
         frexp(fmax(x, y), &ex);
         double const is = ldexp(1.0, -ex);
+        double const is2 = is * is;  // a power of two: every product below is exact
         double const w0r = y * is, w0i = x * is;
         for (int n = 9; n > 0; n--) {
-            double const hn = 0.5 * n * is * is;
+            double const hn = (0.5 * n) * is2;
             double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
             double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
             q2r = q1r;
@@ -828,7 +832,8 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
 __device__ __forceinline__ double ldp_word(const uint64_t *c, uint64_t off, int64_t i)
 {
     uint64_t const k = off + (uint64_t)i;
-    return (i >= 0 && k < c[14]) ? W(c[15 + k]) : 0.0;
+    const double *table = reinterpret_cast<const double *>(c[15]);
+    return (i >= 0 && k < c[14]) ? __ldg(table + k) : 0.0;
 }
 
 __device__ __forceinline__ double ldp_interpolate(const uint64_t *c, double z)

@@ -49,8 +49,11 @@ enum Op : uint32_t {
     OP_FAIL_LOST = 20,      // failure and particle lost (unknown type id)
     OP_SC_INTERP = 21,      // [N, sigma_x, sigma_y, length, x_co, y_co, fallback,
                             //  min_sigma_diff, method, num_values, z0, dz,
-                            //  values@, derivatives@, nwords, data[nwords]]
-                            // aux bit0: interpolate (else the fallback density)
+                            //  values@, derivatives@, nwords, table address]
+                            // the table (nwords words, values@ / derivatives@
+                            // word offsets into it) lies in device memory
+                            // outside the stream; aux bit0: interpolate (else
+                            // the fallback density)
     OP_COUNT
 };
 

@@ -180,17 +180,20 @@ __device__ __forceinline__ int64_t ebe_index(const EbeDevConfig &c, int64_t pid,
 }
 
 // Apply one element; returns 0 or -1 (reference status).  `lost` is set when
-// the particle leaves the aperture (state becomes 0).
-template <bool FAST>
+// the particle leaves the aperture (state becomes 0).  The PLAIN
+// instantiation compiles only the maps of kPlainOps; the host chooses it
+// for lattices without any other opcode, so its fall-through (failure,
+// particle lost, as for an unknown type id) is never taken.
+template <bool FAST, bool PLAIN, bool S_LIVE>
 __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hdr,
                                      const TrackParams &prm, int64_t cur_elem, int64_t cur_turn,
-                                     int64_t ord, bool s_live)
+                                     int64_t ord)
 {
     uint32_t const op = (uint32_t)(hdr & 0xFF);
     uint32_t const aux = (uint32_t)(hdr >> 32);
     switch (op) {
     case OP_DRIFT:
-        drift<FAST>(p, W(rec[1]), s_live);
+        drift<FAST, S_LIVE>(p, W(rec[1]));
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_MULTIPOLE:
@@ -213,7 +216,7 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         multipole<FAST, true>(p, rec, (int)aux);
         return 0;
     case OP_DRIFT_EXACT:
-        drift_exact(p, W(rec[1]), s_live);
+        drift_exact<S_LIVE>(p, W(rec[1]));
         if (aux & DRIFT_APERTURE) p.state &= (int64_t)inside_global(p, prm.xlim_bits, prm.ylim_bits);
         return 0;
     case OP_LIMIT_RECT:
@@ -227,26 +230,44 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
         p.py += W(rec[2]) * p.y;
         return 0;
     case OP_RF_MULTIPOLE:
-        p = rf_multipole(p, rec, (int)aux);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            p = rf_multipole(p, rec, (int)aux);
+            return 0;
+        }
     case OP_BB4D:
-        p = beam_beam_4d(p, rec);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            p = beam_beam_4d(p, rec);
+            return 0;
+        }
     case OP_BB6D:
-        if (aux & BB6D_ROUND)
-            p = beam_beam_6d<true, FAST>(p, rec, (int)(aux & BB6D_SLICES));
-        else
-            p = beam_beam_6d<false, FAST>(p, rec, (int)aux);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            if (aux & BB6D_ROUND)
+                p = beam_beam_6d<true, FAST>(p, rec, (int)(aux & BB6D_SLICES));
+            else
+                p = beam_beam_6d<false, FAST>(p, rec, (int)aux);
+            return 0;
+        }
     case OP_SC_COASTING:
-        p = sc_coasting(p, rec);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            p = sc_coasting(p, rec);
+            return 0;
+        }
     case OP_SC_QGAUSS:
-        p = sc_qgauss<FAST>(p, rec, aux);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            p = sc_qgauss<FAST>(p, rec, aux);
+            return 0;
+        }
     case OP_SC_INTERP:
-        p = sc_interpolated(p, rec, aux);
-        return 0;
+        if constexpr (PLAIN) break;
+        else {
+            p = sc_interpolated(p, rec, aux);
+            return 0;
+        }
     case OP_MONITOR: {
         uint64_t *out = reinterpret_cast<uint64_t *>(rec[8]);
         if (out == nullptr) return 0;
@@ -265,12 +286,51 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
     case OP_FAIL:
         return -1;
     default:  // OP_FAIL_LOST: unknown type id
-        p.state = 0;
-        return -1;
+        break;
     }
+    p.state = 0;
+    return -1;
 }
 
 }  // namespace
+
+// The records of one staged chunk, in order, for the calling thread's
+// particle (lanes whose particle takes no part are predicated off).
+// S_LIVE (block-uniform for the pass): some particle of the block
+// accumulates s, so drifts carry the s update.
+template <bool FAST, bool PLAIN, bool S_LIVE>
+__device__ __forceinline__ void walk_chunk(PState &p, const uint64_t *rec, const TrackParams &prm,
+                                           bool &part, bool &active, int &status,
+                                           int64_t &stop_elem, int64_t &ord, int64_t &ae,
+                                           int64_t start_elem)
+{
+    while (true) {
+        uint64_t const hdr = rec[0];
+        uint32_t const nw = (uint32_t)((hdr >> 8) & 0xFFFFFF);
+        if ((uint32_t)(hdr & 0xFF) == OP_END || nw == 0) break;
+        if (part) {
+            if (prm.mode == MODE_EBE) {
+                int64_t const j = ebe_index(prm.ebe, p.pid, ae, p.at_turn);
+                if (j >= 0 && j < prm.ebe_cap)
+                    store_record(p, prm.ebe_out, prm.ebe_cap, j, ae, p.at_turn,
+                                 p.lazy_s ? prm.s_table[ord] : p.s);
+            }
+            int const rc =
+                apply<FAST, PLAIN, S_LIVE>(p, rec, hdr, prm, start_elem + ord, p.at_turn, ord);
+            if (rc != 0 || p.state != 1) {
+                status |= rc;
+                part = false;
+                active = false;
+                stop_elem = ord;
+                if (p.lazy_s) p.s = prm.s_table[ord + 1];
+            } else {
+                ++ae;
+            }
+        }
+        ++ord;
+        rec += nw;
+    }
+}
 
 __device__ __forceinline__ void mbar_inval(uint64_t *bar)
 {
@@ -284,7 +344,7 @@ __device__ __forceinline__ void mbar_inval(uint64_t *bar)
 // 16 words of mbarriers followed by prm.stages chunk buffers.  Returns with
 // every copy it issued complete; the caller invalidates the barriers before
 // the shared memory is used again.
-template <bool FAST>
+template <bool FAST, bool PLAIN>
 __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, uint64_t *smem)
 {
     int const stages = prm.stages;
@@ -379,32 +439,12 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
                 }
             }
             const uint64_t *rec = bufs + (size_t)buf * cw;
-            while (true) {
-                uint64_t const hdr = rec[0];
-                uint32_t const nw = (uint32_t)((hdr >> 8) & 0xFFFFFF);
-                if ((uint32_t)(hdr & 0xFF) == OP_END || nw == 0) break;
-                if (part) {
-                    if (prm.mode == MODE_EBE) {
-                        int64_t const j = ebe_index(prm.ebe, p.pid, ae, p.at_turn);
-                        if (j >= 0 && j < prm.ebe_cap)
-                            store_record(p, prm.ebe_out, prm.ebe_cap, j, ae, p.at_turn,
-                                         p.lazy_s ? prm.s_table[ord] : p.s);
-                    }
-                    int const rc =
-                        apply<FAST>(p, rec, hdr, prm, start_elem + ord, p.at_turn, ord, s_live);
-                    if (rc != 0 || p.state != 1) {
-                        status |= rc;
-                        part = false;
-                        active = false;
-                        stop_elem = ord;
-                        if (p.lazy_s) p.s = prm.s_table[ord + 1];
-                    } else {
-                        ++ae;
-                    }
-                }
-                ++ord;
-                rec += nw;
-            }
+            if (s_live)
+                walk_chunk<FAST, PLAIN, true>(p, rec, prm, part, active, status, stop_elem, ord,
+                                              ae, start_elem);
+            else
+                walk_chunk<FAST, PLAIN, false>(p, rec, prm, part, active, status, stop_elem, ord,
+                                               ae, start_elem);
             if (!resident) {
                 __syncthreads();  // every warp is done with this stage buffer
                 if (threadIdx.x == 0) {
@@ -493,18 +533,18 @@ __device__ __forceinline__ void track_block(const TrackParams &prm, int64_t t, u
     k[20 * n + i] = p.state;
 }
 
-template <bool FAST, int MIN_BLOCKS>
+template <bool FAST, int MIN_BLOCKS, bool PLAIN>
 __global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS) track_kernel(TrackParams prm)
 {
     extern __shared__ __align__(128) uint64_t smem[];
-    track_block<FAST>(prm, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, smem);
+    track_block<FAST, PLAIN>(prm, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, smem);
 }
 
 // Persistent batched kernel: each CTA takes work items (a tile of
 // blockDim.x particles of one lattice variant) from a global counter until
 // none is left, and tracks the tile until turn *base_turn + turn_offset with
 // that variant's lattice.  Items are ordered longest first by the host.
-template <bool FAST, int MIN_BLOCKS>
+template <bool FAST, int MIN_BLOCKS, bool PLAIN>
 __global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS)
     batch_kernel(const TrackParams *variants, const BatchItem *items, int32_t num_items,
                  int32_t *counter, const int64_t *base_turn, int64_t turn_offset)
@@ -525,25 +565,26 @@ __global__ void __launch_bounds__(kMaxThreads, MIN_BLOCKS)
         prm.count = nullptr;
         prm.i0 = w.first;
         prm.i1 = (w.first + blockDim.x < prm.n) ? w.first + blockDim.x : prm.n;
-        track_block<FAST>(prm, threadIdx.x, smem);
+        track_block<FAST, PLAIN>(prm, threadIdx.x, smem);
         __syncthreads();
         if (threadIdx.x == 0)
             for (int b = 0; b < prm.stages; ++b) mbar_inval(&smem[b]);
     }
 }
 
-template __global__ void track_kernel<false, 1>(TrackParams);
-template __global__ void track_kernel<true, 1>(TrackParams);
-template __global__ void track_kernel<false, 2>(TrackParams);
-template __global__ void track_kernel<true, 2>(TrackParams);
-template __global__ void batch_kernel<false, 1>(const TrackParams *, const BatchItem *, int32_t,
-                                                int32_t *, const int64_t *, int64_t);
-template __global__ void batch_kernel<true, 1>(const TrackParams *, const BatchItem *, int32_t,
-                                               int32_t *, const int64_t *, int64_t);
-template __global__ void batch_kernel<false, 2>(const TrackParams *, const BatchItem *, int32_t,
-                                                int32_t *, const int64_t *, int64_t);
-template __global__ void batch_kernel<true, 2>(const TrackParams *, const BatchItem *, int32_t,
-                                               int32_t *, const int64_t *, int64_t);
+#define STG_INSTANTIATE(F, M, P)                                                             \
+    template __global__ void track_kernel<F, M, P>(TrackParams);                             \
+    template __global__ void batch_kernel<F, M, P>(const TrackParams *, const BatchItem *,    \
+                                                   int32_t, int32_t *, const int64_t *, int64_t);
+STG_INSTANTIATE(false, 1, false)
+STG_INSTANTIATE(true, 1, false)
+STG_INSTANTIATE(false, 2, false)
+STG_INSTANTIATE(true, 2, false)
+STG_INSTANTIATE(false, 1, true)
+STG_INSTANTIATE(true, 1, true)
+STG_INSTANTIATE(false, 2, true)
+STG_INSTANTIATE(true, 2, true)
+#undef STG_INSTANTIATE
 
 }  // namespace stg
 
@@ -554,15 +595,26 @@ size_t track_smem_bytes(int stages, int chunk_words)
     return (size_t)(16 + (size_t)stages * chunk_words) * sizeof(uint64_t);
 }
 
-template <bool FAST, int MB>
+template <bool FAST, int MB, bool PLAIN>
 static int launch_one(const TrackParams &prm, unsigned blocks, int threads, size_t smem,
                       cudaStream_t s)
 {
-    cudaError_t err = cudaFuncSetAttribute(track_kernel<FAST, MB>,
+    cudaError_t err = cudaFuncSetAttribute(track_kernel<FAST, MB, PLAIN>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
-    track_kernel<FAST, MB><<<blocks, threads, smem, s>>>(prm);
+    track_kernel<FAST, MB, PLAIN><<<blocks, threads, smem, s>>>(prm);
     return (int)cudaGetLastError();
+}
+
+template <bool PLAIN>
+static int launch_tier(const TrackParams &prm, bool fast, bool two, unsigned blocks, int threads,
+                       size_t smem, cudaStream_t s)
+{
+    if (fast)
+        return two ? launch_one<true, 2, PLAIN>(prm, blocks, threads, smem, s)
+                   : launch_one<true, 1, PLAIN>(prm, blocks, threads, smem, s);
+    return two ? launch_one<false, 2, PLAIN>(prm, blocks, threads, smem, s)
+               : launch_one<false, 1, PLAIN>(prm, blocks, threads, smem, s);
 }
 
 int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_sm, void *stream)
@@ -574,30 +626,39 @@ int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_
     size_t const smem = track_smem_bytes(prm.stages, prm.chunk_words);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     bool const two = blocks_per_sm >= 2;
-    if (fast)
-        return two ? launch_one<true, 2>(prm, (unsigned)blocks, threads, smem, s)
-                   : launch_one<true, 1>(prm, (unsigned)blocks, threads, smem, s);
-    return two ? launch_one<false, 2>(prm, (unsigned)blocks, threads, smem, s)
-               : launch_one<false, 1>(prm, (unsigned)blocks, threads, smem, s);
+    if (plain_lattice(prm.op_mask))
+        return launch_tier<true>(prm, fast, two, (unsigned)blocks, threads, smem, s);
+    return launch_tier<false>(prm, fast, two, (unsigned)blocks, threads, smem, s);
 }
 
-template <bool FAST, int MB>
+template <bool FAST, int MB, bool PLAIN>
 static cudaError_t batch_occupancy(int threads, size_t smem, int *per_sm)
 {
-    cudaError_t err = cudaFuncSetAttribute(batch_kernel<FAST, MB>,
+    cudaError_t err = cudaFuncSetAttribute(batch_kernel<FAST, MB, PLAIN>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<FAST, MB>, threads,
-                                                         smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<FAST, MB, PLAIN>,
+                                                         threads, smem);
 }
 
-int batch_ctas_per_sm(bool fast, int threads, int blocks_per_sm, size_t smem, int *per_sm)
+template <bool PLAIN>
+static cudaError_t batch_occupancy_tier(bool fast, bool two, int threads, size_t smem,
+                                        int *per_sm)
+{
+    if (fast)
+        return two ? batch_occupancy<true, 2, PLAIN>(threads, smem, per_sm)
+                   : batch_occupancy<true, 1, PLAIN>(threads, smem, per_sm);
+    return two ? batch_occupancy<false, 2, PLAIN>(threads, smem, per_sm)
+               : batch_occupancy<false, 1, PLAIN>(threads, smem, per_sm);
+}
+
+int batch_ctas_per_sm(bool fast, bool plain, int threads, int blocks_per_sm, size_t smem,
+                      int *per_sm)
 {
     bool const two = blocks_per_sm >= 2;
-    cudaError_t err = fast ? (two ? batch_occupancy<true, 2>(threads, smem, per_sm)
-                                  : batch_occupancy<true, 1>(threads, smem, per_sm))
-                           : (two ? batch_occupancy<false, 2>(threads, smem, per_sm)
-                                  : batch_occupancy<false, 1>(threads, smem, per_sm));
+    cudaError_t const err =
+        plain ? batch_occupancy_tier<true>(fast, two, threads, smem, per_sm)
+              : batch_occupancy_tier<false>(fast, two, threads, smem, per_sm);
     return (int)err;
 }
 
@@ -605,19 +666,26 @@ int launch_batch(const BatchLaunch &b, void *stream)
 {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     bool const two = b.blocks_per_sm >= 2;
-#define STG_BATCH(F, M)                                                                         \
-    batch_kernel<F, M><<<b.grid, b.threads, b.smem, s>>>(b.variants, b.items, b.num_items,      \
-                                                         b.counter, b.base_turn, b.turn_offset)
-    if (b.fast) {
-        if (two)
-            STG_BATCH(true, 2);
-        else
-            STG_BATCH(true, 1);
+#define STG_BATCH(F, M, P)                                                                      \
+    batch_kernel<F, M, P><<<b.grid, b.threads, b.smem, s>>>(b.variants, b.items, b.num_items,   \
+                                                            b.counter, b.base_turn,              \
+                                                            b.turn_offset)
+    if (b.plain) {
+        if (b.fast) {
+            if (two) STG_BATCH(true, 2, true);
+            else STG_BATCH(true, 1, true);
+        } else {
+            if (two) STG_BATCH(false, 2, true);
+            else STG_BATCH(false, 1, true);
+        }
     } else {
-        if (two)
-            STG_BATCH(false, 2);
-        else
-            STG_BATCH(false, 1);
+        if (b.fast) {
+            if (two) STG_BATCH(true, 2, false);
+            else STG_BATCH(true, 1, false);
+        } else {
+            if (two) STG_BATCH(false, 2, false);
+            else STG_BATCH(false, 1, false);
+        }
     }
 #undef STG_BATCH
     return (int)cudaGetLastError();
