@@ -454,6 +454,25 @@ int32_t st_TrackJobNew_collect(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_particles(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_beam_elements(st_TrackJobBaseNew *job);
 int32_t st_TrackJobNew_push_output(st_TrackJobBaseNew *job);
+/* Debug mode (track/track_job_base.h:182-189, the CUDA job's debug
+ * kernels track/track_kernel_impl.h:149-250).  In debug mode every
+ * tracking call first validates its inputs and records the outcome in a
+ * debug register: flags from bit 32 up as the reference numbers them (2^32
+ * particle index, 2^33 particle buffer null, 2^34 beam-element buffer null,
+ * 2^36 particle-set index, 2^37 / 2^38 particle / beam-element buffer needs
+ * remapping, 2^39 line boundaries, 2^40 until_turn), then the engine's own
+ * (2^41 a shared-memory pipeline wait timed out, 2^42 elem-by-elem tracking
+ * without an elem-by-elem output), and the track status in the low 32 bits
+ * (control/debug_register.h:59-80).  A raised flag makes the call return
+ * -1 without tracking.  enable / disable return 0 (-1 for a null job);
+ * collect_debug_flag returns 0 in debug mode (the register lives on the
+ * host).  st_TrackJobNew_get_debug_register has no counterpart in the
+ * reference (which keeps its register inside the job): it returns it. */
+bool st_TrackJobNew_is_in_debug_mode(const st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_enable_debug_mode(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_disable_debug_mode(st_TrackJobBaseNew *job);
+int32_t st_TrackJobNew_collect_debug_flag(st_TrackJobBaseNew *job);
+uint64_t st_TrackJobNew_get_debug_register(const st_TrackJobBaseNew *job);
 /* Stored buffers and address assignment (common/track_job.h: stored
  * buffers, NS(AssignAddressItem) of buffer/assign_address_item.h).  A stored
  * buffer is a caller's st_Buffer kept by the job under an id >= 1024.  With
@@ -642,7 +661,12 @@ st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *lat, void *d_col
                                               uint64_t end_idx, bool finish_turn,
                                               void *stream);
 /* Launch without waiting for the status word (asynchronous on `stream`);
- * st_DeviceLattice_last_status() synchronises and returns it. */
+ * st_DeviceLattice_last_status() synchronises and returns it.  The
+ * particle-selection scratch and the status words are shared by every call
+ * on a GPU: a call that uses them waits on the GPU for the previous such
+ * call's work to finish, also when it was launched on another stream (an
+ * event recorded per GPU), so overlapping calls are serialised, not raced.
+ * last_status() reports the status of the last call on the lattice's GPU. */
 int32_t st_DeviceLattice_launch_until(st_DeviceLattice *lat, void *d_cols,
                                       int64_t num_particles, int64_t until_turn, void *stream);
 st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *lat);
@@ -686,7 +710,9 @@ st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *lat, int64_t
  * Pass d_param_begin = NULL for coordinate derivatives only.  Every map the
  * engine tracks has an adjoint; lattices with a map compiled out (TriCub) or
  * an unknown type id are refused (-1).
- * Asynchronous on `stream`; device pointers except `lat`. */
+ * Asynchronous on `stream`; device pointers except `lat`.  Uses the GPU's
+ * shared particle-selection scratch, ordered after (and before) other calls
+ * that use it as st_DeviceLattice_launch_until describes. */
 st_track_status_t st_DeviceLattice_adjoint_turns(st_DeviceLattice *lat, const void *d_start,
                                                  const void *d_end, int64_t num_particles,
                                                  int64_t turn_begin, int64_t turn_end,

@@ -35,6 +35,7 @@
 #include <string>
 
 #include "common.h"
+#include "device_guard.h"
 #include "kernel_api.h"
 #include "lattice_view.h"
 #include "dual.cuh"
@@ -885,6 +886,7 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
     const int32_t *d_param_kind, const int32_t *d_param_id, int32_t num_slots, double *d_grad,
     void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     LatticeLaunchView v;
     if (!device_lattice_view(lat, &v)) {
@@ -912,7 +914,12 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
         return -1;
     }
     uint64_t *scratch = device_scratch(v.device, select_scratch_words(n));
-    if (!scratch) return -1;
+    if (!scratch || !shared_scratch_begin(v.device, stream)) return -1;
+    struct ScratchDone {
+        int device;
+        void *stream;
+        ~ScratchDone() { shared_scratch_end(device, stream); }
+    } done{v.device, stream};
     int64_t *idx = nullptr, *count = nullptr;
     // alive at turn_begin with turns left before turn_end
     int rc = launch_select(static_cast<const uint64_t *>(d_start), n, 0, n, MODE_UNTIL, turn_end,

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "common.h"
+#include "device_guard.h"
 #include "kernel_api.h"
 #include "lattice_view.h"
 
@@ -114,6 +115,7 @@ struct Plan {
     int32_t num_items = 0;
     unsigned grid = 0;
     size_t smem = 0;
+    bool plain = false;  // every variant is a plain ring: the plain-ring kernel
     void release()
     {
         if (d_variants) cudaFree(d_variants);
@@ -176,8 +178,10 @@ bool build_plan(st_BatchTracker *b, const Shape &sh, const std::vector<uint64_t 
     Plan p;
     p.shape = sh;
     p.smem = track_smem_bytes(sh.stages, max_chunk_words(b));
+    p.plain = true;
+    for (const auto &v : b->views) p.plain = p.plain && plain_lattice(v.op_mask);
     int per_sm = 0;
-    int rc = batch_ctas_per_sm(b->fast, sh.threads, sh.blocks_per_sm, p.smem, &per_sm);
+    int rc = batch_ctas_per_sm(b->fast, p.plain, sh.threads, sh.blocks_per_sm, p.smem, &per_sm);
     if (rc != 0 || per_sm <= 0) {
         set_error("batch: launch shape does not fit an SM (threads " +
                   std::to_string(sh.threads) + ", stages " + std::to_string(sh.stages) + ")");
@@ -206,6 +210,7 @@ bool build_plan(st_BatchTracker *b, const Shape &sh, const std::vector<uint64_t 
         t.status = b->d_flags;
         t.error = b->d_flags + 1;
         t.s_table = lv.s_table;
+        t.op_mask = lv.op_mask;
         if (lv.num_elements == 0) continue;  // nothing to apply
         for (int64_t f = 0; f < n[v]; f += sh.threads) items.push_back({(int32_t)v, 0, f});
     }
@@ -267,6 +272,7 @@ bool enqueue_turns(st_BatchTracker *b, const Plan &p, int64_t turns, cudaStream_
         L.base_turn = b->d_base;
         L.turn_offset = std::min(turns, (k + 1) * tpl);
         L.fast = b->fast;
+        L.plain = p.plain;
         L.threads = p.shape.threads;
         L.blocks_per_sm = p.shape.blocks_per_sm;
         L.grid = p.grid;
@@ -313,6 +319,7 @@ extern "C" {
 st_BatchTracker *st_BatchTracker_new(st_DeviceLattice *const *lattices, int32_t num_variants,
                                      const char *config)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!lattices || num_variants <= 0) {
         set_error("batch: no lattices");
@@ -355,11 +362,16 @@ st_BatchTracker *st_BatchTracker_new(st_DeviceLattice *const *lattices, int32_t 
     return b.release();
 }
 
-void st_BatchTracker_delete(st_BatchTracker *b) { delete b; }
+void st_BatchTracker_delete(st_BatchTracker *b)
+{
+    DeviceGuard guard;  // the caller's current device is restored on return
+    delete b;
+}
 
 int32_t st_BatchTracker_set_particles(st_BatchTracker *b, void *const *d_cols,
                                       const int64_t *num_particles)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!b || !d_cols || !num_particles) {
         set_error("batch: invalid arguments");
@@ -394,6 +406,7 @@ int32_t st_BatchTracker_set_particles(st_BatchTracker *b, void *const *d_cols,
 st_track_status_t st_BatchTracker_track_until(st_BatchTracker *b, int64_t from_turn,
                                               int64_t until_turn, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!b || !b->plan.d_variants) {
         set_error("batch: particles not set");
@@ -415,6 +428,7 @@ st_track_status_t st_BatchTracker_track_until(st_BatchTracker *b, int64_t from_t
 
 int32_t st_BatchTracker_capture(st_BatchTracker *b, int64_t turns_per_replay)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!b || !b->plan.d_variants || turns_per_replay <= 0) {
         set_error("batch: particles not set or bad turn count");
@@ -449,6 +463,7 @@ int32_t st_BatchTracker_capture(st_BatchTracker *b, int64_t turns_per_replay)
 
 int32_t st_BatchTracker_set_turn(st_BatchTracker *b, int64_t turn, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!b) return -1;
     cudaSetDevice(b->device);
     set_turn_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(b->d_base, turn);
@@ -457,6 +472,7 @@ int32_t st_BatchTracker_set_turn(st_BatchTracker *b, int64_t turn, void *stream)
 
 int32_t st_BatchTracker_replay(st_BatchTracker *b, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!b || !b->exec) {
         set_error("batch: no captured graph");
@@ -473,6 +489,7 @@ int32_t st_BatchTracker_replay(st_BatchTracker *b, void *stream)
 
 st_track_status_t st_BatchTracker_status(st_BatchTracker *b, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!b) return -1;
     cudaSetDevice(b->device);
     return read_status(b, static_cast<cudaStream_t>(stream));
@@ -493,6 +510,7 @@ int32_t st_BatchTracker_get_shape(const st_BatchTracker *b, int32_t *threads,
 int32_t st_BatchTracker_autotune(st_BatchTracker *b, double sample_fraction, int64_t trial_turns,
                                  double *best_ms)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!b || !b->plan.d_variants || trial_turns <= 0 || !(sample_fraction > 0.0)) {
         set_error("batch autotune: particles not set or bad arguments");

@@ -27,6 +27,7 @@
 
 #include "common.h"
 #include "kernel_api.h"
+#include "device_guard.h"
 #include "lattice.h"
 
 extern "C" uint64_t stg_buffer_generation(const st_Buffer *b);
@@ -164,6 +165,8 @@ struct Device {
     // scratch for the active-particle selection (grown on demand, kept)
     uint64_t *scratch = nullptr;
     int64_t scratch_words = 0;
+    // recorded after the last work that used `scratch` or `d_flags`
+    cudaEvent_t shared_done = nullptr;
 };
 
 static std::mutex g_dev_mu;
@@ -196,13 +199,51 @@ static Device *get_device(int id)
     d->id = id;
     if (!cuda_ok(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaMalloc(&d->d_flags, 2 * sizeof(int32_t)), "cudaMalloc") ||
-        !cuda_ok(cudaMallocHost(&d->h_flags, 4 * sizeof(int32_t)), "cudaMallocHost")) {
+        !cuda_ok(cudaMallocHost(&d->h_flags, 4 * sizeof(int32_t)), "cudaMallocHost") ||
+        !cuda_ok(cudaEventCreateWithFlags(&d->shared_done, cudaEventDisableTiming),
+                 "cudaEventCreate")) {
         delete d;
         return nullptr;
     }
     g_devices[id] = d;
     return d;
 }
+
+// The selection scratch and the status words of a device are shared by
+// every call on that device.  Work that uses them is ordered after the
+// previous such work on the GPU, also when the two calls launch on different
+// streams and return before their kernels finish (the asynchronous entry
+// points): the stream first waits for the event the previous user recorded,
+// and records it again after its own work.  Inside a stream capture the
+// graph orders its own nodes and no event is waited for or recorded.
+static bool stream_capturing(cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+static bool shared_use_begin(Device *dev, cudaStream_t s)
+{
+    if (stream_capturing(s)) return true;
+    return cuda_ok(cudaStreamWaitEvent(s, dev->shared_done, 0), "cudaStreamWaitEvent");
+}
+
+static void shared_use_end(Device *dev, cudaStream_t s)
+{
+    if (!stream_capturing(s)) cudaEventRecord(dev->shared_done, s);
+}
+
+// Brackets one call's use of the shared scratch and status words.
+struct SharedUse {
+    Device *dev;
+    cudaStream_t s;
+    bool ok;
+    SharedUse(Device *d, cudaStream_t st) : dev(d), s(st), ok(shared_use_begin(d, st)) {}
+    ~SharedUse()
+    {
+        if (ok) shared_use_end(dev, s);
+    }
+};
 
 // ------------------------------------------------------- device stream
 struct DevStream {
@@ -235,8 +276,18 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     size_t const bytes = s->cs.words.size() * 8;
     size_t const sbytes = s->cs.s_table.size() * 8;
     size_t const obytes = s->cs.elem_offset.size() * 8;
+    size_t const side_at = (bytes + sbytes + obytes + 15) & ~(size_t)15;
+    size_t const side_bytes = s->cs.side.size() * 8;
     if (!cuda_ok(cudaSetDevice(dev->id), "cudaSetDevice") ||
-        !cuda_ok(cudaMalloc(&s->d, bytes + sbytes + obytes + 8), "cudaMalloc(lattice)") ||
+        !cuda_ok(cudaMalloc(&s->d, side_at + side_bytes + 8), "cudaMalloc(lattice)"))
+        return nullptr;
+    // out-of-line tables: their device addresses go into the records
+    uint64_t const side_base = (uint64_t)(uintptr_t)s->d + side_at;
+    for (const auto &f : s->cs.side_fixups) s->cs.words[f.first] = side_base + f.second * 8u;
+    if ((side_bytes > 0 &&
+         !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + side_at, s->cs.side.data(),
+                             side_bytes, cudaMemcpyHostToDevice),
+                  "cudaMemcpy(line-density tables)")) ||
         !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + bytes + sbytes,
                             s->cs.elem_offset.data(), obytes, cudaMemcpyHostToDevice),
                  "cudaMemcpy(element offsets)") ||
@@ -297,9 +348,12 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
     prm.ebe_out = ebe_out;
     prm.ebe_cap = ebe_cap;
     prm.s_table = ds.s_table;
+    prm.op_mask = ds.cs.info.op_mask;
     if (ebe) prm.ebe = *ebe;
     // stream 0 is the legacy default stream (what torch reports for its
     // default stream): launch there, never substitute another stream
+    SharedUse shared(dev, stream);
+    if (!shared.ok) return -1;
     if (!cuda_ok(cudaMemsetAsync(dev->d_flags, 0, 2 * sizeof(int32_t), stream), "cudaMemsetAsync"))
         return -1;
     if (i1 > i0 && mode != MODE_EBE) {
@@ -369,7 +423,9 @@ static int32_t run_track(Device *dev, const Options &opt, const DevStream &ds, u
         !cuda_ok(cudaStreamSynchronize(stream), "track kernel"))
         return -1;
     if (dev->h_flags[1] != 0) {
-        set_error("track kernel: shared-memory pipeline wait timed out; particles left unchanged");
+        set_error("track kernel: a shared-memory pipeline wait timed out; the blocks that timed "
+                  "out left their particles unchanged, other blocks (and earlier launches of "
+                  "the call) may have advanced theirs");
         return -1;
     }
     return dev->h_flags[0];
@@ -431,6 +487,7 @@ static int32_t track_host(st_Particles *p, int64_t i0, int64_t i1, const st_Buff
                           int mode, int64_t until, uint64_t lb, uint64_t le, bool finish,
                           const st_ElemByElemConfig *ebe_cfg)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!p || !belems) {
         set_error("null particles or beam-elements buffer");
@@ -594,6 +651,7 @@ extern "C" {
 st_DeviceLattice *st_DeviceLattice_new(const unsigned char *image, st_buffer_size_t size,
                                        const char *config)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     std::unique_ptr<st_DeviceLattice> L(new st_DeviceLattice());
     std::string err;
@@ -630,6 +688,7 @@ st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *L, int64_t n
                                                   const int64_t *element, const int32_t *kind,
                                                   const double *value)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!L || num < 0 || (num > 0 && (!element || !kind || !value))) {
         set_error("set_parameters: invalid arguments");
@@ -695,9 +754,13 @@ st_track_status_t st_DeviceLattice_set_parameters(st_DeviceLattice *L, int64_t n
 st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols, int64_t n,
                                                int64_t until_turn, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
-    if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
+    if (L->full->cs.info.num_elements == 0) {  // track/track.h:617: an empty lattice fails
+        set_error("st_DeviceLattice_track_until: empty lattice");
+        return -1;
+    }
     cudaSetDevice(L->dev->id);
     return run_track(L->dev, L->opt, *L->full, (uint64_t *)d_cols, n, 0, n, MODE_UNTIL,
                      until_turn, false, nullptr, 0, nullptr, (cudaStream_t)stream);
@@ -706,6 +769,7 @@ st_track_status_t st_DeviceLattice_track_until(st_DeviceLattice *L, void *d_cols
 st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *L, void *d_cols, int64_t n,
                                               uint64_t b, uint64_t e, bool finish, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
     auto key = std::make_pair(b, e);
@@ -726,9 +790,13 @@ st_track_status_t st_DeviceLattice_track_line(st_DeviceLattice *L, void *d_cols,
 int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t n,
                                       int64_t until_turn, void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (L && n == 0) return 0;
     if (!L || !d_cols) return -1;
-    if (L->full->cs.info.num_elements == 0) return n > 0 ? -1 : 0;
+    if (L->full->cs.info.num_elements == 0) {  // track/track.h:617: an empty lattice fails
+        set_error("st_DeviceLattice_launch_until: empty lattice");
+        return -1;
+    }
     cudaSetDevice(L->dev->id);
     L->last_stream = (cudaStream_t)stream;
     return run_track(L->dev, L->opt, *L->full, (uint64_t *)d_cols, n, 0, n, MODE_UNTIL,
@@ -737,8 +805,10 @@ int32_t st_DeviceLattice_launch_until(st_DeviceLattice *L, void *d_cols, int64_t
 
 st_track_status_t st_DeviceLattice_last_status(st_DeviceLattice *L)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!L) return -1;
     cudaStream_t s = L->last_stream;
+    if (!shared_use_begin(L->dev, s)) return -1;
     if (!cuda_ok(cudaMemcpyAsync(L->dev->h_flags, L->dev->d_flags, 2 * sizeof(int32_t),
                                  cudaMemcpyDeviceToHost, s),
                  "cudaMemcpyAsync(status)") ||
@@ -789,6 +859,10 @@ struct st_TrackJob {
     // device column addresses of the particle sets (fetch_particle_addresses)
     std::vector<st_ParticlesAddr> paddr;
     std::vector<bool> paddr_set;
+    // debug mode (track/track_job_base.h:182-189): inputs validated before
+    // every tracking call, the outcome kept in a debug register
+    bool debug_mode = false;
+    uint64_t debug_reg = 0;
     // stored buffers (id -> buffer, owned) and assignment items; kept
     // across reset, freed with the job
     std::map<uint64_t, std::pair<st_Buffer *, bool>> stored;
@@ -968,6 +1042,7 @@ bool compile_job_lattice(st_TrackJob *j)
 bool setup_job(st_TrackJob *j, st_Buffer *pb, st_buffer_size_t nsets, const st_buffer_size_t *idx,
                st_Buffer *eb, st_Buffer *ob, st_buffer_size_t until_ebe)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     j->release();
     if (!pb || !eb) {
         set_error("TrackJob: particles and beam-elements buffers are required");
@@ -1107,6 +1182,7 @@ bool arch_ok(const char *arch)
 
 st_TrackJob *make_job(const char *arch, const char *cfg)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     if (!arch_ok(arch)) return nullptr;
     std::unique_ptr<st_TrackJob> j(new st_TrackJob());
@@ -1177,20 +1253,92 @@ void st_TrackJob_clear(st_TrackJob *j)
     if (j) j->release();
 }
 
+}  // extern "C"
+
+// Debug register of a job in debug mode (the reference's CUDA debug
+// kernels, track/track_kernel_impl.h:149-250): input flags from
+// SIXTRL_ARCH_DEBUGGING_MIN_FLAG = 2^32 up (control/definitions.h:105-117),
+// the track status in the low 32 bits (control/debug_register.h:59-80).
+constexpr uint64_t kDbgParticleIdxIllegal = 1ull << 32;
+constexpr uint64_t kDbgPbufferNull = 1ull << 33;
+constexpr uint64_t kDbgBelemBufferNull = 1ull << 34;
+constexpr uint64_t kDbgPsetIndexIllegal = 1ull << 36;
+constexpr uint64_t kDbgPbufferRemap = 1ull << 37;
+constexpr uint64_t kDbgBelemBufferRemap = 1ull << 38;
+constexpr uint64_t kDbgLineBoundariesIllegal = 1ull << 39;
+constexpr uint64_t kDbgUntilTurnIllegal = 1ull << 40;
+// the engine's own flags, above the reference's
+constexpr uint64_t kDbgPipelineTimeout = 1ull << 41;
+constexpr uint64_t kDbgNoElemByElemOutput = 1ull << 42;
+
+static uint64_t debug_input_flags(const st_TrackJob *j, int64_t until_turn, bool line,
+                                  uint64_t b, uint64_t e)
+{
+    uint64_t f = 0;
+    if (!j->pbuf) f |= kDbgPbufferNull;
+    if (!j->ebuf) f |= kDbgBelemBufferNull;
+    if (j->pbuf && st_Buffer_needs_remapping(j->pbuf)) f |= kDbgPbufferRemap;
+    if (j->ebuf && st_Buffer_needs_remapping(j->ebuf)) f |= kDbgBelemBufferRemap;
+    if (j->pbuf)
+        for (st_buffer_size_t k : j->psets)
+            if (k >= st_Buffer_get_num_of_objects(j->pbuf) ||
+                !st_Particles_buffer_get_const_particles(j->pbuf, k))
+                f |= kDbgPsetIndexIllegal;
+    if (j->n_total < 0) f |= kDbgParticleIdxIllegal;
+    if (until_turn < 0) f |= kDbgUntilTurnIllegal;
+    if (line && (b > e || !j->ebuf || e > st_Buffer_get_num_of_objects(j->ebuf)))
+        f |= kDbgLineBoundariesIllegal;
+    return f;
+}
+
+// Runs `track` unless the inputs fail validation, and records the outcome;
+// returns the reference's status: the track status, or failure when any
+// flag is raised.
+template <class F>
+static st_track_status_t debug_track(st_TrackJob *j, uint64_t flags, F track)
+{
+    int32_t status = -1;
+    if (flags == 0) {
+        status = track();
+        if (j->dev && j->dev->h_flags[1] != 0) flags |= kDbgPipelineTimeout;
+    }
+    j->debug_reg = flags | (uint64_t)(uint32_t)status;
+    return flags != 0 ? -1 : status;
+}
+
+extern "C" {
+
 st_track_status_t st_TrackJob_track_until(st_TrackJob *j, st_buffer_size_t until_turn)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!j || !j->lat) return -1;
     clear_error();
-    cudaSetDevice(j->dev->id);
-    if (j->lat->cs.info.num_elements == 0) return j->n_total > 0 ? -1 : 0;
-    return run_track(j->dev, j->opt, *j->lat, j->d_cols, j->n_total, 0, j->n_total, MODE_UNTIL,
-                     (int64_t)until_turn, false, nullptr, 0, nullptr, j->dev->stream);
+    auto track = [&]() -> int32_t {
+        cudaSetDevice(j->dev->id);
+        if (j->lat->cs.info.num_elements == 0) return j->n_total > 0 ? -1 : 0;
+        return run_track(j->dev, j->opt, *j->lat, j->d_cols, j->n_total, 0, j->n_total,
+                         MODE_UNTIL, (int64_t)until_turn, false, nullptr, 0, nullptr,
+                         j->dev->stream);
+    };
+    if (j->debug_mode)
+        return debug_track(j, debug_input_flags(j, (int64_t)until_turn, false, 0, 0), track);
+    return track();
 }
 
 st_track_status_t st_TrackJob_track_elem_by_elem(st_TrackJob *j, st_buffer_size_t until_turn)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!j || !j->lat) return -1;
     clear_error();
+    if (j->debug_mode) {
+        uint64_t f = debug_input_flags(j, (int64_t)until_turn, false, 0, 0);
+        if (!j->has_ebe || j->outs.empty()) f |= kDbgNoElemByElemOutput;
+        if (f != 0) return debug_track(j, f, [] { return -1; });
+        j->debug_mode = false;  // validated: run the plain call, then record it
+        st_track_status_t const st = st_TrackJob_track_elem_by_elem(j, until_turn);
+        j->debug_mode = true;
+        return debug_track(j, 0, [st] { return st; });
+    }
     if (!j->has_ebe || j->outs.empty()) {
         set_error("TrackJob: no elem-by-elem output configured (until_turn_elem_by_elem)");
         return -1;
@@ -1206,8 +1354,17 @@ st_track_status_t st_TrackJob_track_elem_by_elem(st_TrackJob *j, st_buffer_size_
 st_track_status_t st_TrackJob_track_line(st_TrackJob *j, st_buffer_size_t b, st_buffer_size_t e,
                                          bool finish)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     if (!j || !j->lat) return -1;
     clear_error();
+    if (j->debug_mode) {
+        uint64_t const f = debug_input_flags(j, 0, true, b, e);
+        if (f != 0) return debug_track(j, f, [] { return -1; });
+        j->debug_mode = false;
+        st_track_status_t const st = st_TrackJob_track_line(j, b, e, finish);
+        j->debug_mode = true;
+        return debug_track(j, 0, [st] { return st; });
+    }
     uint64_t const ne = st_Buffer_get_num_of_objects(j->ebuf);
     if (b > e || e > ne) {
         set_error("TrackJob: line range outside the lattice");
@@ -1457,6 +1614,29 @@ void st_TrackJobNew_delete(st_TrackJobBaseNew *j) { delete j; }
 st_track_status_t st_TrackJobNew_track_until(st_TrackJobBaseNew *j, st_buffer_size_t u)
 {
     return st_TrackJob_track_until(j, u);
+}
+bool st_TrackJobNew_is_in_debug_mode(const st_TrackJobBaseNew *j) { return j && j->debug_mode; }
+int32_t st_TrackJobNew_enable_debug_mode(st_TrackJobBaseNew *j)
+{
+    if (!j) return -1;
+    j->debug_mode = true;
+    j->debug_reg = 0;
+    return 0;
+}
+int32_t st_TrackJobNew_disable_debug_mode(st_TrackJobBaseNew *j)
+{
+    if (!j) return -1;
+    j->debug_mode = false;
+    return 0;
+}
+int32_t st_TrackJobNew_collect_debug_flag(st_TrackJobBaseNew *j)
+{
+    // the register is written on the host by every call in debug mode
+    return (j && j->debug_mode) ? 0 : -1;
+}
+uint64_t st_TrackJobNew_get_debug_register(const st_TrackJobBaseNew *j)
+{
+    return j ? j->debug_reg : 0;
 }
 st_track_status_t st_TrackJobNew_track_elem_by_elem(st_TrackJobBaseNew *j, st_buffer_size_t u)
 {
@@ -2019,6 +2199,18 @@ uint64_t *device_scratch(int device, int64_t words)
         dev->scratch_words = words;
     }
     return dev->scratch;
+}
+
+bool shared_scratch_begin(int device, void *stream)
+{
+    Device *dev = get_device(device);
+    return dev && shared_use_begin(dev, static_cast<cudaStream_t>(stream));
+}
+
+void shared_scratch_end(int device, void *stream)
+{
+    Device *dev = get_device(device);
+    if (dev) shared_use_end(dev, static_cast<cudaStream_t>(stream));
 }
 
 void count_launches(uint64_t n) { g_launches.fetch_add(n); }

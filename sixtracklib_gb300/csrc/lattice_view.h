@@ -23,6 +23,11 @@ struct LatticeLaunchView {
 
 bool device_lattice_view(const st_DeviceLattice *lat, LatticeLaunchView *view);
 uint64_t *device_scratch(int device, int64_t words);
+// Order work on `stream` that uses device_scratch() after the previous work
+// that used it (any stream), and mark the end of this work: begin before the
+// first launch that touches the scratch, end after the last one.
+bool shared_scratch_begin(int device, void *stream);
+void shared_scratch_end(int device, void *stream);
 void count_launches(uint64_t n);
 
 }  // namespace stg

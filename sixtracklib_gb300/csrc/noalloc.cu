@@ -28,6 +28,7 @@
 #include <string>
 
 #include "common.h"
+#include "device_guard.h"
 #include "kernel_api.h"
 #include "lattice_view.h"
 
@@ -81,6 +82,7 @@ extern "C" st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLatti
                                                                    int64_t until_turn,
                                                                    void *stream)
 {
+    DeviceGuard guard;  // the caller's current device is restored on return
     clear_error();
     LatticeLaunchView v;
     if (!device_lattice_view(lat, &v)) {
@@ -96,7 +98,10 @@ extern "C" st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLatti
         set_error("st_DeviceLattice_track_until_noalloc: null particle columns");
         return -1;
     }
-    if (v.num_elements == 0) return -1;  // track/track.h:617: empty lattice fails
+    if (v.num_elements == 0) {  // track/track.h:617: an empty lattice fails
+        set_error("st_DeviceLattice_track_until_noalloc: empty lattice");
+        return -1;
+    }
     cudaError_t rc = cudaSetDevice(v.device);
     if (rc != cudaSuccess) {
         set_error(std::string("cudaSetDevice: ") + cudaGetErrorString(rc));
@@ -140,6 +145,7 @@ extern "C" st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLatti
     prm.idx = idx;
     prm.count = count;
     prm.s_table = v.s_table;
+    prm.op_mask = v.op_mask;
     int const rt = launch_track(prm, v.fast, v.threads, v.blocks_per_sm, stream);
     if (rt != 0) {
         set_error(std::string("track kernel launch: ") + cudaGetErrorString((cudaError_t)rt));
@@ -153,7 +159,9 @@ extern "C" st_track_status_t st_DeviceLattice_track_until_noalloc(st_DeviceLatti
         return -1;
     }
     if (host_flags[1] != 0) {
-        set_error("track kernel: shared-memory pipeline wait timed out; particles left unchanged");
+        set_error("track kernel: a shared-memory pipeline wait timed out; the blocks that timed "
+                  "out left their particles unchanged, other blocks (and earlier launches of "
+                  "the call) may have advanced theirs");
         return -1;
     }
     return host_flags[0];

@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "sixtracklib_gb300.h"
+#include "device_guard.h"
 
 namespace {
 
@@ -34,6 +35,7 @@ __global__ void fp64_fma_loop(double *out, int iters, double a, double b)
 
 extern "C" double st_engine_measure_fp64_peak(int device)
 {
+    stg::DeviceGuard guard;  // the caller's current device is restored on return
     if (cudaSetDevice(device) != cudaSuccess) return -1.0;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);

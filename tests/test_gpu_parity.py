@@ -334,6 +334,39 @@ def test_interpolated_space_charge(torch_cuda, oracle):
     del tables
 
 
+def test_interpolated_space_charge_large_tables(torch_cuda, oracle):
+    """Line-density tables of 10,000 points (cubic and linear) stay in global
+    memory outside the element records: the lattice keeps the default
+    1,024-word chunks and tracks like the oracle (1e-13 after one turn,
+    1e-10 after 20)."""
+    from sixtracklib_gb300.device import DeviceTracker
+    from sixtracklib_gb300.sc_line_density import LineDensityBuffer
+
+    tables = LineDensityBuffer()
+    z = np.linspace(-0.4, 0.4, 10_000)
+    prof = np.exp(-0.5 * (z / 0.1) ** 2) * (1 + 0.05 * np.sin(40 * z)) * 1e12
+    dz = float(z[1] - z[0])
+    idx = [tables.add(prof, z0=-0.4, dz=dz, method="cubic"),
+           tables.add(prof * 0.9, z0=-0.4, dz=dz, method="linear")]
+    e = lattices.fodo_ring()
+    for k in range(6):
+        e.SCInterpolatedProfile(number_of_particles=1e11, length=0.5, sigma_x=1e-3,
+                                sigma_y=1e-3 if k % 2 else 1.2e-3,
+                                interpol_data_addr=tables.address(idx[k % 2]),
+                                line_density_prof_fallback=5e11, min_sigma_diff=1e-10)
+    lat = e.cbuffer.to_image()
+    assert DeviceTracker(lat).num_chunks == 1  # records stay small: one 1,024-word chunk
+    p = lattices.gaussian_particles(2048, seed=29, sz=0.12)
+    for turns, tol in ((1, 1e-13), (20, 1e-10)):
+        exp = p.block.copy()
+        assert oracle.track_until(lat, exp, turns) == 0
+        for mode in ("exact", "fast"):
+            st, got = run_device(torch_cuda, lat, p.block, until=turns, mode=mode)
+            assert st == 0
+            assert_parity(got, exp, tol=tol)
+    del tables
+
+
 # ------------------------------------------------------------ edge cases
 def test_edge_cases(torch_cuda, oracle):
     e = Elements()
@@ -635,6 +668,80 @@ def test_trackjobnew_c_abi(torch_cuda, oracle):
     assert_parity(capi_columns(pb2), exp3, tol=1e-13)
     L.st_TrackJobNew_delete(job)
     for b in (pb, pb2, eb):
+        L.st_Buffer_delete(b)
+
+
+def test_trackjobnew_debug_mode_c_abi(torch_cuda, oracle):
+    """st_TrackJobNew_{is_in,enable,disable}_debug_mode and the debug
+    register (track/track_job_base.h:182-189, track/track_kernel_impl.h:
+    149-250): in debug mode a valid call tracks as in normal mode and leaves
+    the track status in the register's low bits; invalid line boundaries and
+    an elem-by-elem call without an output raise their flags and return -1
+    without tracking; out of debug mode the same calls fail as before."""
+    import ctypes as Cc
+
+    from sixtracklib_gb300 import ParticlesSet, _native
+    from tests import capi
+
+    L = _native.load()
+    vp, u64, cb = Cc.c_void_p, Cc.c_uint64, Cc.c_bool
+    sig = {"st_TrackJobNew_new": ([Cc.c_char_p, vp, vp, Cc.c_char_p], vp),
+           "st_TrackJobNew_is_in_debug_mode": ([vp], cb),
+           "st_TrackJobNew_enable_debug_mode": ([vp], Cc.c_int32),
+           "st_TrackJobNew_disable_debug_mode": ([vp], Cc.c_int32),
+           "st_TrackJobNew_collect_debug_flag": ([vp], Cc.c_int32),
+           "st_TrackJobNew_get_debug_register": ([vp], u64),
+           "st_TrackJobNew_track_until": ([vp, u64], Cc.c_int32),
+           "st_TrackJobNew_track_line": ([vp, u64, u64, cb], Cc.c_int32),
+           "st_TrackJobNew_track_elem_by_elem": ([vp, u64], Cc.c_int32),
+           "st_TrackJobNew_collect_particles": ([vp], Cc.c_int32),
+           "st_TrackJobNew_delete": ([vp], None)}
+    for name, (args, res) in sig.items():
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = res
+    e = lattices.fodo_ring()
+    n_elem = len(e)
+    ps = ParticlesSet()
+    p = ps.Particles(num_particles=200)
+    q = lattices.gaussian_particles(200, seed=17, sx=5e-3, sy=5e-3)
+    p.set_block(q.block)
+    pb = capi.c_buffer_from_image(ps.cbuffer.to_image())
+    eb = capi.c_buffer_from_image(e.cbuffer.to_image())
+    job = L.st_TrackJobNew_new(b"cuda", pb, eb, b"mode=exact")
+    assert job, _native.last_error()
+    assert not L.st_TrackJobNew_is_in_debug_mode(job)
+    assert L.st_TrackJobNew_collect_debug_flag(job) == -1
+    assert L.st_TrackJobNew_enable_debug_mode(job) == 0
+    assert L.st_TrackJobNew_is_in_debug_mode(job)
+    assert L.st_TrackJobNew_collect_debug_flag(job) == 0
+    # a valid call: tracks, the register holds status 0 and no flag
+    assert L.st_TrackJobNew_track_until(job, 20) == 0
+    assert L.st_TrackJobNew_get_debug_register(job) == 0
+    assert L.st_TrackJobNew_collect_particles(job) == 0
+    exp = q.block.copy()
+    oracle.track_until(e.cbuffer.to_image(), exp, 20)
+    assert_parity(capi_columns(pb), exp, tol=1e-13)
+    # invalid line boundaries: flag 2^39, -1, nothing tracked
+    before = capi_columns(pb).copy()
+    assert L.st_TrackJobNew_track_line(job, 5, n_elem + 3, False) == -1
+    reg = L.st_TrackJobNew_get_debug_register(job)
+    assert reg & (1 << 39) and (reg & 0xFFFFFFFF) == 0xFFFFFFFF
+    assert L.st_TrackJobNew_collect_particles(job) == 0
+    assert np.array_equal(capi_columns(pb), before)
+    # elem-by-elem without an output: the engine's flag 2^42
+    assert L.st_TrackJobNew_track_elem_by_elem(job, 21) == -1
+    assert L.st_TrackJobNew_get_debug_register(job) & (1 << 42)
+    # a valid line call afterwards clears the register
+    assert L.st_TrackJobNew_track_line(job, 0, 10, False) == 0
+    assert L.st_TrackJobNew_get_debug_register(job) == 0
+    # out of debug mode: the invalid line is refused as before
+    assert L.st_TrackJobNew_disable_debug_mode(job) == 0
+    assert not L.st_TrackJobNew_is_in_debug_mode(job)
+    assert L.st_TrackJobNew_track_line(job, 5, n_elem + 3, False) == -1
+    assert "line range" in _native.last_error()
+    assert L.st_TrackJobNew_enable_debug_mode(None) == -1
+    L.st_TrackJobNew_delete(job)
+    for b in (pb, eb):
         L.st_Buffer_delete(b)
 
 

@@ -55,6 +55,37 @@ def test_noalloc_matches_allocating_entry_point():
     assert 0 < lost < ref.shape[1]
 
 
+def test_noalloc_allocates_no_device_memory():
+    """After warm-up (the first call on the device and the allocating path),
+    a call with more particles than any earlier allocating call leaves the
+    device's free memory and torch's reserved memory unchanged: the
+    allocating entry point would have had to grow its selection scratch."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    from sixtracklib_gb300 import _native, lattices
+    from sixtracklib_gb300.device import DeviceTracker
+
+    lib, noalloc = _lib()
+    trk = DeviceTracker(lattices.fodo_ring().cbuffer, config="mode=fast")
+    stream = torch.cuda.current_stream().cuda_stream
+    small = torch.from_numpy(lattices.gaussian_particles(1000, seed=3).block.copy()
+                             .view(np.int64)).cuda()
+    assert trk.track_until(small.clone(), 1) == 0
+    assert noalloc(trk._ptr, small.data_ptr(), small.shape[1], 1, stream) == 0
+    big = torch.from_numpy(lattices.gaussian_particles(900_000, seed=4).block.copy()
+                           .view(np.int64)).cuda()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    assert noalloc(trk._ptr, big.data_ptr(), big.shape[1], 2, stream) == 0, _native.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_reserved() == reserved0
+    assert int((big[19] == 2).sum()) > 0  # the call did track
+
+
 def test_noalloc_rejects_oversized_calls():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
