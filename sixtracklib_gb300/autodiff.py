@@ -25,7 +25,9 @@ Conventions: delta is the independent longitudinal coordinate; rpp, rvv and
 psigma follow it as NS(Particles_update_delta_value) defines them
 (particles.h:5459-5496).  Lost particles keep the coordinates they had when
 they were lost (the reference's convention); their gradient flows back from
-there.  Apertures contribute no derivative.
+there.  Apertures contribute no derivative to the tracking itself; a loss
+that should see particle losses adds :func:`aperture_penalty`, a smooth
+function of the final (or loss-point) coordinates.
 """
 
 from __future__ import annotations
@@ -195,6 +197,81 @@ def apply_values(elements: Elements, params, values) -> Elements:
     for obj in objs:
         out.cbuffer.add_object(*obj._encode())
     return out
+
+
+def aperture_shapes(elements: Elements, x_limit: float = 1.0, y_limit: float = 1.0):
+    """The distinct apertures a particle of `elements` can be lost at, as
+    ``(kind, parameters)``: ``("rect", (cx, cy, hx, hy))`` for LimitRect
+    (be_limit/track.h:90-111) and for the global aperture after drifts
+    (be_limit/track.h:54-88, limits x_limit / y_limit), ``("ellipse",
+    (a_squ, b_squ))`` for LimitEllipse (be_limit/track.h:113-137); a
+    LimitRectEllipse (be_limit/track.h:139-162) contributes both shapes."""
+    shapes = {("rect", (0.0, 0.0, float(x_limit), float(y_limit)))}
+    for obj in elements.get_elements():
+        name = type(obj).__name__
+        if name == "LimitRect":
+            shapes.add(("rect", (0.5 * (obj.max_x + obj.min_x), 0.5 * (obj.max_y + obj.min_y),
+                                 0.5 * (obj.max_x - obj.min_x), 0.5 * (obj.max_y - obj.min_y))))
+        elif name == "LimitEllipse":
+            shapes.add(("ellipse", (float(obj.a_squ), float(obj.b_squ))))
+        elif name == "LimitRectEllipse":
+            shapes.add(("rect", (0.0, 0.0, float(obj.max_x), float(obj.max_y))))
+            shapes.add(("ellipse", (float(obj.a_squ), float(obj.b_squ))))
+    return sorted(shapes)
+
+
+def aperture_penalty(coords, shapes, width: float = 0.05, power: int = 16):
+    """Smooth lost-particle penalty, one value per particle.
+
+    The reference's loss is a step: a particle is lost where its state
+    becomes 0 at an aperture (be_limit/track.h:54-162; the loop freezes it
+    there, track/track.h:663-666), which has no derivative.  This penalty
+    replaces the step by a softplus of each particle's normalised aperture
+    coordinate rho (1 on the aperture boundary, 0 on the axis):
+
+        P = width * softplus((rho - 1) / width)
+
+    ~0 deep inside, width * log(2) on the boundary, rho - 1 beyond it.
+    rho combines the apertures with a p-norm (power 16), a smooth maximum:
+    rho_rect = (|(x - cx) / hx|^p + |(y - cy) / hy|^p)^(1/p) (the rectangle's
+    smooth stand-in), rho_ellipse = sqrt(x^2 / a^2 + y^2 / b^2),
+    rho = (sum of rho_k^p)^(1/p).  A lost particle keeps the coordinates
+    it had at its aperture (rho ~ 1), so the penalty's gradient reaches it
+    through the adjoint from the element where it was lost; a surviving
+    particle near an edge is pushed inwards.  Non-finite coordinates (a
+    particle lost at the global aperture with a NaN / inf coordinate) give
+    a constant penalty of `width * log(2)` and no gradient.  The
+    derivative is PyTorch's autograd of these expressions.
+
+    `coords` is 6 x n (x, px, y, py, zeta, delta); `shapes` from
+    :func:`aperture_shapes`."""
+    import torch
+
+    x, y = coords[0], coords[2]
+    ok = torch.isfinite(x) & torch.isfinite(y)
+    x = torch.where(ok, x, torch.zeros_like(x))
+    y = torch.where(ok, y, torch.zeros_like(y))
+    acc = torch.zeros_like(x)
+    for kind, prm in shapes:
+        if kind == "rect":
+            cx, cy, hx, hy = prm
+            r = (((x - cx) / hx) ** power + ((y - cy) / hy) ** power) ** (1.0 / power)
+        else:
+            a_squ, b_squ = prm
+            r = torch.sqrt(x * x / a_squ + y * y / b_squ)
+        acc = acc + r ** power
+    rho = acc ** (1.0 / power)
+    pen = width * torch.nn.functional.softplus((rho - 1.0) / width)
+    return torch.where(ok, pen, torch.full_like(pen, width * float(np.log(2.0))))
+
+
+def orbit_loss(out, state, shapes, penalty_weight: float = 1e-3, width: float = 0.05):
+    """The differentiable-tracking objective: mean over surviving particles
+    of x^2 + y^2 after the last turn, plus `penalty_weight` times the mean
+    over all particles of :func:`aperture_penalty`."""
+    alive = state == 1
+    core = ((out[0] ** 2 + out[2] ** 2) * alive).sum() / alive.sum().clamp(min=1)
+    return core + penalty_weight * aperture_penalty(out, shapes, width).mean()
 
 
 def coordinates(cols):

@@ -20,6 +20,13 @@ Two kinds of fixture:
 2. Outputs of the reference's own tracking code (oracle/_ref) on seeded
    synthetic inputs: ref_<case>.npz with the initial and final column blocks
    and, for small lattices, the lattice image.
+3. Outputs of the reference's own tracking code on the reference's shipped
+   machine descriptions (`lhc_no_bb`, `beambeam`): ref_shipped_<name>.npz
+   (`python tests/golden/make_golden.py --shipped` makes only these).
+4. Gradients of 1,000-turn differentiable tracking from the dual-number
+   oracle: adjoint_fodo_1000.npz (`--adjoint` makes only this one).
+5. The shipped lattices' 6D beam-beam elements: lab-frame parameters and
+   the stored payloads, bb6d_shipped.npz (`--bb6d`).
 """
 
 from __future__ import annotations
@@ -27,6 +34,7 @@ from __future__ import annotations
 import hashlib
 import os
 import sys
+from math import factorial
 
 import numpy as np
 
@@ -76,7 +84,160 @@ def misc_lattice() -> Elements:
     return e
 
 
+SHIPPED_SAMPLE = 1024
+SHIPPED_TURNS = (1, 1000)
+
+
+def shipped_lattices():
+    """The reference's shipped machine descriptions (tests/testdata):
+    `lhc_no_bb` (18,657 elements: Drift, Multipole, Cavity, XYShift,
+    SRotation) and `beambeam` (10,866: Drift, Multipole, Cavity, 72
+    BeamBeam4D, 2 pysixtrack-initialised BeamBeam6D).  Their particle dumps
+    are not shipped (the generator needs pysixtrack / sixtracktools), so a
+    seeded 1,024-proton sample at 6.5 TeV (the energy of both SixTrack inputs,
+    fort.3) is tracked 1 and 1,000 turns by the reference build and stored:
+    ref_shipped_<name>.npz holds the lattice image, the initial block and the
+    final block and status after each turn count."""
+    ref = Oracle.reference(omp=True)
+    if ref is None:
+        raise SystemExit("reference build not available (REF_ROOT)")
+    for seed, name in ((21, "lhc_no_bb"), (22, "beambeam")):
+        cb = CBuffer.fromfile(os.path.join(TD, name, "beam_elements.bin"))
+        img = cb.to_image()
+        p = lattices.gaussian_particles(SHIPPED_SAMPLE, seed=seed, sx=1e-4, spx=1e-6, sy=1e-4,
+                                        spy=1e-6, sz=0.02, sdelta=1e-4, p0c=6.5e12)
+        init = p.block.copy()
+        arrays = dict(lattice=img, initial=init, lattice_sha256=np.array(image_hash(img)))
+        for turns in SHIPPED_TURNS:
+            fin = init.copy()
+            st = ref.track_until(img, fin, turns)
+            arrays[f"final_{turns}"] = fin
+            arrays[f"status_{turns}"] = np.int64(st)
+            lost = int((fin[20].view(np.int64) == 0).sum())
+            print(f"ref_shipped_{name}: {turns} turns, status {st}, lost {lost}")
+        np.savez_compressed(os.path.join(HERE, f"ref_shipped_{name}.npz"), **arrays)
+
+
+ADJ_PARTICLES = 256
+ADJ_TURNS = 1000
+ADJ_EDGE = 8  # particles started near the LimitRect edge (lost within the run)
+SIGMA = np.array([1e-3, 1e-5, 1e-3, 1e-5, 0.05, 1e-4])
+
+
+def adjoint_beam():
+    """The 256-particle beam of the differentiable-tracking fixture: the
+    Gaussian beam of the learnable FODO ring with ADJ_EDGE particles started
+    at x in [0.013, 0.019] m, close to the +-0.02 m LimitRect."""
+    from sixtracklib_gb300.particles import COL
+
+    blk = lattices.gaussian_particles(ADJ_PARTICLES, seed=41).block.copy()
+    blk.view(np.float64)[COL["x"], :ADJ_EDGE] = np.linspace(0.013, 0.019, ADJ_EDGE)
+    return blk
+
+
+def adjoint_fixture():
+    """Gradients of 1,000-turn tracking on the learnable FODO ring (64 quad
+    strengths, 16 sextupoles; the differentiable-tracking workload) from the
+    dual-number oracle (oracle/dual.py, pinned to the C oracle and to finite
+    differences on the CPU), for two objectives: a random linear functional
+    of the final coordinates (every Jacobian entry) and the workload's
+    objective autodiff.orbit_loss (mean x^2 + y^2 of the survivors plus the
+    smooth aperture penalty).  The dual pass takes a few minutes, too long
+    for a GPU test, so its results are stored: adjoint_fodo_1000.npz."""
+    import torch
+
+    from oracle import dual
+    from sixtracklib_gb300.autodiff import aperture_shapes, orbit_loss
+
+    ring, params = lattices.learnable_fodo_ring()
+    blk = adjoint_beam()
+    kinds = [(int(p[0]), -1 if p[1] == "voltage" else 2 * int(p[2]) + (p[1] == "ksl"))
+             for p in params]
+    scale = np.array([1.0 if p[1] == "voltage" else 1.0 / factorial(int(p[2])) for p in params])
+    vals, ders, st, at, ae = dual.track_until(ring, blk.copy(), ADJ_TURNS, params=kinds)
+    w = np.random.default_rng(42).normal(size=(6, ADJ_PARTICLES)) / SIGMA[:, None]
+    out = torch.from_numpy(vals.copy()).requires_grad_(True)
+    loss = orbit_loss(out, torch.from_numpy(st.astype(np.int64)), aperture_shapes(ring))
+    loss.backward()
+    dl = out.grad.numpy()
+    arrays = dict(initial=blk, values=vals, state=st.astype(np.int64),
+                  at_turn=np.asarray(at, np.int64), at_element=np.asarray(ae, np.int64),
+                  weights=w, turns=np.int64(ADJ_TURNS),
+                  linear_grad_coords=np.einsum("rn,crn->cn", w, ders[:6]),
+                  linear_grad_params=np.einsum("rn,jrn->j", w, ders[6:]) * scale,
+                  loss=np.float64(loss.item()),
+                  loss_grad_coords=np.einsum("rn,crn->cn", dl, ders[:6]),
+                  loss_grad_params=np.einsum("rn,jrn->j", dl, ders[6:]) * scale)
+    np.savez_compressed(os.path.join(HERE, "adjoint_fodo_1000.npz"), **arrays)
+    print(f"adjoint_fodo_1000: lost {int((st == 0).sum())}/{ADJ_PARTICLES}, "
+          f"loss {loss.item():.6e}")
+
+
+BB6D_KEYS = ("q_part", "N_part_tot", "sigmaz", "N_slices", "min_sigma_diff",
+             "threshold_singular", "phi", "alpha", "Sig_11_0", "Sig_12_0", "Sig_13_0",
+             "Sig_14_0", "Sig_22_0", "Sig_23_0", "Sig_24_0", "Sig_33_0", "Sig_34_0",
+             "Sig_44_0", "delta_x", "delta_y", "x_CO", "px_CO", "y_CO", "py_CO", "sigma_CO",
+             "delta_CO", "Dx_sub", "Dpx_sub", "Dy_sub", "Dpy_sub", "Dsigma_sub", "Ddelta_sub",
+             "enabled")
+
+
+def bb6d_fixture():
+    """The 6D beam-beam elements of the reference's shipped `bbsimple` and
+    `beambeam` lattices, twice: the strong-beam parameters in the lab frame
+    as the pysixtrack line of the same test data holds them (line.pkl, read
+    as data: its objects are restored into plain stand-in classes, nothing
+    of pysixtrack is imported), and the payload words pysixtrack's
+    initialisation wrote into beam_elements.bin.  bb6d_shipped.npz:
+    `<lattice>_params` (one row per element, columns BB6D_KEYS) and
+    `<lattice>_payload_<k>`."""
+    import pickle
+
+    class _Stub:
+        def __setstate__(self, state):
+            if isinstance(state, tuple):
+                for part in state:
+                    if isinstance(part, dict):
+                        self.__dict__.update(part)
+            elif isinstance(state, dict):
+                self.__dict__.update(state)
+
+    class _Reader(pickle.Unpickler):
+        def find_class(self, module, name):
+            if module.startswith(("pysixtrack", "sixtracktools", "__main__")):
+                return type(name, (_Stub,), {})
+            return super().find_class(module, name)
+
+    arrays = {}
+    for name in ("bbsimple", "beambeam"):
+        with open(os.path.join(TD, name, "line.pkl"), "rb") as f:
+            line = _Reader(f).load()
+        rows = []
+        for item in line:
+            el = item[-1] if isinstance(item, tuple) else item
+            if type(el).__name__ == "BeamBeam6D":
+                rows.append([float(getattr(el, k)) for k in BB6D_KEYS])
+        stored = [np.asarray(o.data, dtype=np.float64)
+                  for o in Elements.fromfile(os.path.join(TD, name, "beam_elements.bin"))
+                  .get_elements() if type(o).__name__ == "BeamBeam6D"]
+        assert len(rows) == len(stored) > 0
+        arrays[f"{name}_params"] = np.array(rows)
+        for k, w in enumerate(stored):
+            arrays[f"{name}_payload_{k}"] = w
+        print(f"bb6d_shipped: {name}: {len(rows)} BeamBeam6D elements")
+    np.savez_compressed(os.path.join(HERE, "bb6d_shipped.npz"), keys=np.array(BB6D_KEYS),
+                        **arrays)
+
+
 def main():
+    if "--bb6d" in sys.argv:
+        bb6d_fixture()
+        return
+    if "--shipped" in sys.argv:
+        shipped_lattices()
+        return
+    if "--adjoint" in sys.argv:
+        adjoint_fixture()
+        return
     ref = Oracle.reference()
     if ref is None:
         raise SystemExit("reference build not available (REF_ROOT)")
@@ -156,6 +317,9 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **arrays)
         lost = int((fin[20].view(np.int64) == 0).sum())
         print(f"ref_{name}: status {st}, lost {lost}/{fin.shape[1]}")
+    shipped_lattices()
+    adjoint_fixture()
+    bb6d_fixture()
     print("fixtures written to", HERE)
 
 

@@ -15,6 +15,7 @@ difference quotient is dominated by the tracking's rounding noise):
 agreement within 1e-6 relative.
 """
 
+import os
 from math import factorial
 
 import numpy as np
@@ -29,6 +30,7 @@ from .adjoint_cases import misc_ring
 pytestmark = pytest.mark.gpu
 
 SIGMA = np.array([1e-3, 1e-5, 1e-3, 1e-5, 0.05, 1e-4])
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
 def _torch():
@@ -239,3 +241,160 @@ def test_lattice_without_adjoint_is_refused():
     lam = torch.ones((6, 64), dtype=torch.float64, device="cuda")
     with pytest.raises(RuntimeError, match="without an adjoint"):
         lat.adjoint_turns(cols, cols.clone(), lam, 0, 1)
+
+
+# ------------------------------------------- the workload at its full length
+def _fixture_1000():
+    return np.load(os.path.join(GOLDEN, "adjoint_fodo_1000.npz"))
+
+
+def _track_1000(lat, blk, reconstruct, turns=1000, every=100):
+    torch = _torch()
+    from sixtracklib_gb300.autodiff import coordinates
+
+    cols = torch.from_numpy(blk.view(np.int64).copy()).cuda()
+    coords = coordinates(cols).clone().requires_grad_(True)
+    values = torch.tensor(lat.initial_values, dtype=torch.float64, device="cuda",
+                          requires_grad=True)
+    out, state = lat.track(coords, values, cols, turns, checkpoint_every=every,
+                           reconstruct=reconstruct)
+    return coords, values, out, state
+
+
+@pytest.mark.parametrize("reconstruct", ["inverse", "recompute"])
+def test_adjoint_1000_turns_matches_dual_numbers(reconstruct):
+    """The differentiable-tracking workload at its full length: the learnable
+    FODO ring (64 quad strengths, 16 sextupoles), 1,000 turns, a checkpoint
+    every 100 turns, 256 particles of which 8 start near the LimitRect edge
+    and are lost during the run.  Gradients with respect to the initial
+    coordinates and the 80 strengths against the dual-number pass
+    (tests/golden/adjoint_fodo_1000.npz, made by make_golden.py --adjoint):
+    for a random linear functional of the final coordinates and for the
+    workload's objective (autodiff.orbit_loss: mean x^2 + y^2 of the
+    survivors plus the smooth aperture penalty), within 1e-9 of the largest
+    entry of each gradient row."""
+    torch = _torch()
+    from sixtracklib_gb300.autodiff import DifferentiableLattice, aperture_shapes, orbit_loss
+
+    d = _fixture_1000()
+    e, params = lattices.learnable_fodo_ring()
+    lat = DifferentiableLattice(e, params, "mode=exact")
+    shapes = aperture_shapes(e)
+    assert 0 < int((d["state"] == 0).sum()) < d["state"].size
+    for objective in ("linear", "loss"):
+        coords, values, out, state = _track_1000(lat, d["initial"], reconstruct)
+        st = state.cpu().numpy()
+        assert np.array_equal(st, d["state"])
+        vals = out.detach().cpu().numpy()
+        assert np.all(_rel_rows(vals, d["values"]) < 1e-11), _rel_rows(vals, d["values"])
+        if objective == "linear":
+            loss = (torch.from_numpy(d["weights"]).cuda() * out).sum()
+        else:
+            loss = orbit_loss(out, state, shapes)
+            assert abs(loss.item() - float(d["loss"])) <= 1e-11 * abs(float(d["loss"]))
+        loss.backward()
+        gc, gp = coords.grad.cpu().numpy(), values.grad.cpu().numpy()
+        gc_d, gp_d = d[objective + "_grad_coords"], d[objective + "_grad_params"]
+        rc = _rel_rows(gc, gc_d)
+        rp = np.max(np.abs(gp - gp_d)) / np.max(np.abs(gp_d))
+        print(f"{reconstruct} {objective}: coordinate rows {rc.max():.2e}, strengths {rp:.2e}")
+        assert np.all(rc < 1e-9), rc
+        assert rp < 1e-9, rp
+
+
+def _fd_check(lat, blk, loss_fn, checks, turns=1000, every=100):
+    """Central differences of GPU tracking for the parameters `checks`
+    ({index: relative step}) against the adjoint's gradient, within 1e-6
+    relative.  Every particle must be lost at the same turn and element in
+    the +h and -h runs (the difference quotient is then that of a smooth
+    function)."""
+    torch = _torch()
+    from sixtracklib_gb300.autodiff import coordinates
+
+    cols = torch.from_numpy(blk.view(np.int64).copy()).cuda()
+    coords = coordinates(cols).clone()
+    values = torch.tensor(lat.initial_values, dtype=torch.float64, device="cuda",
+                          requires_grad=True)
+    out, state = lat.track(coords, values, cols, turns, checkpoint_every=every)
+    loss_fn(out, state).backward()
+    g = values.grad.cpu().numpy()
+    v0 = lat.initial_values
+    worst = 0.0
+    with torch.no_grad():
+        for j, rel_h in checks.items():
+            h = rel_h * abs(v0[j])
+            runs, where = [], []
+            for s in (1.0, -1.0):
+                v = v0.copy()
+                v[j] += s * h
+                o, stt = lat.track(coords, torch.from_numpy(v).cuda(), cols, turns,
+                                   checkpoint_every=every)
+                runs.append((o, stt))
+                c = cols.clone()  # where each particle stopped (state, turn, element)
+                lat.set_values(v)
+                assert lat.tracker.track_until(c, turns) == 0
+                where.append(c[18:21].clone())
+            assert torch.equal(runs[0][1], state) and torch.equal(runs[1][1], state)
+            assert torch.equal(where[0], where[1]), "a loss moved between the +h and -h runs"
+            g_fd = loss_fn(runs[0][0], state, runs[1][0]) / (2 * h)
+            rel = abs(g[j] - g_fd) / abs(g_fd)
+            worst = max(worst, rel)
+            assert rel <= 1e-6, (j, g[j], g_fd)
+    return worst
+
+
+def _orbit_loss_difference(shapes, weight=1e-3):
+    """orbit_loss, and the difference of its values at two final states
+    taken before the reductions (so that the sums' rounding stays out of the
+    difference quotient)."""
+    from sixtracklib_gb300.autodiff import aperture_penalty, orbit_loss
+
+    def fn(out, state, other=None):
+        if other is None:
+            return orbit_loss(out, state, shapes, penalty_weight=weight)
+        alive = state == 1
+        core = ((out[0] - other[0]) * (out[0] + other[0]) +
+                (out[2] - other[2]) * (out[2] + other[2])) * alive
+        pen = aperture_penalty(out, shapes) - aperture_penalty(other, shapes)
+        return float(core.sum() / alive.sum() + weight * pen.mean())
+    return fn
+
+
+def test_adjoint_1000_turns_vs_finite_differences():
+    """The workload's objective (mean x^2 + y^2 of the survivors plus the
+    smooth aperture penalty) over 1,000 turns with a checkpoint every 100:
+    the adjoint's derivatives with respect to four quad strengths (central
+    differences with h = 1e-7 relative) and two sextupole strengths
+    (h = 1e-3 relative: their effect on the coordinates is ~1e6 times weaker,
+    and at 1e-7 the quotient is the tracking's rounding noise) within 1e-6
+    relative."""
+    from sixtracklib_gb300.autodiff import DifferentiableLattice, aperture_shapes
+
+    d = _fixture_1000()
+    e, params = lattices.learnable_fodo_ring()
+    lat = DifferentiableLattice(e, params, "mode=exact")
+    worst = _fd_check(lat, d["initial"], _orbit_loss_difference(aperture_shapes(e)),
+                      {0: 1e-7, 17: 1e-7, 41: 1e-7, 63: 1e-7, 64: 1e-3, 79: 1e-3})
+    print(f"orbit loss, 1000 turns: adjoint vs central differences {worst:.2e}")
+
+
+def test_aperture_penalty_adjoint_vs_finite_differences():
+    """The smooth lost-particle penalty alone (its derivative reaches the lost
+    particles through the adjoint from the element where each was lost):
+    central differences of the mean penalty over 1,000 turns against the
+    adjoint, within 1e-6 relative, for four quad strengths."""
+    from sixtracklib_gb300.autodiff import (DifferentiableLattice, aperture_penalty,
+                                            aperture_shapes)
+
+    d = _fixture_1000()
+    e, params = lattices.learnable_fodo_ring()
+    lat = DifferentiableLattice(e, params, "mode=exact")
+    shapes = aperture_shapes(e)
+
+    def fn(out, state, other=None):
+        if other is None:
+            return aperture_penalty(out, shapes).mean()
+        return float((aperture_penalty(out, shapes) - aperture_penalty(other, shapes)).mean())
+
+    worst = _fd_check(lat, d["initial"], fn, {3: 1e-7, 22: 1e-7, 40: 1e-7, 61: 1e-7})
+    print(f"aperture penalty, 1000 turns: adjoint vs central differences {worst:.2e}")
