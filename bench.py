@@ -18,15 +18,18 @@ particle passes counts once (lost particles stop counting where they are lost).
   batched     256 lattice variants (rings built like the synthetic ring, element
               count ~ U(500, 20000), particle count ~ log-uniform(1024, 262144),
               Gaussian 6D): one captured CUDA graph of the persistent batch
-              kernel (autotuned launch shape) against one plain tracking launch
-              per variant, both over the same 2 turns after 2 warm-up turns;
+              kernel (autotuned launch shape; turns per launch up to 8
+              compete) against one plain tracking launch per variant, both
+              over the same 20 turns (--batched-turns) after one warm-up turn;
               results compared bit for bit.
   adjoint     the differentiable-tracking workload: the FODO ring with 64
               quadrupole and 16 sextupole strengths as parameters, 65,536
               Gaussian protons, 1,000 turns, a checkpoint every 100 turns;
               loss = mean over surviving particles of x^2 + y^2 plus a
-              penalty on the lost fraction; forward and backward timed with
-              CUDA events; ratio = backward / plain tracking of the same turns.
+              smooth lost-particle penalty (autodiff.orbit_loss: softplus of
+              each particle's normalised aperture coordinate); forward and
+              backward timed with CUDA events; ratio = backward / plain
+              tracking of the same turns.
   beam_beam_space_charge
               the beam-beam and space-charge mix: the FODO ring plus 4
               BeamBeam6D (21 slices), 4 BeamBeam4D and 200 q-Gaussian
@@ -78,6 +81,15 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-bbsc", action="store_true")
     ap.add_argument("--batch-variants", type=int, default=256)
+    ap.add_argument("--batched-turns", type=int, default=20)
+    ap.add_argument("--batched-detail", action="store_true",
+                    help="also time one plain launch per variant on its own")
+    ap.add_argument("--batched-no-tune", action="store_true",
+                    help="keep the batch's default launch shape (no autotuning)")
+    ap.add_argument("--bbsc-particles", type=int, default=262144)
+    ap.add_argument("--bbsc-turns", type=int, default=5)
+    ap.add_argument("--adjoint-particles", type=int, default=65536)
+    ap.add_argument("--adjoint-turns", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
 
@@ -172,6 +184,32 @@ def pet_between(before, after, n_elem):
     return int(pet.sum().item())
 
 
+def host_cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo: `model name`, or on Arm the
+    implementer / part numbers when no name is given), with the core count."""
+    name, impl, part = "", "", ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key, _, val = line.partition(":")
+                key, val = key.strip().lower(), val.strip()
+                if key == "model name" and not name:
+                    name = val
+                elif key == "cpu implementer" and not impl:
+                    impl = val
+                elif key == "cpu part" and not part:
+                    part = val
+    except OSError:
+        pass
+    if not name and impl:
+        # 0x41 = Arm Ltd; part 0xd4f = Neoverse V2 (the Grace CPU core)
+        known = {("0x41", "0xd4f"): "Arm Neoverse V2 (NVIDIA Grace)"}
+        name = known.get((impl, part), f"Arm implementer {impl} part {part}")
+    import platform
+
+    return f"{name or platform.processor() or platform.machine()}, {os.cpu_count()} cores"
+
+
 def cpu_baseline(ring, parts, seconds, threads=None):
     """Time the oracle (OpenMP over particles) on a sample of the workload."""
     from oracle.pyoracle import Oracle
@@ -198,6 +236,7 @@ def cpu_baseline(ring, parts, seconds, threads=None):
     pet = int((alive0 * t1 * n_elem).sum() + ((alive0 & (st1 == 0)) * (e1 + 1)).sum())
     cores = orc.set_num_threads(0)
     out = {"value": pet / dt, "unit": METRIC, "cores": cores, "kind": "port",
+           "cpu": host_cpu_model(),
            "sample": f"{n} particles (strided) x {turns} turns of the same ring, "
                      f"{pet:.3e} PET in {dt:.2f} s; oracle/oracle.c, OpenMP over particles"}
     # one host thread on the first 1,024 particles of the sample, as many
@@ -303,7 +342,41 @@ def build_variants(n_variants):
     return specs, images
 
 
-def batched_measure(dev, mode, specs, images, turns=2):
+def per_variant_plain(dev, trk, cols, n_elem, threads=128):
+    """One plain one-turn launch per variant, each timed alone with CUDA
+    events: its particles, grid, time and PET/s, against which the batched
+    kernel's gain is read (a variant whose grid cannot fill the GPU runs at a
+    fraction of the full-GPU rate)."""
+    import torch
+
+    props = torch.cuda.get_device_properties(dev)
+    stream = torch.cuda.current_stream(dev)
+    rows = []
+    for t, c, ne in zip(trk, cols, n_elem):
+        work = c.clone()
+        t.launch_until(work, 1)  # warm-up turn
+        before = work.clone()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        t.launch_until(work, 2)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        sec = a.elapsed_time(b) / 1e3
+        live = int((before[20] == 1).sum())
+        blocks = (live + threads - 1) // threads
+        rows.append({"particles": int(c.shape[1]), "elements": int(ne), "blocks": blocks,
+                     "sm_fill": min(1.0, blocks / props.multi_processor_count),
+                     "ms": sec * 1e3, "value": pet_between(before, work, ne) / sec})
+    return rows
+
+
+def batched_measure(dev, mode, specs, images, turns=20, trial_turns=8, detail=False,
+                    tune=True):
+    """The batched workload over `turns` turns (after one warm-up turn): one
+    tracking call per variant (plain) against one captured graph of the
+    persistent batch kernel, with the launch shape autotuned first (turns
+    per launch up to `trial_turns` compete)."""
     import torch
 
     from sixtracklib_gb300 import lattices
@@ -325,13 +398,13 @@ def batched_measure(dev, mode, specs, images, turns=2):
     # plain: one tracking launch per variant, one variant after the other
     plain = [c.clone() for c in cols]
     for t, c in zip(trk, plain):
-        t.launch_until(c, turns)
+        t.launch_until(c, 1)  # warm-up turn
     torch.cuda.synchronize(dev)
     before = [c.clone() for c in plain]
     a, b = ev(), ev()
     a.record(stream)
     for t, c in zip(trk, plain):
-        t.launch_until(c, 2 * turns)
+        t.launch_until(c, 1 + turns)
     b.record(stream)
     torch.cuda.synchronize(dev)
     t_plain = a.elapsed_time(b) / 1e3
@@ -341,14 +414,12 @@ def batched_measure(dev, mode, specs, images, turns=2):
     bt = BatchTracker(trk)
     bt.set_particles(work)
     t0 = time.time()
-    tune_ms = bt.autotune(sample_fraction=1 / 64, trial_turns=2)
+    tune_ms = bt.autotune(sample_fraction=1 / 64, trial_turns=trial_turns) if tune else None
     tune_s = time.time() - t0
+    assert bt.track_until(0, 1) == 0, "batch status"  # warm-up turn, as the plain arm's
     bt.capture(turns)
-    bt.set_turn(0)
-    bt.replay()  # warm-up replay: turns 0..turns
-    assert bt.status() == 0, "batch status"
     before = [c.clone() for c in work]
-    bt.set_turn(turns)
+    bt.set_turn(1)
     torch.cuda.synchronize(dev)
     a, b = ev(), ev()
     a.record(stream)
@@ -367,8 +438,10 @@ def batched_measure(dev, mode, specs, images, turns=2):
         "plain_per_lattice": {"seconds": t_plain, "value": pet_plain / t_plain,
                               "launches": "one tracking call per variant"},
         "batched_graph": {"seconds": t_batch, "value": pet_batch / t_batch,
-                          "shape": bt.shape, "autotune_s": tune_s, "autotune_trial_ms": tune_ms},
+                          "shape": bt.shape, "autotune_s": tune_s, "autotune_trial_ms": tune_ms,
+                          "autotune_trial_turns": trial_turns},
         "unit": METRIC, "speedup": t_plain / t_batch, "bit_identical": bool(identical),
+        **({"per_variant_plain": per_variant_plain(dev, trk, cols, n_elem)} if detail else {}),
     }
 
 
@@ -377,10 +450,12 @@ def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
     import torch
 
     from sixtracklib_gb300 import lattices
-    from sixtracklib_gb300.autodiff import DifferentiableLattice, coordinates
+    from sixtracklib_gb300.autodiff import (DifferentiableLattice, aperture_shapes, coordinates,
+                                            orbit_loss)
 
     ring, params = lattices.learnable_fodo_ring()
     lat = DifferentiableLattice(ring, params, f"mode={mode}")
+    shapes = aperture_shapes(ring)
     cols = torch.from_numpy(lattices.gaussian_particles(n, seed=1).block.copy()
                             .view(np.int64)).to(dev)
     stream = torch.cuda.current_stream(dev)
@@ -390,6 +465,8 @@ def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
 
     out = {"workload": f"learnable FODO ring ({len(ring)} elements, {len(params)} strengths), "
                        f"{n} particles, {turns} turns, checkpoint every {every}",
+           "loss": "mean x^2 + y^2 of the surviving particles + 1e-3 x mean smooth aperture "
+                   "penalty (softplus of the normalised aperture coordinate, width 0.05)",
            "mode": mode, "particles": n, "turns": turns, "checkpoint_every": every,
            "parameters": len(params)}
     for rep in range(2):  # warm-up, then timed
@@ -411,9 +488,7 @@ def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
             a.record(stream)
             fin, state = lat.track(coords, values, cols, turns, checkpoint_every=every,
                                    reconstruct=rec)
-            alive = state == 1
-            loss = (((fin[0] ** 2 + fin[2] ** 2) * alive).sum() / alive.sum().clamp(min=1)
-                    + 1e-3 * (~alive).sum() / n)
+            loss = orbit_loss(fin, state, shapes)
             b.record(stream)
             loss.backward()
             c2.record(stream)
@@ -427,13 +502,69 @@ def adjoint_measure(dev, mode, n=65536, turns=1000, every=100):
     return out
 
 
-def bbsc_bench(args, n=262144, turns=5):
-    """The beam-beam and space-charge mix (see module doc): GPU figures per
-    strong-beam shape, and the oracle on a sample of the same particles."""
-    from sixtracklib_gb300 import lattices
-    from sixtracklib_gb300.run_case import bbsc_measure
+def bbsc_measure(n: int, turns: int, modes=("fast", "exact")) -> list:
+    """Particle-element-turns/s of the beam-beam and space-charge mix
+    (lattices.bb_sc_ring) with round and with elliptic strong beams: `turns`
+    turns timed with CUDA events after 2 warm-up turns."""
+    import torch
 
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.device import DeviceTracker
+
+    out = []
+    stream = torch.cuda.current_stream()
+    for elliptic in (False, True):
+        ring = lattices.bb_sc_ring(elliptic=elliptic)
+        block = lattices.gaussian_particles(n, seed=3).block
+        for mode in modes:
+            trk = DeviceTracker(ring, config=f"mode={mode}")
+            cols = torch.from_numpy(block.copy().view(np.int64)).cuda()
+            if trk.track_until(cols, 2) != 0:
+                raise SystemExit("bbsc: tracking failed")
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            trk.launch_until(cols, 2 + turns)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if trk.last_status() != 0:
+                raise SystemExit("bbsc: tracking failed")
+            sec = a.elapsed_time(b) / 1e3
+            alive = int((cols[20] == 1).sum())
+            out.append({"beams": "elliptic (sigma_y = 1.3 sigma_x)" if elliptic else "round",
+                        "mode": mode, "particles": n, "alive": alive,
+                        "elements": len(ring), "turns_timed": turns,
+                        "ms_per_turn": sec / turns * 1e3,
+                        "value": alive * len(ring) * turns / sec})
+    return out
+
+
+def bbsc_bench(args, peak):
+    """The beam-beam and space-charge mix (see module doc): GPU figures per
+    strong-beam shape with their FP64 roofline, and the oracle on a sample of
+    the same particles."""
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.roofline import lattice_flops_per_pet
+
+    n, turns = args.bbsc_particles, args.bbsc_turns
     gpu = bbsc_measure(n, turns, modes=(args.mode,))
+    # algorithmic FP64 operations per particle-element-turn of each mix; the
+    # Faddeeva function's cost depends on where a particle sits relative to
+    # the strong beam: averaged over the beam's positions at the start of
+    # the turn (the kicks sit together at the end of the ring, where the
+    # particles are where they start)
+    sample = lattices.gaussian_particles(n, seed=3)
+    xs, ys = sample.x[::max(1, n // 16384)], sample.y[::max(1, n // 16384)]
+    for g in gpu:
+        ring = lattices.bb_sc_ring(elliptic=g["beams"] != "round")
+        f = lattice_flops_per_pet(ring, xs, ys)
+        achieved = g["value"] * f / 1e12
+        g["roofline"] = {"bound": "fp64", "flops_per_pet": f, "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak and peak > 0 else None,
+                         "flops": "sixtracklib_gb300/roofline.py element_flops (reference "
+                                  "formulas, libm calls counted as 1)"}
     out = {"workload": f"FODO ring + 4 BeamBeam6D (21 slices) + 4 BeamBeam4D + 200 "
                        f"SCQGaussProfile, {n} Gaussian protons, FP64 {args.mode}, "
                        f"{turns} turns after 2 warm-up turns",
@@ -511,10 +642,12 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample_particles": n, "lattice_elements": n_elem},
         "cpu_baseline": {"value": val, "unit": METRIC, "cores": cores, "kind": "port",
+                         "cpu": host_cpu_model(),
                          "sample": f"{n} of the {args.particles} particles (strided), one turn "
                                    "per step; the CPU restatement of the reference loop "
-                                   "(oracle/oracle.c) -- the reference's own build is "
-                                   "x86-only here"},
+                                   "(oracle/oracle.c, pinned bit for bit to the reference's "
+                                   "own build) -- the reference's sources, from which its "
+                                   "build is made, are not on the GPU host"},
         "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -632,17 +765,21 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(ring, parts, args.cpu_seconds)
     if variants is not None:
         try:
-            line["batched"] = batched_measure(dev, args.mode, *variants)
+            line["batched"] = batched_measure(dev, args.mode, *variants,
+                                              turns=args.batched_turns,
+                                              detail=args.batched_detail,
+                                              tune=not args.batched_no_tune)
         except Exception as exc:  # report, do not hide
             line["batched"] = {"error": str(exc)}
     if not args.no_adjoint:
         try:
-            line["adjoint"] = adjoint_measure(dev, args.mode)
+            line["adjoint"] = adjoint_measure(dev, args.mode, n=args.adjoint_particles,
+                                              turns=args.adjoint_turns)
         except Exception as exc:  # report, do not hide
             line["adjoint"] = {"error": str(exc)}
     if not args.no_bbsc:
         try:
-            line["beam_beam_space_charge"] = bbsc_bench(args)
+            line["beam_beam_space_charge"] = bbsc_bench(args, peak)
         except Exception as exc:  # report, do not hide
             line["beam_beam_space_charge"] = {"error": str(exc)}
     if not args.no_e2e:
