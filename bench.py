@@ -61,8 +61,8 @@ WORKLOAD = "synthetic 20k-element ring, 1M particles polar grid, FP64, 1 turn pe
 # DRAM bytes (read + write) of one tracking launch of the default workload
 # (1M particles, fast, 128 threads, 2 CTAs/SM), measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass; two launches after
-# the warm-up: 120.6 and 118.6 MB; profiles/track_kernel_synthetic_ring_20k.md)
-TRACK_TRAFFIC_BYTES = 1.196e8
+# the warm-up: 113.0 and 111.6 MB; profiles/track_kernel_synthetic_ring_20k.md)
+TRACK_TRAFFIC_BYTES = 1.123e8
 
 
 def parse():
