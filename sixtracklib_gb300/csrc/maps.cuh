@@ -21,6 +21,9 @@ namespace stg {
 struct PState {
     double x, px, y, py, zeta, delta, psigma, rpp, rvv, chi, s;
     double beta0, q0, p0c, mass0, charge_ratio, gamma0, energy0;
+    // 1 / (pc0 beta), pc0 = p0c e, beta = beta0 rvv: the space-charge kicks'
+    // particle factor under the fast policy, refreshed whenever rvv changes
+    double inv_pc0_beta;
     int64_t pid, at_element, at_turn, state;
     bool lazy_s;    // s is +0 at this turn's start: s is read from the lattice's s table
 };
@@ -33,6 +36,11 @@ constexpr double kEps0D = 8.854187817620e-12;
 constexpr double kSqrtPiD = 1.7724538509055160272981674833411451827975494561224;
 constexpr double kQelemD = 1.60217662e-19;
 constexpr double kCharge0SiD = 1.602176634e-19;
+
+__device__ __forceinline__ void refresh_inv_pc0_beta(PState &p)
+{
+    p.inv_pc0_beta = 1.0 / ((p.p0c * kCharge0SiD) * (p.beta0 * p.rvv));
+}
 
 // ------------------------------------------------------------------ energy
 // NS(Particles_add_to_energy_value): particles.h:5255-5297
@@ -51,6 +59,7 @@ __device__ __forceinline__ void add_energy(PState &p, double de)
     p.zeta *= rvv / p.rvv;
     p.rvv = rvv;
     p.rpp = 1.0 / opd;
+    refresh_inv_pc0_beta(p);
 }
 
 // NS(Particles_update_delta_value): particles.h:5459-5496
@@ -64,6 +73,7 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
     p.rvv = opd / (1.0 + ptau_beta0);
     p.rpp = 1.0 / opd;
     p.psigma = ptau_beta0 / (beta0 * beta0);
+    refresh_inv_pc0_beta(p);
 }
 
 // ------------------------------------------------------------------- maps
@@ -615,15 +625,22 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
     double py = p.py - W(d[24]);
     double sg = p.zeta - W(d[25]);
     double dl = p.delta - W(d[26]);
+    // FAST: one reciprocal each for cos(phi), pz and the inverse boost's
+    // determinant and one for the slices' charge factor, multiplications
+    // in place of the reference's repeated divisions by them
+    double const icphi = FAST ? 1. / cphi : 0.;
     {  // boost
         double const h = dl + 1. - sqrt((1. + dl) * (1. + dl) - px * px - py * py);
-        double const px_st = px / cphi - h * calpha * tphi / cphi;
-        double const py_st = py / cphi - h * salpha * tphi / cphi;
+        double const px_st = FAST ? px * icphi - h * calpha * tphi * icphi
+                                  : px / cphi - h * calpha * tphi / cphi;
+        double const py_st = FAST ? py * icphi - h * salpha * tphi * icphi
+                                  : py / cphi - h * salpha * tphi / cphi;
         double const dl_st = dl - px * calpha * tphi - py * salpha * tphi + h * tphi * tphi;
         double const pz_st = sqrt((1. + dl_st) * (1. + dl_st) - px_st * px_st - py_st * py_st);
-        double const hx = px_st / pz_st;
-        double const hy = py_st / pz_st;
-        double const hs = 1. - (dl_st + 1) / pz_st;
+        double const ipz = FAST ? 1. / pz_st : 0.;
+        double const hx = FAST ? px_st * ipz : px_st / pz_st;
+        double const hy = FAST ? py_st * ipz : py_st / pz_st;
+        double const hs = FAST ? 1. - (dl_st + 1) * ipz : 1. - (dl_st + 1) / pz_st;
         double const L11 = 1. + hx * calpha * sphi;
         double const L12 = hx * salpha * sphi;
         double const L13 = calpha * tphi;
@@ -632,7 +649,7 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
         double const L23 = salpha * tphi;
         double const L31 = hs * calpha * sphi;
         double const L32 = hs * salpha * sphi;
-        double const L33 = 1. / cphi;
+        double const L33 = FAST ? icphi : 1. / cphi;
         double const nx = L11 * x + L12 * y + L13 * sg;
         double const ny = L21 * x + L22 * y + L23 * sg;
         double const ns = L31 * x + L32 * y + L33 * sg;
@@ -645,8 +662,9 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
     }
     double const thr = W(d[17]);
     double const msd = W(d[16]);
+    double const kq = FAST ? W(d[0]) * q0 * (1. / (P0 * kClightD)) : 0.;
     for (int i = 0; i < n_slices; ++i) {
-        double const Ksl = W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
+        double const Ksl = FAST ? W(np_[i]) * kq : W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
         double const S = 0.5 * (sg - W(ss_[i]));
         double const xb = x + px * S - W(xs_[i]);
         double const yb = y + py * S - W(ys_[i]);
@@ -691,21 +709,26 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
     }
     {  // inverse boost
         double const pz = sqrt((1. + dl) * (1. + dl) - px * px - py * py);
-        double const hx = px / pz;
-        double const hy = py / pz;
-        double const hs = 1. - (dl + 1) / pz;
-        double const Det = 1. / cphi + (hx * calpha + hy * salpha - hs * sphi) * tphi;
-        double const Li11 = (1. / cphi + salpha * tphi * (hy - hs * salpha * sphi)) / Det;
-        double const Li12 = (salpha * tphi * (hs * calpha * sphi - hx)) / Det;
+        double const ipz = FAST ? 1. / pz : 0.;
+        double const hx = FAST ? px * ipz : px / pz;
+        double const hy = FAST ? py * ipz : py / pz;
+        double const hs = FAST ? 1. - (dl + 1) * ipz : 1. - (dl + 1) / pz;
+        double const c1 = FAST ? icphi : 1. / cphi;
+        double const Det = c1 + (hx * calpha + hy * salpha - hs * sphi) * tphi;
+        // Li = N / Det: FAST multiplies by one reciprocal of Det
+        double const iD = FAST ? 1. / Det : 0.;
+        auto over_det = [&](double num) { return FAST ? num * iD : num / Det; };
+        double const Li11 = over_det(c1 + salpha * tphi * (hy - hs * salpha * sphi));
+        double const Li12 = over_det(salpha * tphi * (hs * calpha * sphi - hx));
         double const Li13 =
-            -tphi * (calpha - hx * salpha * salpha * sphi + hy * calpha * salpha * sphi) / Det;
-        double const Li21 = (calpha * tphi * (-hy + hs * salpha * sphi)) / Det;
-        double const Li22 = (1. / cphi + calpha * tphi * (hx - hs * calpha * sphi)) / Det;
+            over_det(-tphi * (calpha - hx * salpha * salpha * sphi + hy * calpha * salpha * sphi));
+        double const Li21 = over_det(calpha * tphi * (-hy + hs * salpha * sphi));
+        double const Li22 = over_det(c1 + calpha * tphi * (hx - hs * calpha * sphi));
         double const Li23 =
-            -tphi * (salpha - hy * calpha * calpha * sphi + hx * calpha * salpha * sphi) / Det;
-        double const Li31 = -hs * calpha * sphi / Det;
-        double const Li32 = -hs * salpha * sphi / Det;
-        double const Li33 = (1. + hx * calpha * sphi + hy * salpha * sphi) / Det;
+            over_det(-tphi * (salpha - hy * calpha * calpha * sphi + hx * calpha * salpha * sphi));
+        double const Li31 = over_det(-hs * calpha * sphi);
+        double const Li32 = over_det(-hs * salpha * sphi);
+        double const Li33 = over_det(1. + hx * calpha * sphi + hy * salpha * sphi);
         double const xi = Li11 * x + Li12 * y + Li13 * sg;
         double const yi = Li21 * x + Li22 * y + Li23 * sg;
         double const si = Li31 * x + Li32 * y + Li33 * sg;
@@ -758,8 +781,7 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
     double const beta0 = p.beta0;
     double const beta = beta0 * p.rvv;
     double const pc0 = p.p0c * kCharge0SiD;
-    double inv_pc0_beta = 0.0;
-    if (FAST) inv_pc0_beta = 1.0 / (pc0 * beta);
+    double const inv_pc0_beta = FAST ? p.inv_pc0_beta : 0.0;  // 1 / (pc0 beta)
     double const z = FAST ? p.zeta * (inv_pc0_beta * (pc0 * beta0)) : p.zeta / p.rvv;
     double fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
     fk *= W(c[0]);
