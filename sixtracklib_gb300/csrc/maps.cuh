@@ -21,9 +21,10 @@ namespace stg {
 struct PState {
     double x, px, y, py, zeta, delta, psigma, rpp, rvv, chi, s;
     double beta0, q0, p0c, mass0, charge_ratio, gamma0, energy0;
-    // 1 / (pc0 beta), pc0 = p0c e, beta = beta0 rvv: the space-charge kicks'
-    // particle factor under the fast policy, refreshed whenever rvv changes
-    double inv_pc0_beta;
+    // the q-Gaussian space-charge kick's particle factors under the fast
+    // policy, refreshed whenever rvv changes: chi charge_ratio (e q0)^2
+    // (1 - beta0 beta) / (pc0 beta) and 1 / rvv (pc0 = p0c e, beta = beta0 rvv)
+    double sc_k, inv_rvv;
     int64_t pid, at_element, at_turn, state;
     bool lazy_s;    // s is +0 at this turn's start: s is read from the lattice's s table
 };
@@ -37,9 +38,14 @@ constexpr double kSqrtPiD = 1.7724538509055160272981674833411451827975494561224;
 constexpr double kQelemD = 1.60217662e-19;
 constexpr double kCharge0SiD = 1.602176634e-19;
 
-__device__ __forceinline__ void refresh_inv_pc0_beta(PState &p)
+__device__ __forceinline__ void refresh_kick_factors(PState &p)
 {
-    p.inv_pc0_beta = 1.0 / ((p.p0c * kCharge0SiD) * (p.beta0 * p.rvv));
+    double const pc0 = p.p0c * kCharge0SiD;
+    double const beta = p.beta0 * p.rvv;
+    double const inv_pc0_beta = 1.0 / (pc0 * beta);
+    double const charge = kCharge0SiD * p.q0;
+    p.sc_k = p.chi * p.charge_ratio * charge * charge * (1.0 - p.beta0 * beta) * inv_pc0_beta;
+    p.inv_rvv = inv_pc0_beta * (pc0 * p.beta0);
 }
 
 // ------------------------------------------------------------------ energy
@@ -59,7 +65,7 @@ __device__ __forceinline__ void add_energy(PState &p, double de)
     p.zeta *= rvv / p.rvv;
     p.rvv = rvv;
     p.rpp = 1.0 / opd;
-    refresh_inv_pc0_beta(p);
+    refresh_kick_factors(p);
 }
 
 // NS(Particles_update_delta_value): particles.h:5459-5496
@@ -73,7 +79,7 @@ __device__ __forceinline__ void set_delta(PState &p, double nd)
     p.rvv = opd / (1.0 + ptau_beta0);
     p.rpp = 1.0 / opd;
     p.psigma = ptau_beta0 / (beta0 * beta0);
-    refresh_inv_pc0_beta(p);
+    refresh_kick_factors(p);
 }
 
 // ------------------------------------------------------------------- maps
@@ -781,10 +787,15 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
     double const beta0 = p.beta0;
     double const beta = beta0 * p.rvv;
     double const pc0 = p.p0c * kCharge0SiD;
-    double const inv_pc0_beta = FAST ? p.inv_pc0_beta : 0.0;  // 1 / (pc0 beta)
-    double const z = FAST ? p.zeta * (inv_pc0_beta * (pc0 * beta0)) : p.zeta / p.rvv;
-    double fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
-    fk *= W(c[0]);
+    // FAST: the particle's factors kept since its last energy change
+    double const z = FAST ? p.zeta * p.inv_rvv : p.zeta / p.rvv;
+    double fk;
+    if (FAST) {
+        fk = p.sc_k * (W(c[4]) * W(c[0]));
+    } else {
+        fk = p.chi * p.charge_ratio * W(c[4]) * charge * charge * (1.0 - beta0 * beta);
+        fk *= W(c[0]);
+    }
     // c[11..14]: sqrt_beta = 1 / (sqrt(2) bunchlength_rms), sqrt_beta^2,
     // sqrt_beta / cq, 1 / (1 - q), computed by the lattice compiler
     double const q = W(c[8]);
@@ -802,7 +813,6 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
     fk *= W(c[13]) * e;
     double ex, ey, gx, gy;
     if (FAST) {
-        fk *= inv_pc0_beta;
         if (aux & SC_ROUND) {
             double const x = p.x - W(c[5]), y = p.y - W(c[6]);
             double const r2 = x * x + y * y;

@@ -107,7 +107,7 @@ __device__ __forceinline__ void load_particle(PState &p, const uint64_t *cols, i
     p.at_turn = k[19 * n + i];
     p.state = k[20 * n + i];
     p.energy0 = sqrt(p.p0c * p.p0c + p.mass0 * p.mass0);
-    refresh_inv_pc0_beta(p);
+    refresh_kick_factors(p);
     p.lazy_s = false;
 }
 
