@@ -27,6 +27,8 @@ Two kinds of fixture:
    oracle: adjoint_fodo_1000.npz (`--adjoint` makes only this one).
 5. The shipped lattices' 6D beam-beam elements: lab-frame parameters and
    the stored payloads, bb6d_shipped.npz (`--bb6d`).
+6. The shipped pysixtrack lines of `bbsimple` and `beambeam` as gzipped
+   JSON, line_<name>.json.gz (`--lines`).
 """
 
 from __future__ import annotations
@@ -228,7 +230,46 @@ def bb6d_fixture():
                         **arrays)
 
 
+def lines_fixture():
+    """The pysixtrack lines of the shipped `bbsimple` and `beambeam` test data
+    (line.pkl, read as data into stand-in classes, nothing of pysixtrack
+    imported): per element its class name and attributes, as gzipped JSON
+    (line_<name>.json.gz).  The shipped beam_elements.bin were written from
+    these lines by the reference's Elements.fromline."""
+    import gzip
+    import json
+    import pickle
+
+    class _Stub:
+        def __setstate__(self, state):
+            for part in (state if isinstance(state, tuple) else (state,)):
+                if isinstance(part, dict):
+                    self.__dict__.update(part)
+
+    class _Reader(pickle.Unpickler):
+        def find_class(self, module, name):
+            if module.startswith(("pysixtrack", "sixtracktools", "__main__")):
+                return type(name, (_Stub,), {})
+            return super().find_class(module, name)
+
+    for name in ("bbsimple", "beambeam"):
+        with open(os.path.join(TD, name, "line.pkl"), "rb") as f:
+            line = _Reader(f).load()
+        out = []
+        for item in line:
+            el = item[-1] if isinstance(item, tuple) else item
+            attrs = {k: (v.tolist() if hasattr(v, "tolist") else v)
+                     for k, v in el.__dict__.items() if not k.startswith("_")}
+            out.append([type(el).__name__, attrs])
+        with gzip.open(os.path.join(HERE, f"line_{name}.json.gz"), "wt") as f:
+            json.dump(out, f)
+        print(f"line_{name}: {len(out)} elements")
+
+
 def main():
+    if "--lines" in sys.argv:
+        lines_fixture()
+        return
     if "--bb6d" in sys.argv:
         bb6d_fixture()
         return
@@ -320,6 +361,7 @@ def main():
     shipped_lattices()
     adjoint_fixture()
     bb6d_fixture()
+    lines_fixture()
     print("fixtures written to", HERE)
 
 

@@ -237,3 +237,95 @@ def test_truncated_objects_stay_undecoded():
     e.cbuffer.add_object(TYPE_TRICUB, np.zeros(3, np.uint64))
     assert isinstance(e.get(1), CObject)
     assert parameter_table(e, [])["begin"].size == 3
+
+
+# ------------------------------------------- the reference's shipped lines
+class _LineElement:
+    """A pysixtrack element as the shipped line holds it: its class name and
+    attributes, with to_dict(keepextra=True)."""
+
+    def __init__(self, cls_name, attrs):
+        self.__class__ = type(cls_name, (_LineElement,), {})
+        self._attrs = attrs
+
+    def to_dict(self, keepextra=False):
+        return dict(self._attrs)
+
+
+BB4D_KEYS = ("q_part", "N_part", "sigma_x", "sigma_y", "beta_s", "min_sigma_diff", "Delta_x",
+             "Delta_y", "Dpx_sub", "Dpy_sub", "enabled")
+
+
+@pytest.mark.parametrize("name,image", [("bbsimple", "bbsimple.npz"),
+                                        ("beambeam", "ref_shipped_beambeam.npz")])
+def test_shipped_line_converts_to_the_shipped_lattice(name, image):
+    """The pysixtrack lines of the reference's `bbsimple` and `beambeam` test
+    data (tests/golden/line_<name>.json.gz) converted here reproduce the
+    lattices the reference wrote from them (beam_elements.bin, via
+    Elements.fromline, python/sixtracklib/beam_elements.py:748-757): same
+    element types in the same order, Drift / Multipole / Cavity words
+    identical, the beam-beam payloads within 4e-16.  The line predates the
+    named beam-beam parameters: its BeamBeam4D lists the payload in order
+    (BB4D_data, be_beamfields.h:36-56), its BeamBeam6D the lab-frame strong
+    beam that beam_elements.bb6d_data and gaussian_equal_charge_slices set
+    up."""
+    import gzip
+    import json
+    import os
+
+    from sixtracklib_gb300 import CBuffer
+    from sixtracklib_gb300.beam_elements import gaussian_equal_charge_slices
+
+    golden = os.path.join(os.path.dirname(__file__), "golden")
+    with gzip.open(os.path.join(golden, f"line_{name}.json.gz"), "rt") as f:
+        items = json.load(f)
+    beam_beam = []
+    e = Elements()
+    for cls_name, attrs in items:
+        if cls_name in ("Drift", "Multipole", "Cavity"):
+            e.append_line(SimpleNamespace(elements=[_LineElement(cls_name, attrs)]))
+        elif cls_name == "BeamBeam4D":
+            e.BeamBeam4D(data=[float(attrs[k]) for k in BB4D_KEYS])
+            beam_beam.append(len(e) - 1)
+        else:
+            assert cls_name == "BeamBeam6D"
+            charge, z = gaussian_equal_charge_slices(attrs["N_part_tot"], attrs["sigmaz"],
+                                                     int(attrs["N_slices"]))
+            sig = [attrs[f"Sig_{ij}_0"] for ij in ("11", "12", "13", "14", "22", "23", "24",
+                                                   "33", "34", "44")]
+            e.BeamBeam6D(data=bb6d_data(
+                q_part=attrs["q_part"], phi=attrs["phi"], alpha=attrs["alpha"],
+                delta_x=attrs["delta_x"], delta_y=attrs["delta_y"], n_part_per_slice=charge,
+                z_slices=z, sigmas=sig,
+                co=[attrs[k] for k in ("x_CO", "px_CO", "y_CO", "py_CO", "sigma_CO",
+                                       "delta_CO")],
+                min_sigma_diff=attrs["min_sigma_diff"],
+                threshold_singular=attrs["threshold_singular"],
+                d_sub=[attrs[k] for k in ("Dx_sub", "Dpx_sub", "Dy_sub", "Dpy_sub", "Dsigma_sub",
+                                          "Ddelta_sub")],
+                enabled=float(attrs["enabled"])))
+            beam_beam.append(len(e) - 1)
+    ref = Elements(cbuffer=CBuffer.from_image(np.load(os.path.join(golden, image))["lattice"]))
+    mine, theirs = e.cbuffer.objects, ref.cbuffer.objects
+    assert len(mine) == len(theirs) == len(items)
+    for k, (a, b) in enumerate(zip(mine, theirs)):
+        assert a.typeid == b.typeid, k
+        if k in beam_beam:
+            da = np.asarray(e.get(k).data, dtype=np.float64)
+            db = np.asarray(ref.get(k).data, dtype=np.float64)
+            assert da.shape == db.shape, k
+            wa, wb = da.view(np.uint64), db.view(np.uint64)
+            if a.typeid == 9:  # BeamBeam6D: slice count and relative offsets are integers
+                assert wa[18] == wb[18] and np.array_equal(wa[34:38], wb[34:38])
+                real = np.r_[0:18, 19:33, 38:da.size]
+                assert (da[33] > 0) == (db[33] > 0)  # `enabled`: integer 1 there, 1.0 here
+            else:
+                real = np.r_[0:10]
+                assert (da[10] > 0) == (db[10] > 0)
+            dev = np.abs(da[real] - db[real])
+            assert np.all((dev == 0) | (dev <= 4e-16 * np.abs(db[real]))), k
+        else:  # every field of the element, arrays (the multipole's bal) included
+            ea, eb = e.get(k), ref.get(k)
+            for field, _ in type(ea)._fields:
+                assert np.array_equal(np.asarray(getattr(ea, field)),
+                                      np.asarray(getattr(eb, field))), (k, field)
