@@ -322,6 +322,11 @@ int64_t st_ElemByElemConfig_get_stored_num_particles(const st_ElemByElemConfig *
  *   mode=exact|fast  threads_per_block=N  track_threads_per_block=N
  *   device=N  aperture=always|never|conditional  aperture_min_length=L
  *   x_limit=X  y_limit=Y
+ *   track_beambeam4d=  track_beambeam6d=  track_spacecharge=  track_tricub=
+ *     enabled|skip|disabled (the reference's SIXTRL_TRACK_* build flags,
+ *     track/track.h:421-575: a disabled map fails and the particle is lost,
+ *     a skipped one does nothing; defaults enabled, enabled, enabled,
+ *     disabled as the reference's default build)
  * and the reference's TOML forms ("[cuda]\n track_threads_per_block = N",
  * "cuda.threads_per_block = N").  Block sizes are multiples of 32 up to
  * 1024, as in the reference; the tracking kernel (track_threads_per_block,

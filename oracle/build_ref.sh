@@ -7,7 +7,9 @@
 # configuration headers with CMake; this script writes its own versions with
 # the reference's default feature values (BB4D/BB6D/SC enabled, TriCub
 # disabled, global aperture |x|,|y| < 1 m after every drift) into
-# oracle/_ref/include instead of running the reference's build system.
+# oracle/_ref/include instead of running the reference's build system, and
+# builds the same driver twice more with other map feature flags
+# (oracle/_ref/libstref_flags_{a,b}.so).
 # Flags follow the reference CPU build: -O2 -fno-fast-math, plus
 # -ffp-contract=off so no FMA contraction happens on any host.
 set -euo pipefail
@@ -20,16 +22,20 @@ if [ ! -f "$REF_ROOT/sixtracklib/common/track/track.h" ]; then
 fi
 GEN="$OUT/include/sixtracklib/common/generated"
 mkdir -p "$GEN"
-cat > "$GEN/config.h" <<'EOF'
+# config.h with the map feature flags BB4D, BB6D, SC, TRICUB (2 enabled,
+# 1 skip, 0 disabled) into the include tree $1
+write_config() {
+mkdir -p "$1/sixtracklib/common/generated"
+cat > "$1/sixtracklib/common/generated/config.h" <<EOF
 #ifndef STG_REF_GENERATED_CONFIG_H
 #define STG_REF_GENERATED_CONFIG_H
 #define SIXTRL_TRACK_MAP_ENABLED 2
 #define SIXTRL_TRACK_MAP_SKIP 1
 #define SIXTRL_TRACK_MAP_DISABLED 0
-#define SIXTRL_TRACK_BEAMBEAM4D 2
-#define SIXTRL_TRACK_BEAMBEAM6D 2
-#define SIXTRL_TRACK_SPACECHARGE 2
-#define SIXTRL_TRACK_TRICUB 0
+#define SIXTRL_TRACK_BEAMBEAM4D $2
+#define SIXTRL_TRACK_BEAMBEAM6D $3
+#define SIXTRL_TRACK_SPACECHARGE $4
+#define SIXTRL_TRACK_TRICUB $5
 #define SIXTRL_GLOBAL_APERTURE_CHECK_ALWAYS 2
 #define SIXTRL_GLOBAL_APERTURE_CHECK_CONDITIONAL 1
 #define SIXTRL_GLOBAL_APERTURE_CHECK_NEVER 0
@@ -39,6 +45,8 @@ cat > "$GEN/config.h" <<'EOF'
 #define SIXTRL_APERTURE_Y_LIMIT 1.0
 #endif
 EOF
+}
+write_config "$OUT/include" 2 2 2 0
 cat > "$GEN/namespace.h" <<'EOF'
 #ifndef STG_REF_GENERATED_NAMESPACE_H
 #define STG_REF_GENERATED_NAMESPACE_H
@@ -66,4 +74,15 @@ gcc $CFLAGS -shared -I "$OUT/include" -I "$REF_ROOT" -I "$HERE" \
 # particle, parallel over particles), used for CPU timing here.
 gcc $CFLAGS -fopenmp -shared -I "$OUT/include" -I "$REF_ROOT" -I "$HERE" \
     "$HERE/ref_driver.c" -DSTG_REF_OMP -o "$OUT/libstref_omp.so" -lm
+# Two builds with other feature flags, for the flag semantics and the
+# TriCub map: (a) BB4D skip, BB6D disabled, SC skip, TriCub enabled;
+# (b) BB4D disabled, BB6D skip, SC disabled, TriCub skip.
+for v in "a 1 0 1 2" "b 0 1 0 1"; do
+    set -- $v
+    INC="$OUT/include_$1"
+    write_config "$INC" "$2" "$3" "$4" "$5"
+    cp "$GEN/namespace.h" "$GEN/modules.h" "$INC/sixtracklib/common/generated/"
+    gcc $CFLAGS -shared -I "$INC" -I "$REF_ROOT" -I "$HERE" \
+        "$HERE/ref_driver.c" -o "$OUT/libstref_flags_$1.so" -lm
+done
 echo "built $OUT/libstref.so"

@@ -68,6 +68,16 @@ void orc_set_aperture_mode(int mode, double min_length, double x_limit,
     g_ap_ylim = y_limit;
 }
 
+static int g_flag_bb4d = 2, g_flag_bb6d = 2, g_flag_sc = 2, g_flag_tricub = 0;
+
+void orc_set_track_flags(int bb4d, int bb6d, int sc, int tricub)
+{
+    g_flag_bb4d = bb4d;
+    g_flag_bb6d = bb6d;
+    g_flag_sc = sc;
+    g_flag_tricub = tricub;
+}
+
 /* ------------------------------------------------------- particle record */
 typedef struct {
     double q0, mass0, beta0, gamma0, p0c, s, x, y, px, py, zeta, psigma,
@@ -1061,6 +1071,132 @@ static int m_sc_interpol(const lattice_t *L, prec *p, const uint64_t *w)
     return ST_OK;
 }
 
+/* ------------------------------------------------------------ TriCub */
+/* NS(tricub_construct_coefs) (be_tricub/coefficients.h): the coefficients
+ * c[i + 4 j + 16 k] of x^i y^j z^k are the inverse tricubic Hermite
+ * constraint matrix times the corner values b[8 l + corner] (l: f, f_x, f_y,
+ * f_z, f_xy, f_xz, f_yz, f_xyz; corner bit 0 / 1 / 2: upper node in x / y /
+ * z).  That matrix is the Kronecker product of the 1-D cubic Hermite inverse
+ * H (columns f(0), f(1), f'(0), f'(1)) in x, y and z; the reference's
+ * generated code sums, per coefficient, entry * value over the nonzero
+ * entries in ascending value order, the first one assigned, which is what
+ * this loop does. */
+static const int o_hermite[4][4] = {
+    {1, 0, 0, 0}, {0, 0, 1, 0}, {-3, 3, -2, -1}, {2, -2, 1, 1}};
+static const int o_tc_order[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+                                     {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+
+void orc_tricub_coefs(const double *b, double *coefs)
+{
+    for (int r = 0; r < 64; ++r) {
+        int const i = r & 3, j = (r >> 2) & 3, k = r >> 4;
+        int first = 1;
+        double acc = 0.0;
+        for (int v = 0; v < 64; ++v) {
+            int const l = v >> 3, c = v & 7;
+            int const a = o_hermite[i][2 * o_tc_order[l][0] + (c & 1)] *
+                          o_hermite[j][2 * o_tc_order[l][1] + ((c >> 1) & 1)] *
+                          o_hermite[k][2 * o_tc_order[l][2] + (c >> 2)];
+            if (a == 0) continue;
+            double const t = (double)a * b[v];
+            acc = first ? t : acc + t;
+            first = 0;
+        }
+        coefs[r] = acc;
+    }
+}
+
+/* be_tricub/track.h:51-262; NS(TriCub) {x_shift, y_shift, tau_shift,
+ * dipolar_kick_px, dipolar_kick_py, dipolar_kick_ptau, length, data_addr}
+ * and NS(TriCubData) {x0, dx, nx, y0, dy, ny, z0, dz, nz, mirror_x,
+ * mirror_y, mirror_z, table_addr} (be_tricub.h:33-52, 309-319).  data_addr
+ * is a plain address: inside this image or a host address.  The reference
+ * reads outside its table for a particle outside the grid (a debug
+ * assertion only); here the particle is lost and the map fails, as on the
+ * GPU.  data_addr 0 (the reference dereferences null) fails likewise. */
+static int m_tricub(const lattice_t *L, prec *p, const uint64_t *w)
+{
+    const double *e = (const double *)w;
+    uint64_t const addr = w[7];
+    uint64_t const size = ((const uint64_t *)L->img)[1];
+    const uint64_t *d;
+    const double *table;
+    if (addr == 0) return ST_FAIL;
+    if (addr >= L->base && addr + 13u * 8u <= L->base + size) {
+        d = (const uint64_t *)lat_at(L, addr);
+        table = (const double *)lat_at(L, d[12]);
+    } else {
+        d = (const uint64_t *)(uintptr_t)addr;
+        table = (const double *)(uintptr_t)d[12];
+    }
+    double const dx = w2d(d[1]), dy = w2d(d[4]), dz = w2d(d[7]);
+    int64_t const nx = (int64_t)d[2], ny = (int64_t)d[5], nz = (int64_t)d[8];
+    double const inv_dx = 1. / dx, inv_dy = 1. / dy, inv_dz = 1. / dz;
+    double const z = p->zeta / (p->beta0 * p->rvv);
+    double const fx = ((p->x - e[0]) - w2d(d[0])) * inv_dx;
+    double const fy = ((p->y - e[1]) - w2d(d[3])) * inv_dy;
+    double const fz = ((z - e[2]) - w2d(d[6])) * inv_dz;
+    double const sign_x = ((int64_t)d[9] == 1 && fx < 0.0) ? -1. : 1.;
+    double const sign_y = ((int64_t)d[10] == 1 && fy < 0.0) ? -1. : 1.;
+    double const sign_z = ((int64_t)d[11] == 1 && fz < 0.0) ? -1. : 1.;
+    double const sfx = sign_x * fx, sfy = sign_y * fy, sfz = sign_z * fz;
+    double const ixf = floor(sfx), iyf = floor(sfy), izf = floor(sfz);
+    if (!(ixf >= 0.0 && ixf <= (double)(nx - 2) && iyf >= 0.0 && iyf <= (double)(ny - 2) &&
+          izf >= 0.0 && izf <= (double)(nz - 2))) {
+        p->state = 0;
+        return ST_FAIL;
+    }
+    int64_t const ix = (int64_t)ixf, iy = (int64_t)iyf, iz = (int64_t)izf;
+    double const xn = sfx - ixf, yn = sfy - iyf, zn = sfz - izf;
+    double b[64], c[64];
+    for (int l = 0; l < 8; ++l)
+        for (int corner = 0; corner < 8; ++corner) {
+            int64_t const node = (ix + (corner & 1)) +
+                                 nx * ((iy + ((corner >> 1) & 1)) + ny * (iz + (corner >> 2)));
+            b[8 * l + corner] = table[l + 8 * node];
+        }
+    orc_tricub_coefs(b, c);
+    double xp[4], yp[4], zp[4];
+    xp[0] = yp[0] = zp[0] = 1.;
+    xp[1] = xn;
+    yp[1] = yn;
+    zp[1] = zn;
+    xp[2] = xn * xn;
+    yp[2] = yn * yn;
+    zp[2] = zn * zn;
+    xp[3] = xp[2] * xn;
+    yp[3] = yp[2] * yn;
+    zp[3] = zp[2] * zn;
+    double kpx = 0., kpy = 0., kpt = 0.;
+    for (int i = 1; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            for (int k = 0; k < 4; ++k)
+                kpx += i * (((c[i + 4 * j + 16 * k] * xp[i - 1]) * yp[j]) * zp[k]);
+    kpx *= (e[6] * inv_dx);
+    kpx *= -sign_x;
+    kpx -= e[3];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 1; j < 4; ++j)
+            for (int k = 0; k < 4; ++k)
+                kpy += j * (((c[i + 4 * j + 16 * k] * xp[i]) * yp[j - 1]) * zp[k]);
+    kpy *= (e[6] * inv_dy);
+    kpy *= -sign_y;
+    kpy -= e[4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            for (int k = 1; k < 4; ++k)
+                kpt += k * (((c[i + 4 * j + 16 * k] * xp[i]) * yp[j]) * zp[k - 1]);
+    kpt *= (e[6] * inv_dz);
+    kpt *= -sign_z;
+    kpt -= e[5];
+    double const q = p->q0 * p->charge_ratio;
+    double const energy_kick = q * (p->p0c * kpt);
+    p->px += kpx;
+    p->py += kpy;
+    p_add_energy(p, energy_kick);
+    return ST_OK;
+}
+
 /* ---------------------------------------------------------- monitors */
 typedef struct {
     const orc_monitor_outputs *mon;
@@ -1166,26 +1302,40 @@ static int dispatch(const lattice_t *L, prec *p, int64_t obj,
     case T_DIPEDGE:
         ret = m_dipedge(p, obj_reals(L, obj));
         break;
-    case T_TRICUB:      /* disabled map: failure, particle left as is */
+    /* feature flags, track.h:421-575: a disabled map fails (the loop marks
+     * the particle lost), a skipped one succeeds */
+    case T_TRICUB:
+        ret = g_flag_tricub == 2 ? m_tricub(L, p, obj_words(L, obj))
+                                 : (g_flag_tricub == 1 ? ST_OK : ST_FAIL);
+        break;
     case T_TRICUB_DATA:
-        ret = ST_FAIL;
+        ret = g_flag_tricub != 0 ? ST_OK : ST_FAIL;
         break;
     case T_BB4D:
-        ret = m_bb4d(L, p, obj_words(L, obj));
+        ret = g_flag_bb4d == 2 ? m_bb4d(L, p, obj_words(L, obj))
+                               : (g_flag_bb4d == 1 ? ST_OK : ST_FAIL);
         break;
     case T_BB6D:
-        ret = m_bb6d(L, p, obj_words(L, obj));
+        ret = g_flag_bb6d == 2 ? m_bb6d(L, p, obj_words(L, obj))
+                               : (g_flag_bb6d == 1 ? ST_OK : ST_FAIL);
         break;
     case T_SC_COASTING:
-        ret = m_sc_coasting(p, obj_reals(L, obj));
+        ret = g_flag_sc == 2 ? m_sc_coasting(p, obj_reals(L, obj))
+                             : (g_flag_sc == 1 ? ST_OK : ST_FAIL);
         break;
     case T_SC_QGAUSS:
-        ret = m_sc_qgauss(p, obj_reals(L, obj));
+        ret = g_flag_sc == 2 ? m_sc_qgauss(p, obj_reals(L, obj))
+                             : (g_flag_sc == 1 ? ST_OK : ST_FAIL);
         break;
+    /* with space charge skipped or disabled the interpolated profile has no
+     * case label (the preprocessor branch that starts in the q-Gaussian
+     * case, track.h:537-575, encloses it): the default branch below */
     case T_SC_INTERPOL:
+        if (g_flag_sc != 2) goto unknown;
         ret = m_sc_interpol(L, p, obj_words(L, obj));
         break;
     default:
+    unknown:
         p->state = 0;
         ret = ST_FAIL;
     }

@@ -58,6 +58,15 @@ int orc_set_num_threads(int n);
 void orc_set_aperture_mode(int mode, double min_length, double x_limit,
                            double y_limit);
 
+/* Feature flags of the maps, as SIXTRL_TRACK_BEAMBEAM4D / _BEAMBEAM6D /
+ * _SPACECHARGE / _TRICUB: 2 enabled, 1 skip, 0 disabled (defaults 2, 2, 2,
+ * 0 as the reference's default build). */
+void orc_set_track_flags(int bb4d, int bb6d, int sc, int tricub);
+
+/* The 64 tricubic coefficients of one cell from its 64 corner values
+ * (NS(tricub_construct_coefs), be_tricub/coefficients.h). */
+void orc_tricub_coefs(const double *b, double *coefs);
+
 int32_t orc_track_until(const uint8_t *lattice, void *cols, int64_t n,
                         int64_t idx_begin, int64_t idx_end, int64_t until_turn,
                         const orc_monitor_outputs *mon);

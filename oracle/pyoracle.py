@@ -25,6 +25,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libstref.so")
 REF_OMP_LIB = os.path.join(HERE, "_ref", "libstref_omp.so")
+# reference builds with other map feature flags (oracle/build_ref.sh):
+# name -> (path, (bb4d, bb6d, spacecharge, tricub)), 2 enabled, 1 skip, 0 disabled
+REF_FLAG_LIBS = {
+    "a": (os.path.join(HERE, "_ref", "libstref_flags_a.so"), (1, 0, 1, 2)),
+    "b": (os.path.join(HERE, "_ref", "libstref_flags_b.so"), (0, 1, 0, 1)),
+}
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=gnu99", "-fno-fast-math",
           "-ffp-contract=off", "-fopenmp"]
@@ -121,8 +127,10 @@ class Oracle:
                                                        C.c_double, C.c_double]
 
     @classmethod
-    def reference(cls, omp: bool = False):
-        path = REF_OMP_LIB if omp else REF_LIB
+    def reference(cls, omp: bool = False, flags: str | None = None):
+        """The reference build; `flags` names one with other map feature
+        flags (REF_FLAG_LIBS)."""
+        path = REF_FLAG_LIBS[flags][0] if flags else (REF_OMP_LIB if omp else REF_LIB)
         if not os.path.exists(path):
             if build_reference() is None:
                 return None
@@ -148,6 +156,23 @@ class Oracle:
     def set_aperture_mode(self, mode=2, min_length=0.0, x_limit=1.0, y_limit=1.0):
         self.lib.orc_set_aperture_mode(int(mode), float(min_length), float(x_limit),
                                        float(y_limit))
+
+    def set_track_flags(self, bb4d=2, bb6d=2, spacecharge=2, tricub=0):
+        """Map feature flags (2 enabled, 1 skip, 0 disabled); the defaults
+        are the reference's default build."""
+        fn = self.lib.orc_set_track_flags
+        fn.argtypes = [C.c_int] * 4
+        fn(int(bb4d), int(bb6d), int(spacecharge), int(tricub))
+
+    def tricub_coefs(self, b):
+        """The 64 tricubic coefficients (x^i y^j z^k at i + 4 j + 16 k) of
+        one cell's 64 corner values."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        out = np.empty(64)
+        fn = getattr(self.lib, self.prefix + "tricub_coefs")
+        fn.argtypes = [C.c_void_p, C.c_void_p]
+        fn(b.ctypes.data, out.ctypes.data)
+        return out
 
     def track_until(self, lattice, block, until_turn, i0=0, i1=None, monitors=None):
         lat = _u8(lattice)

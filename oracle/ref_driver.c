@@ -70,6 +70,13 @@ static int open_lattice(ref_lattice *L, const uint8_t *img,
      * this image, move it with the image, as the caller would */
     uint64_t const new_base = (uint64_t)(uintptr_t)L->mem;
     for (NS(Object) const *it = L->begin; it != L->end; ++it) {
+        if (NS(Object_get_type_id)(it) == NS(OBJECT_TYPE_TRICUB)) {
+            /* TriCub's data_addr likewise */
+            NS(TriCub) *tc = (NS(TriCub) *)(uintptr_t)NS(Object_get_begin_addr)(it);
+            if (tc->data_addr >= old_base && tc->data_addr < old_base + size)
+                tc->data_addr = tc->data_addr - old_base + new_base;
+            continue;
+        }
         if (NS(Object_get_type_id)(it) != NS(OBJECT_TYPE_SC_INTERPOLATED_PROF)) continue;
         NS(SCInterpolatedProfile) *sc =
             (NS(SCInterpolatedProfile) *)(uintptr_t)NS(Object_get_begin_addr)(it);
@@ -249,4 +256,11 @@ void ref_bb6d_boost(const double *boost, double *c6, int inverse)
         NS(BeamBeam6D_inv_boost)(&b, &c6[0], &c6[1], &c6[2], &c6[3], &c6[4], &c6[5]);
     else
         NS(BeamBeam6D_boost)(&b, &c6[0], &c6[1], &c6[2], &c6[3], &c6[4], &c6[5]);
+}
+
+/* NS(tricub_construct_coefs) (be_tricub/coefficients.h) on one cell's 64
+ * corner values. */
+void ref_tricub_coefs(const double *b, double *coefs)
+{
+    NS(tricub_construct_coefs)(b, coefs);
 }

@@ -11,12 +11,13 @@ from .buffer import AssignAddressItem, Buffer, get_cbuffer_from_obj  # noqa: F40
 from .trackjob import CudaTrackJob, TrackJob  # noqa: F401
 from .sc_line_density import LineDensityProfileData_create_buffer_assignment  # noqa: F401
 from .tricub import TriCub_buffer_create_assign_address_item  # noqa: F401
+from . import config  # noqa: F401
 
 
 def supports(architecture):
     """Whether the engine tracks on `architecture` (config_helper.py:7-8):
     CUDA only."""
-    return str(architecture).strip().lower() == "cuda"
+    return bool(config.SIXTRACKLIB_MODULES.get(str(architecture).strip().lower(), False))
 
 
 __version__ = "0.1.0"

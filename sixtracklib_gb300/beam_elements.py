@@ -702,12 +702,31 @@ SpaceChargeCoasting = SCCoasting
 SpaceChargeQGaussianProfile = SCQGaussProfile
 SpaceChargeBunched = SCQGaussProfile
 
+class _BufferArray(np.ndarray):
+    """float64 view of an array field inside a lattice buffer: item writes
+    go to the buffer (and invalidate its cached image), as the reference's
+    CObject array fields are views of their buffer."""
+
+    def __array_finalize__(self, obj):
+        self._cb = getattr(obj, "_cb", None)
+
+    def __setitem__(self, key, value):
+        super().__setitem__(key, value)
+        if self._cb is not None:
+            self._cb.touch()
+
+
 class TriCubData(_Element):
     """Tricubic interpolation table (python/sixtracklib/tricub.py:21-49):
     grid origin, step and size per axis, mirror flags, and nx ny nz x 8
-    coefficients.  The TriCub map is compiled out of the reference's default
-    build, and here: tracking through a TriCub (or a TriCubData in the
-    lattice) fails, as there."""
+    values: f, df/dx, df/dy, df/dz, d2f/dxdy, d2f/dxdz, d2f/dydz,
+    d3f/dxdydz (derivatives scaled by the grid steps) at node
+    l + 8 (ix + nx (iy + ny iz)).  The table is zero-filled unless given;
+    ``table_addr`` of an element in a buffer is a view of the buffer, so
+    ``table_addr[i] = v`` edits the buffer, as with the reference.  The
+    TriCub map is disabled in the reference's default build and here
+    (a TriCubData in the lattice then fails to track too); the
+    ``track_tricub`` configuration key enables or skips it."""
 
     _typeid = TYPE_TRICUB_DATA
     _fields = (
@@ -718,6 +737,37 @@ class TriCubData(_Element):
         ("table_addr", ("p", "nx*ny*nz*8")),
     )
 
+    def __init__(self, cbuffer=None, nx=0, ny=0, nz=0, table_addr=None, **kw):
+        n = int(nx) * int(ny) * int(nz) * 8
+        table = np.zeros(n) if table_addr is None else np.asarray(table_addr, dtype=np.float64)
+        if table.size != n:
+            raise ValueError(f"TriCubData: {table.size} table values for {n} = nx ny nz 8")
+        super().__init__(cbuffer=cbuffer, nx=nx, ny=ny, nz=nz, table_addr=table.ravel(), **kw)
+        self._attach_table()
+
+    def _attach_table(self):
+        cb, index = self.__dict__.get("_cbuffer"), self.__dict__.get("_index")
+        if cb is None or index is None:
+            return
+        obj = cb.objects[index]
+        off = int(obj.words[12])
+        n = self._array_len(self, "nx*ny*nz*8")
+        view = obj.words[off:off + n].view(np.float64).view(_BufferArray)
+        view._cb = cb
+        object.__setattr__(self, "table_addr", view)
+
+    @classmethod
+    def _from_cobject(cls, obj, cbuffer=None, index=None):
+        self = super()._from_cobject(obj, cbuffer, index)
+        if isinstance(self, cls):
+            self._attach_table()
+        return self
+
+    def __setattr__(self, name, value):
+        super().__setattr__(name, value)
+        if name == "table_addr":
+            self._attach_table()
+
     @staticmethod
     def ptr_offset():
         return 0
@@ -725,8 +775,13 @@ class TriCubData(_Element):
 
 class TriCub(_Element):
     """Tricubic-interpolated kick element (python/sixtracklib/tricub.py:52-68);
-    ``data_addr`` holds the address of its TriCubData (the reference's
-    TrackJob assigns it).  Compiled out: tracking through it fails."""
+    ``data_addr`` holds the address of its TriCubData: a job assigns it from
+    a stored buffer (tricub.TriCub_buffer_create_assign_address_item), or
+    ``data`` names a TriCubData of the same buffer, whose absolute address
+    is written into ``data_addr`` whenever the buffer is serialised.  The map
+    is disabled in the reference's default build and here (tracking through
+    it fails); the ``track_tricub`` configuration key ("enabled", "skip",
+    "disabled") selects it."""
 
     _typeid = TYPE_TRICUB
     _fields = (
@@ -734,6 +789,22 @@ class TriCub(_Element):
         ("dipolar_kick_px", "f"), ("dipolar_kick_py", "f"), ("dipolar_kick_ptau", "f"),
         ("length", "f"), ("data_addr", "u"),
     )
+
+    def __init__(self, data=None, cbuffer=None, **kw):
+        self.data = None if data is None else int(data)
+        super().__init__(cbuffer=cbuffer, **kw)
+
+    def _encode(self):
+        typeid, words, arrays = super()._encode()
+        links = [] if self.data is None else [(7, self.data)]
+        return typeid, words, arrays, links
+
+    @classmethod
+    def _from_cobject(cls, obj: CObject, cbuffer=None, index=None):
+        self = super()._from_cobject(obj, cbuffer, index)
+        if isinstance(self, cls):
+            self.data = obj.links[0][1] if obj.links else None
+        return self
 
     @staticmethod
     def data_addr_offset():

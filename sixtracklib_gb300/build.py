@@ -31,6 +31,7 @@ CUDA_SOURCES = {
     "noalloc.cu": [],
     "adjoint.cu": [],
     "batch.cu": [],
+    "tricub.cu": ["-fmad=false"],
 }
 
 

@@ -32,6 +32,7 @@ SLOT = 8
 HEADER_WORDS = 8
 DEFAULT_BASE = 4096
 TYPE_SC_INTERPOLATED_PROF = 257
+TYPE_TRICUB = 261
 
 
 @dataclass
@@ -240,14 +241,16 @@ class CBuffer:
                 j += 1
             out.objects.append(CObject(t, words, ptrs))
         # interpolated space charge (type 257): field 6 addresses the line
-        # density object of the same buffer when it is linked
+        # density object of the same buffer when it is linked; TriCub (261):
+        # field 7 its TriCubData likewise
         begin_index = {b: i for i, (b, _, _) in enumerate(starts)}
         base_w = {base + b * SLOT: i for b, i in begin_index.items()}
         for o in out.objects:
-            if o.typeid == TYPE_SC_INTERPOLATED_PROF and o.words.size > 6:
-                tgt = base_w.get(int(o.words[6]))
-                if tgt is not None:
-                    o.links.append((6, tgt))
+            for typeid, f in ((TYPE_SC_INTERPOLATED_PROF, 6), (TYPE_TRICUB, 7)):
+                if o.typeid == typeid and o.words.size > f:
+                    tgt = base_w.get(int(o.words[f]))
+                    if tgt is not None:
+                        o.links.append((f, tgt))
         return out
 
 

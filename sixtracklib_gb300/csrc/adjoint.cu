@@ -28,7 +28,7 @@
 // memory and added to the global gradient once per CTA and launch.
 //
 // Apertures contribute no derivative (a loss is a discontinuity).  Lattices
-// with elements that have no adjoint (maps compiled out, such as TriCub, and
+// with elements that have no adjoint (the TriCub map, disabled maps and
 // unknown type ids) are refused before launch.
 #include <cuda_runtime.h>
 
@@ -893,10 +893,10 @@ extern "C" st_track_status_t st_DeviceLattice_adjoint_turns(
         set_error("adjoint: invalid lattice");
         return -1;
     }
-    uint32_t const no_adjoint = (1u << OP_FAIL) | (1u << OP_FAIL_LOST);
+    uint32_t const no_adjoint = (1u << OP_FAIL) | (1u << OP_FAIL_LOST) | (1u << OP_TRICUB);
     if (v.op_mask & no_adjoint) {
         set_error("adjoint: the lattice contains elements without an adjoint "
-                  "(a disabled map or an unknown type)");
+                  "(a TriCub, a disabled map or an unknown type)");
         return -1;
     }
     if (turn_end < turn_begin) {

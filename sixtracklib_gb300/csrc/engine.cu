@@ -47,7 +47,19 @@ struct Options {
     int stages = kDefaultStages;
     int chunk_words = 1024;
     int blocks_per_sm = 2;
+    // SIXTRL_TRACK_BEAMBEAM4D / _BEAMBEAM6D / _SPACECHARGE / _TRICUB
+    int track_bb4d = MAP_ENABLED, track_bb6d = MAP_ENABLED, track_sc = MAP_ENABLED;
+    int track_tricub = MAP_DISABLED;
 };
+
+// "enabled" | "skip" | "disabled" (python/sixtracklib/config.py.template)
+static int map_flag(const std::string &v)
+{
+    if (v == "enabled") return MAP_ENABLED;
+    if (v == "skip") return MAP_SKIP;
+    if (v == "disabled" || v == "disable") return MAP_DISABLED;
+    throw std::invalid_argument(v);
+}
 
 static std::string trim(const std::string &s)
 {
@@ -123,6 +135,14 @@ static bool parse_options(const char *cfg, Options *o, std::string *err)
                     o->chunk_words = std::stoi(v);
                 } else if (k == "blocks_per_sm") {
                     o->blocks_per_sm = std::stoi(v);
+                } else if (k == "track_beambeam4d") {
+                    o->track_bb4d = map_flag(v);
+                } else if (k == "track_beambeam6d") {
+                    o->track_bb6d = map_flag(v);
+                } else if (k == "track_spacecharge") {
+                    o->track_sc = map_flag(v);
+                } else if (k == "track_tricub") {
+                    o->track_tricub = map_flag(v);
                 } else {
                     if (err) *err = "config: unknown key '" + k + "'";
                     return false;
@@ -268,6 +288,10 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     copt.aperture_mode = opt.aperture_mode;
     copt.aperture_min_length = opt.aperture_min_length;
     copt.min_chunk_words = opt.chunk_words;
+    copt.track_bb4d = opt.track_bb4d;
+    copt.track_bb6d = opt.track_bb6d;
+    copt.track_sc = opt.track_sc;
+    copt.track_tricub = opt.track_tricub;
     std::string err;
     if (!compile_lattice(img, b, e, copt, &s->cs, &err)) {
         set_error(err);
@@ -278,8 +302,9 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     size_t const obytes = s->cs.elem_offset.size() * 8;
     size_t const side_at = (bytes + sbytes + obytes + 15) & ~(size_t)15;
     size_t const side_bytes = s->cs.side.size() * 8;
+    size_t const device_bytes = s->cs.side_device_words * 8;
     if (!cuda_ok(cudaSetDevice(dev->id), "cudaSetDevice") ||
-        !cuda_ok(cudaMalloc(&s->d, side_at + side_bytes + 8), "cudaMalloc(lattice)"))
+        !cuda_ok(cudaMalloc(&s->d, side_at + side_bytes + device_bytes + 8), "cudaMalloc(lattice)"))
         return nullptr;
     // out-of-line tables: their device addresses go into the records
     uint64_t const side_base = (uint64_t)(uintptr_t)s->d + side_at;
@@ -287,7 +312,7 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
     if ((side_bytes > 0 &&
          !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + side_at, s->cs.side.data(),
                              side_bytes, cudaMemcpyHostToDevice),
-                  "cudaMemcpy(line-density tables)")) ||
+                  "cudaMemcpy(side tables)")) ||
         !cuda_ok(cudaMemcpy(reinterpret_cast<char *>(s->d) + bytes + sbytes,
                             s->cs.elem_offset.data(), obytes, cudaMemcpyHostToDevice),
                  "cudaMemcpy(element offsets)") ||
@@ -297,6 +322,16 @@ static std::unique_ptr<DevStream> build_stream(const ImageView &img, uint64_t b,
                             cudaMemcpyHostToDevice),
                  "cudaMemcpy(s table)"))
         return nullptr;
+    // TriCub cell coefficients, computed on the GPU from the node tables
+    if (!s->cs.tricub_tables.empty()) {
+        double *side_dev = reinterpret_cast<double *>(reinterpret_cast<char *>(s->d) + side_at);
+        for (const auto &t : s->cs.tricub_tables)
+            if (!cuda_ok((cudaError_t)launch_tricub_cells(side_dev + t.nodes, side_dev + t.cells,
+                                                          t.nx, t.ny, t.nz, nullptr),
+                         "tricub cell coefficients"))
+                return nullptr;
+        if (!cuda_ok(cudaDeviceSynchronize(), "tricub cell coefficients")) return nullptr;
+    }
     s->s_table = reinterpret_cast<const double *>(reinterpret_cast<char *>(s->d) + bytes);
     s->elem_offset =
         reinterpret_cast<const int64_t *>(reinterpret_cast<char *>(s->d) + bytes + sbytes);

@@ -71,6 +71,12 @@ int launch_track(const TrackParams &prm, bool fast, int threads, int blocks_per_
                  void *stream);
 size_t track_smem_bytes(int stages, int chunk_words);
 
+// TriCub cell coefficients (tricub.cu): from the node table `nodes` (8
+// values per node of an nx x ny x nz grid) into `cells` (64 per cell), on
+// `stream`.  Returns the CUDA error code of the launch.
+int launch_tricub_cells(const double *nodes, double *cells, int64_t nx, int64_t ny, int64_t nz,
+                        void *stream);
+
 // Batched tracking (track_kernel.cu): a work item is a tile of particles of
 // one lattice variant, starting at particle `first`.
 struct BatchItem {

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <map>
 
 namespace stg {
 
@@ -27,6 +28,8 @@ struct Emitter {
     // {record, parameter index, offset in the side data}: parameter words
     // that receive the device address of out-of-line data
     std::vector<std::array<uint64_t, 3>> side_refs;
+    // the same for offsets into the device-only region after the side data
+    std::vector<std::array<uint64_t, 3>> device_refs;
     void push(uint32_t op, uint32_t aux, const std::vector<uint64_t> &params)
     {
         uint32_t const n = (uint32_t)params.size() + 1;
@@ -42,6 +45,13 @@ bool bad(std::string *err, uint64_t i, const char *what)
     return false;
 }
 
+// Opcode of an element whose map is skipped or disabled by its feature flag.
+uint32_t flagged_op(int flag) { return flag == MAP_SKIP ? OP_NOP : OP_FAIL; }
+
+// Cell tables of one lattice are capped at this many cells in total
+// (64 coefficients, 512 bytes each: 32 GiB).
+constexpr uint64_t kMaxTricubCells = (uint64_t)1 << 26;
+
 }  // namespace
 
 bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
@@ -52,6 +62,10 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
     out->monitor_elements.clear();
     out->side.clear();
     out->side_fixups.clear();
+    out->side_device_words = 0;
+    out->tricub_tables.clear();
+    std::map<uint64_t, size_t> tricub_of_data;  // TriCubData address -> table
+    uint64_t tricub_cells = 0;
     out->s_table.assign(1, 0.0);
     uint32_t op_mask = 0;
     for (uint64_t i = begin; i < end; ++i) {
@@ -155,6 +169,10 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             break;
         }
         case ST_OBJECT_TYPE_BEAM_BEAM_4D: {
+            if (opt.track_bb4d != MAP_ENABLED) {
+                op = flagged_op(opt.track_bb4d);
+                break;
+            }
             if (!need(2)) return bad(err, i, "truncated beam-beam 4d");
             const uint64_t *bd = img.deref(i, 1);
             if (!bd || w[0] < 11) return bad(err, i, "beam-beam 4d data missing");
@@ -167,6 +185,10 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             break;
         }
         case ST_OBJECT_TYPE_BEAM_BEAM_6D: {
+            if (opt.track_bb6d != MAP_ENABLED) {
+                op = flagged_op(opt.track_bb6d);
+                break;
+            }
             if (!need(2)) return bad(err, i, "truncated beam-beam 6d");
             const uint64_t *bd = img.deref(i, 1);
             if (!bd || w[0] < 38) return bad(err, i, "beam-beam 6d data missing");
@@ -195,11 +217,19 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             break;
         }
         case ST_OBJECT_TYPE_SC_COASTING:
+            if (opt.track_sc != MAP_ENABLED) {
+                op = flagged_op(opt.track_sc);
+                break;
+            }
             if (!need(9)) return bad(err, i, "truncated space-charge coasting");
             op = OP_SC_COASTING;
             p.assign(w, w + 9);
             break;
         case ST_OBJECT_TYPE_SC_QGAUSSIAN_PROF:
+            if (opt.track_sc != MAP_ENABLED) {
+                op = flagged_op(opt.track_sc);
+                break;
+            }
             if (!need(11)) return bad(err, i, "truncated space-charge q-gaussian");
             op = OP_SC_QGAUSS;
             p.assign(w, w + 11);
@@ -233,6 +263,11 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             }
             break;
         case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {
+            // With space charge skipped or disabled the reference's
+            // dispatcher has no case label for this type: the preprocessor
+            // branch that starts in the q-Gaussian case (track.h:537-575)
+            // encloses it, so the default branch loses the particle.
+            if (opt.track_sc != MAP_ENABLED) break;
             // be_beamfields/track.h:273-337.  interpol_data_addr (field 6)
             // is a plain address of a NS(LineDensityProfileData): inside
             // this buffer, or else a host address, which the reference's CPU
@@ -305,12 +340,89 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
             out->monitor_elements.push_back(i);
             break;
         }
-        case ST_OBJECT_TYPE_TRICUB:
         case ST_OBJECT_TYPE_TRICUB_DATA:
-            // TriCub is compiled "disabled" in the reference's default build
-            // (Settings.cmake.default): tracking returns failure.
-            op = OP_FAIL;
+            // track.h:446-460: skipped unless the TriCub map is disabled
+            op = opt.track_tricub == MAP_DISABLED ? OP_FAIL : OP_NOP;
             break;
+        case ST_OBJECT_TYPE_TRICUB: {
+            // TriCub is "disabled" in the reference's default build
+            // (Settings.cmake.default): tracking returns failure.
+            if (opt.track_tricub != MAP_ENABLED) {
+                op = flagged_op(opt.track_tricub);
+                break;
+            }
+            // be_tricub/track.h:51-224.  data_addr (field 7) is a plain
+            // address of a NS(TriCubData) {x0, dx, nx, y0, dy, ny, z0, dz,
+            // nz, mirror_x, mirror_y, mirror_z, table_addr}
+            // (be_tricub.h:33-52): inside this buffer, or else a host
+            // address (a stored buffer the job assigned it from).
+            if (!need(8)) return bad(err, i, "truncated tricub");
+            uint64_t const addr = w[7];
+            uint64_t const dw = addr ? img.word_of(addr) : UINT64_MAX;
+            bool const inside = dw != UINT64_MAX && dw + 13 <= img.size_words;
+            if (addr == 0) {
+                op = OP_FAIL;  // no data: the reference dereferences null
+                break;
+            }
+            const uint64_t *td = inside ? img.img + dw : reinterpret_cast<const uint64_t *>((uintptr_t)addr);
+            int64_t const nx = (int64_t)td[2], ny = (int64_t)td[5], nz = (int64_t)td[8];
+            if (nx < 2 || ny < 2 || nz < 2) {
+                op = OP_FAIL;  // no grid cell: every particle is outside
+                break;
+            }
+            uint64_t const cells = (uint64_t)(nx - 1) * (uint64_t)(ny - 1) * (uint64_t)(nz - 1);
+            if (nx > ((int64_t)1 << 26) || ny > ((int64_t)1 << 26) || nz > ((int64_t)1 << 26) ||
+                cells > kMaxTricubCells)
+                return bad(err, i, "tricub grid too large");
+            auto found = tricub_of_data.find(addr);
+            size_t tab;
+            if (found != tricub_of_data.end()) {
+                tab = found->second;
+            } else {
+                if (tricub_cells + cells > kMaxTricubCells)
+                    return bad(err, i, "tricub grids too large in total");
+                uint64_t const nvals = (uint64_t)nx * (uint64_t)ny * (uint64_t)nz * 8u;
+                const uint64_t *nodes;
+                if (inside) {
+                    uint64_t const tw = img.word_of(td[12]);
+                    if (tw == UINT64_MAX || tw + nvals > img.size_words)
+                        return bad(err, i, "tricub table outside the lattice buffer");
+                    nodes = img.img + tw;
+                } else {
+                    nodes = reinterpret_cast<const uint64_t *>((uintptr_t)td[12]);
+                    if (!nodes) return bad(err, i, "tricub data without a table");
+                }
+                CompiledStream::TricubTable t;
+                t.nodes = out->side.size();
+                t.cells = out->side_device_words;
+                t.nx = nx;
+                t.ny = ny;
+                t.nz = nz;
+                out->side.insert(out->side.end(), nodes, nodes + nvals);
+                out->side.resize((out->side.size() + 1) & ~(size_t)1);
+                out->side_device_words += cells * 64u;
+                tricub_cells += cells;
+                tab = out->tricub_tables.size();
+                out->tricub_tables.push_back(t);
+                tricub_of_data[addr] = tab;
+            }
+            op = OP_TRICUB;
+            double const dx = w2d(td[1]), dy = w2d(td[4]), dz = w2d(td[7]);
+            double const inv_dx = 1. / dx, inv_dy = 1. / dy, inv_dz = 1. / dz;
+            double const length = w2d(w[6]);
+            aux = ((int64_t)td[9] == 1 ? TRICUB_MIRROR_X : 0u) |
+                  ((int64_t)td[10] == 1 ? TRICUB_MIRROR_Y : 0u) |
+                  ((int64_t)td[11] == 1 ? TRICUB_MIRROR_Z : 0u);
+            p = {w[0], w[1], w[2], w[3], w[4], w[5],
+                 d2w(length * inv_dx), d2w(length * inv_dy), d2w(length * inv_dz),
+                 td[0], td[3], td[6],
+                 d2w(inv_dx), d2w(inv_dy), d2w(inv_dz),
+                 d2w((double)(nx - 2)), d2w((double)(ny - 2)), d2w((double)(nz - 2)),
+                 (uint64_t)(nx - 1), (uint64_t)(ny - 1), 0};
+            em.device_refs.push_back({(uint64_t)em.rec_len.size(), (uint64_t)p.size() - 1,
+                                      out->tricub_tables[tab].cells});
+            break;
+        }
         default:
             op = OP_FAIL_LOST;
             break;
@@ -354,6 +466,11 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
     if (used > 0 || nchunks == 0) close_chunk();
     for (const auto &r : em.side_refs)
         out->side_fixups.push_back({(uint64_t)out->elem_offset[r[0]] + 1u + r[1], r[2]});
+    // the device-only region follows the side data (kept 16-byte aligned)
+    uint64_t const device_at = out->side.size();
+    for (auto &t : out->tricub_tables) t.cells += device_at;
+    for (const auto &r : em.device_refs)
+        out->side_fixups.push_back({(uint64_t)out->elem_offset[r[0]] + 1u + r[1], device_at + r[2]});
     out->info.num_elements = (int64_t)(end - begin);
     out->info.num_chunks = nchunks;
     out->info.chunk_words = (int32_t)cw;

@@ -912,4 +912,109 @@ static __device__ __noinline__ PState sc_interpolated(PState p, const uint64_t *
     return p;
 }
 
+// be_tricub/track.h:51-224: the kick of a tricubic interpolant of a
+// potential on a regular grid.  c: the record's parameters (stream.h
+// OP_TRICUB); the cell's 64 polynomial coefficients come from the table the
+// uploader computed (tricub.cu) with the reference's arithmetic, so they
+// equal the ones NS(tricub_construct_coefs) forms per particle.  The
+// reference reads outside its table for a particle outside the grid (only a
+// debug assertion guards it); here such a particle is lost and the map fails
+// (state 0 on return).
+//   exact: the three derivative sums term by term in the reference's order
+//          (i, then j, then k; each term ((c x^i) y^j) z^k times the power);
+//   fast:  the sums as nested Horner forms over z, y and x with FMAs.
+template <bool FAST>
+static __device__ __noinline__ PState tricub(PState p, const uint64_t *rec, uint32_t aux)
+{
+    const uint64_t *c = rec + 1;
+    double const z = p.zeta / (p.beta0 * p.rvv);
+    double const fx = ((p.x - W(c[0])) - W(c[9])) * W(c[12]);
+    double const fy = ((p.y - W(c[1])) - W(c[10])) * W(c[13]);
+    double const fz = ((z - W(c[2])) - W(c[11])) * W(c[14]);
+    double const sign_x = ((aux & TRICUB_MIRROR_X) && fx < 0.0) ? -1. : 1.;
+    double const sign_y = ((aux & TRICUB_MIRROR_Y) && fy < 0.0) ? -1. : 1.;
+    double const sign_z = ((aux & TRICUB_MIRROR_Z) && fz < 0.0) ? -1. : 1.;
+    double const sfx = sign_x * fx, sfy = sign_y * fy, sfz = sign_z * fz;
+    double const ixf = floor(sfx), iyf = floor(sfy), izf = floor(sfz);
+    // inside the grid: 0 <= i <= n - 2 in every coordinate (NaN fails)
+    if (!(ixf >= 0.0 && ixf <= W(c[15]) && iyf >= 0.0 && iyf <= W(c[16]) && izf >= 0.0 &&
+          izf <= W(c[17]))) {
+        p.state = 0;
+        return p;
+    }
+    int64_t const ix = (int64_t)ixf, iy = (int64_t)iyf, iz = (int64_t)izf;
+    double const xn = sfx - ixf, yn = sfy - iyf, zn = sfz - izf;
+    const double *cf = reinterpret_cast<const double *>(c[20]) +
+                       64 * (ix + (int64_t)c[18] * (iy + (int64_t)c[19] * iz));
+    double kpx, kpy, kpt;
+    if (FAST) {
+        double dfx = 0.0, dfy = 0.0, dfz = 0.0;
+#pragma unroll
+        for (int i = 3; i >= 0; --i) {
+            double R = 0.0, S = 0.0, T = 0.0;  // sums over j of P, j P y^-1, Q
+#pragma unroll
+            for (int j = 3; j >= 0; --j) {
+                double2 const a = __ldg(reinterpret_cast<const double2 *>(cf + 4 * j + 16 * i));
+                double2 const b = __ldg(reinterpret_cast<const double2 *>(cf + 4 * j + 16 * i + 2));
+                // P = sum_k c_ijk z^k, Q = dP/dz
+                double const P = fma(fma(fma(b.y, zn, b.x), zn, a.y), zn, a.x);
+                double const Q = fma(fma(3.0 * b.y, zn, 2.0 * b.x), zn, a.y);
+                if (j >= 1) S = fma(S, yn, (double)j * P);
+                R = fma(R, yn, P);
+                T = fma(T, yn, Q);
+            }
+            if (i >= 1) dfx = fma(dfx, xn, (double)i * R);
+            dfy = fma(dfy, xn, S);
+            dfz = fma(dfz, xn, T);
+        }
+        kpx = dfx;
+        kpy = dfy;
+        kpt = dfz;
+    } else {
+        double const x2 = xn * xn, y2 = yn * yn, z2 = zn * zn;
+        double const xp[4] = {1., xn, x2, x2 * xn};
+        double const yp[4] = {1., yn, y2, y2 * yn};
+        double const zp[4] = {1., zn, z2, z2 * zn};
+        kpx = 0.;
+#pragma unroll
+        for (int i = 1; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    kpx += (double)i * (((__ldg(cf + k + 4 * j + 16 * i) * xp[i - 1]) * yp[j]) * zp[k]);
+        kpy = 0.;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 1; j < 4; ++j)
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    kpy += (double)j * (((__ldg(cf + k + 4 * j + 16 * i) * xp[i]) * yp[j - 1]) * zp[k]);
+        kpt = 0.;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int k = 1; k < 4; ++k)
+                    kpt += (double)k * (((__ldg(cf + k + 4 * j + 16 * i) * xp[i]) * yp[j]) * zp[k - 1]);
+    }
+    kpx *= W(c[6]);
+    kpx *= -sign_x;
+    kpx -= W(c[3]);
+    kpy *= W(c[7]);
+    kpy *= -sign_y;
+    kpy -= W(c[4]);
+    kpt *= W(c[8]);
+    kpt *= -sign_z;
+    kpt -= W(c[5]);
+    double const q = p.q0 * p.charge_ratio;
+    double const energy_kick = q * (p.p0c * kpt);
+    p.px += kpx;
+    p.py += kpy;
+    add_energy(p, energy_kick);
+    return p;
+}
+
 }  // namespace stg

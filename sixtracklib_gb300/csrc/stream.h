@@ -54,10 +54,25 @@ enum Op : uint32_t {
                             // word offsets into it) lies in device memory
                             // outside the stream; aux bit0: interpolate (else
                             // the fallback density)
+    OP_TRICUB = 22,         // [x_shift, y_shift, tau_shift, dipolar_kick_px,
+                            //  dipolar_kick_py, dipolar_kick_ptau,
+                            //  length / dx, length / dy, length / dz,
+                            //  x0, y0, z0, 1 / dx, 1 / dy, 1 / dz,
+                            //  nx - 2, ny - 2, nz - 2 (as doubles),
+                            //  nx - 1, ny - 1 (cells per row / plane),
+                            //  cell coefficient table address]
+                            // aux bits 0-2: mirror in x, y, z.  The table (64
+                            // coefficients per grid cell, x^i y^j z^k at
+                            // k + 4 j + 16 i) lies in device memory outside
+                            // the stream, computed there from the node table
     OP_COUNT
 };
 
 constexpr uint32_t DRIFT_APERTURE = 1u;
+// TriCub aux flags: mirror the grid coordinate in x / y / z (mirror_* == 1).
+constexpr uint32_t TRICUB_MIRROR_X = 1u;
+constexpr uint32_t TRICUB_MIRROR_Y = 2u;
+constexpr uint32_t TRICUB_MIRROR_Z = 4u;
 // SC q-Gaussian aux flag: the transverse field is the round one.
 constexpr uint32_t SC_ROUND = 1u;
 constexpr uint32_t SC_ELL_X = 2u;

@@ -269,6 +269,12 @@ __device__ __forceinline__ int apply(PState &p, const uint64_t *rec, uint64_t hd
             p = sc_interpolated(p, rec, aux);
             return 0;
         }
+    case OP_TRICUB:
+        if constexpr (PLAIN) break;
+        else {
+            p = tricub<FAST>(p, rec, aux);
+            return p.state == 1 ? 0 : -1;  // outside the grid: lost, failure
+        }
     case OP_MONITOR: {
         uint64_t *out = reinterpret_cast<uint64_t *>(rec[8]);
         if (out == nullptr) return 0;

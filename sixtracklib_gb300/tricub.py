@@ -1,8 +1,12 @@
 """TriCub elements (python/sixtracklib/tricub.py).  The TriCub map is
-compiled out of the reference's default build and of this engine: a lattice
-with a TriCub fails to track.  The element classes and the address
-assignment of a table exist so that such lattices can be built, stored and
-read as with the reference."""
+disabled in the reference's default build (Settings.cmake.default) and in
+this engine's default configuration: a lattice with a TriCub fails to
+track.  The configuration key ``track_tricub`` ("enabled", "skip",
+"disabled") selects the map per job or tracker, as SIXTRACKL_TRACK_TRICUB
+selects it per reference build.  The TriCubData's table is gathered to the
+GPU when the lattice is compiled; a job assigns its address to the TriCub
+from a stored buffer (below), or the TriCub names TriCubData of its own
+buffer."""
 
 from __future__ import annotations
 

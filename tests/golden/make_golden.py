@@ -29,6 +29,12 @@ Two kinds of fixture:
    the stored payloads, bb6d_shipped.npz (`--bb6d`).
 6. The shipped pysixtrack lines of `bbsimple` and `beambeam` as gzipped
    JSON, line_<name>.json.gz (`--lines`).
+7. The TriCub map and the map feature flags (`--tricub`): the reference's
+   TriCub known-answer kicks (tests/testdata/tricub/precomputed_kicks.txt,
+   read as text) with their seed, tricub_kicks.npz; the reference's builds
+   with other feature flags (oracle/_ref/libstref_flags_{a,b}.so, TriCub
+   enabled in `a`) tracking tests/tricub_cases.py's lattices,
+   ref_tricub.npz and ref_flags.npz.
 """
 
 from __future__ import annotations
@@ -266,7 +272,63 @@ def lines_fixture():
         print(f"line_{name}: {len(out)} elements")
 
 
+def tricub_fixtures():
+    """tricub_kicks.npz, ref_tricub.npz, ref_flags.npz (see the module doc)."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    import tricub_cases as tc
+
+    with open(os.path.join(TD, "tricub", "precomputed_kicks.txt")) as f:
+        rows = [r.split() for r in f.read().strip().split("\n")]
+    kicks = np.array([[float(v) for v in r] for r in rows[:-1]])
+    seed = int(float(rows[-1][0]))
+    np.savez_compressed(os.path.join(HERE, "tricub_kicks.npz"), kicks=kicks,
+                        seed=np.int64(seed))
+    print(f"tricub_kicks: {kicks.shape[0]} particles, seed {seed}")
+
+    orc = Oracle()
+    ref_a = Oracle.reference(flags="a")
+    if ref_a is None:
+        raise SystemExit("reference build not available (REF_ROOT)")
+    # the reference reads outside its table for a particle outside the grid:
+    # the oracle (which stops such a particle) runs first and must succeed
+    ring = tc.tricub_ring()
+    img = ring.cbuffer.to_image()
+    p = tc.tricub_particles(512, 21)
+    arrays = dict(lattice=img, initial=p.block.copy())
+    orc.set_track_flags(*tc.FLAG_BUILDS["a"])
+    for turns in (1, 20):
+        chk = p.block.copy()
+        if orc.track_until(img, chk, turns) != 0:
+            raise SystemExit("tricub ring: a particle leaves a grid")
+        fin = p.block.copy()
+        arrays[f"final_{turns}"] = fin
+        arrays[f"status_{turns}"] = np.int64(ref_a.track_until(img, fin, turns))
+    np.savez_compressed(os.path.join(HERE, "ref_tricub.npz"), **arrays)
+
+    lat = tc.flags_lattice()
+    img = lat.cbuffer.to_image()
+    p = tc.tricub_particles(64, 8)
+    arrays = dict(lattice=img, initial=p.block.copy())
+    for name, flags in tc.FLAG_BUILDS.items():
+        ref = Oracle.reference(flags=None if name == "default" else name)
+        fin = p.block.copy()
+        arrays[f"until_{name}"] = fin
+        arrays[f"until_status_{name}"] = np.int64(ref.track_until(img, fin, 3))
+        lines, status = [], []
+        for k in range(len(lat)):
+            fin = p.block.copy()
+            status.append(ref.track_line(img, fin, k, k + 1))
+            lines.append(fin)
+        arrays[f"line_{name}"] = np.stack(lines)
+        arrays[f"line_status_{name}"] = np.array(status, dtype=np.int64)
+    np.savez_compressed(os.path.join(HERE, "ref_flags.npz"), **arrays)
+    print("ref_tricub, ref_flags written")
+
+
 def main():
+    if "--tricub" in sys.argv:
+        tricub_fixtures()
+        return
     if "--lines" in sys.argv:
         lines_fixture()
         return
