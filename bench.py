@@ -37,6 +37,12 @@ particle passes counts once (lost particles stop counting where they are lost).
               elliptic (sigma_y = 1.3 sigma_x) strong beams; 5 turns timed
               with CUDA events after 2 warm-up turns, next to the oracle on
               the host cores on a strided sample of the same particles.
+  tricub      the TriCub map enabled (track_tricub=enabled): the FODO ring
+              plus 64 TriCub kicks sharing one 100 x 100 x 50 field map,
+              262,144 Gaussian protons, 5 turns timed with CUDA events after
+              2 warm-up turns (the first call also computes the map's cell
+              coefficients on the GPU, timed apart), FP64 roofline with the
+              Horner operation count, the oracle on the host cores beside it.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -80,6 +86,9 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-bbsc", action="store_true")
+    ap.add_argument("--no-tricub", action="store_true")
+    ap.add_argument("--tricub-particles", type=int, default=262144)
+    ap.add_argument("--tricub-turns", type=int, default=5)
     ap.add_argument("--batch-variants", type=int, default=256)
     ap.add_argument("--batched-turns", type=int, default=20)
     ap.add_argument("--batched-detail", action="store_true",
@@ -210,11 +219,13 @@ def host_cpu_model() -> str:
     return f"{name or platform.processor() or platform.machine()}, {os.cpu_count()} cores"
 
 
-def cpu_baseline(ring, parts, seconds, threads=None):
-    """Time the oracle (OpenMP over particles) on a sample of the workload."""
+def cpu_baseline(ring, parts, seconds, threads=None, flags=None):
+    """Time the oracle (OpenMP over particles) on a sample of the workload
+    (map feature flags `flags` as Oracle.set_track_flags takes them)."""
     from oracle.pyoracle import Oracle
 
     orc = Oracle()
+    orc.set_track_flags(*(flags or ()))
     lat = ring.cbuffer.to_image()
     n_elem = len(ring)
     stride = max(1, parts.num_particles // 16384)
@@ -581,6 +592,57 @@ def bbsc_bench(args, peak):
     return out
 
 
+def tricub_bench(args, peak):
+    """The TriCub workload (see module doc): PET/s with its FP64 roofline,
+    the one-time cell-coefficient set-up, and the oracle on a sample."""
+    import torch
+
+    from sixtracklib_gb300 import lattices
+    from sixtracklib_gb300.device import DeviceTracker
+    from sixtracklib_gb300.roofline import lattice_flops_per_pet
+
+    n, turns = args.tricub_particles, args.tricub_turns
+    ring = lattices.tricub_field_ring()
+    parts = lattices.gaussian_particles(n, seed=3)
+    img = ring.cbuffer.to_image()
+    t0 = time.perf_counter()
+    trk = DeviceTracker(img, config=f"mode={args.mode} track_tricub=enabled")
+    setup = time.perf_counter() - t0
+    cols = torch.from_numpy(parts.block.copy().view(np.int64)).cuda()
+    if trk.track_until(cols, 2) != 0:
+        raise SystemExit("tricub: tracking failed")
+    stream = torch.cuda.current_stream()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    trk.launch_until(cols, 2 + turns)
+    b.record(stream)
+    torch.cuda.synchronize()
+    if trk.last_status() != 0:
+        raise SystemExit("tricub: tracking failed")
+    sec = a.elapsed_time(b) / 1e3
+    alive = int((cols[20] == 1).sum())
+    value = alive * len(ring) * turns / sec
+    f = lattice_flops_per_pet(ring)
+    achieved = value * f / 1e12
+    out = {"workload": f"FODO ring + 64 TriCub kicks on one 100 x 100 x 50 map ({len(ring)} "
+                       f"elements), {n} Gaussian protons, FP64 {args.mode}, {turns} turns "
+                       f"after 2 warm-up turns",
+           "unit": METRIC, "value": value, "ms_per_turn": sec / turns * 1e3, "alive": alive,
+           "setup_s": setup,
+           "roofline": {"bound": "fp64", "flops_per_pet": f, "achieved": achieved,
+                        "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak if peak and peak > 0 else None,
+                        "flops": "sixtracklib_gb300/roofline.py (TriCub: Horner form from "
+                                 "per-cell coefficients)"}}
+    if not args.no_cpu:
+        c = cpu_baseline(ring, parts, args.cpu_seconds / 2, flags=(2, 2, 2, 2))
+        out["cpu_baseline"] = c
+        out["vs_cpu"] = value / c["value"]
+    return out
+
+
 def aggregate_over_ranks(pet, elapsed, device):
     """Whole-job figures of a weak-scaling run: PET summed over ranks, time =
     the slowest rank's (every rank tracks its own particles, no exchange)."""
@@ -782,6 +844,11 @@ def run_ours(args):
             line["beam_beam_space_charge"] = bbsc_bench(args, peak)
         except Exception as exc:  # report, do not hide
             line["beam_beam_space_charge"] = {"error": str(exc)}
+    if not args.no_tricub:
+        try:
+            line["tricub"] = tricub_bench(args, peak)
+        except Exception as exc:  # report, do not hide
+            line["tricub"] = {"error": str(exc)}
     if not args.no_e2e:
         try:
             line["e2e"] = e2e_measure(ring, parts, max(2, args.steps // 2), 1, args.mode,

@@ -16,6 +16,8 @@ synthetic (no public dataset is involved) and fully determined by the seed:
   space-charge kicks on tabulated line densities;
 * :func:`learnable_fodo_ring` -- the FODO ring with 64 quadrupole and 16
   sextupole strengths marked as learnable (differentiable tracking);
+* :func:`tricub_field_ring` -- the FODO ring plus 64 TriCub kicks sharing one
+  100 x 100 x 50 field map (a Gaussian potential bump);
 * :func:`variant_ring` / :func:`batch_specs` -- rings built like the
   synthetic ring at any size, and the 256-variant batched workload;
 * particle sets: Gaussian 6D and the polar amplitude grid.
@@ -162,6 +164,57 @@ def sc_interpolated_ring(n_kicks=8, seed=3):
                                 interpol_data_addr=addr, line_density_prof_fallback=5e11,
                                 min_sigma_diff=1e-10)
     return e, tables
+
+
+def gaussian_bump_table(nx, ny, nz, dx, dy, dz, x0, y0, z0, amplitude, sx, sy, sz):
+    """Node table of phi = amplitude exp(-x^2/2sx^2 - y^2/2sy^2 - z^2/2sz^2)
+    for a TriCubData: f, f_x, f_y, f_z, f_xy, f_xz, f_yz, f_xyz at every
+    node, the derivatives scaled by the grid steps, at l + 8 (ix + nx (iy +
+    ny iz))."""
+    def axis(n, d, o, s):
+        u = o + d * np.arange(n)
+        g = np.exp(-0.5 * (u / s) ** 2)
+        return g, -u / (s * s) * g * d  # value, derivative times the step
+
+    gx, dgx = axis(nx, dx, x0, sx)
+    gy, dgy = axis(ny, dy, y0, sy)
+    gz, dgz = axis(nz, dz, z0, sz)
+    kinds = [(gx, gy, gz), (dgx, gy, gz), (gx, dgy, gz), (gx, gy, dgz),
+             (dgx, dgy, gz), (dgx, gy, dgz), (gx, dgy, dgz), (dgx, dgy, dgz)]
+    t = np.empty((nz, ny, nx, 8))
+    for l, (a, b, c) in enumerate(kinds):
+        t[..., l] = amplitude * c[:, None, None] * b[None, :, None] * a[None, None, :]
+    return t.reshape(-1)
+
+
+def tricub_field_ring(n_kicks=64, length=0.5, amplitude=2e-11) -> Elements:
+    """The FODO ring plus ``n_kicks`` TriCub kicks (spread over the ring's
+    cells) that share one TriCubData: a 100 x 100 x 50 grid over +-12.4 mm
+    transversely and +-0.49 m longitudinally holding a Gaussian potential
+    bump (sigma 3 mm x 2.5 mm x 0.2 m); kicks of order 1e-8 rad.  The
+    TriCubData is the last element (skipped when the map is enabled)."""
+    e = fodo_ring()
+    n_fodo = len(e)
+    out = Elements()
+    step = max(1, n_fodo // n_kicks)
+    data_index = n_fodo + n_kicks
+    k = 0
+    for i, o in enumerate(e.get_elements()):
+        out.cbuffer.add_raw(e.cbuffer.objects[i])
+        if k < n_kicks and i % step == step - 1:
+            out.TriCub(data=data_index, length=length)
+            k += 1
+    while k < n_kicks:
+        out.TriCub(data=data_index, length=length)
+        k += 1
+    nx, ny, nz = 100, 100, 50
+    dx = dy = 0.25e-3
+    dz = 0.02
+    x0, y0, z0 = -0.5 * (nx - 1) * dx, -0.5 * (ny - 1) * dy, -0.5 * (nz - 1) * dz
+    out.TriCubData(nx=nx, ny=ny, nz=nz, x0=x0, y0=y0, z0=z0, dx=dx, dy=dy, dz=dz,
+                   table_addr=gaussian_bump_table(nx, ny, nz, dx, dy, dz, x0, y0, z0,
+                                                  amplitude, 3e-3, 2.5e-3, 0.2))
+    return out
 
 
 def variant_ring(seed: int, n_elements: int) -> Elements:

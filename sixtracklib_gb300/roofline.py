@@ -26,6 +26,17 @@ FLOPS_LIMIT_RECT_ELLIPSE = 5
 FLOPS_DIPEDGE = 4
 # add_to_energy 36 + cavity phase/energy 9
 FLOPS_CAVITY = 45
+# TriCub (be_tricub/track.h:51-224) from per-cell coefficients (an FMA
+# counted as 2): grid coordinates z, fx, fy, fz, floor, fractions (17); the
+# three partial derivatives of the tricubic as nested Horner forms (per
+# (i, j): the z polynomial 6, its z derivative 6, the y sums 4, the y
+# derivative 3 for j >= 1; per i: the x sums 7 or 4) (317); scaling by
+# length / d and the dipolar corrections (6); the energy kick 3, px / py 2
+# and add_to_energy 36.  The reference forms the 64 coefficients per
+# particle (1,000 products and 936 sums) and sums the 144 derivative terms
+# one by one (720); the coefficients depend only on the grid cell, which
+# makes them lattice preparation here (computed once per cell).
+FLOPS_TRICUB = 17 + 317 + 6 + 3 + 2 + 36
 
 
 def multipole_flops(order: int, curvature: bool = False) -> int:
@@ -63,6 +74,8 @@ def lattice_flops_per_element(cbuffer: CBuffer) -> float:
             f = FLOPS_LIMIT_RECT_ELLIPSE
         elif t == 24:
             f = FLOPS_DIPEDGE
+        elif t == 261:
+            f = FLOPS_TRICUB
         else:
             f = 0
         tot += f
@@ -178,6 +191,8 @@ def element_flops(obj, x=None, y=None) -> float:
         return FLOPS_LIMIT_RECT_ELLIPSE
     if name == "DipoleEdge":
         return FLOPS_DIPEDGE
+    if name == "TriCub":
+        return FLOPS_TRICUB
     if name == "BeamBeam4D":
         d = np.asarray(obj.data)
         if d[10] <= 0.0:

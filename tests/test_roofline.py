@@ -40,3 +40,14 @@ def test_beam_field_mix_counts():
     per_slice = (roofline.FLOPS_BB6D_SLICE + roofline.FLOPS_BB6D_SINGULAR +
                  roofline.FIELD_ROUND + roofline.G_ROUND)
     assert roofline.element_flops(bb6d, p.x, p.y) == roofline.FLOPS_BB6D_ELEMENT + n * per_slice
+
+
+def test_tricub_count():
+    ring = lattices.tricub_field_ring()
+    n = len(ring)
+    per_pet = roofline.lattice_flops_per_pet(ring)
+    assert roofline.FLOPS_TRICUB == 381
+    fodo = lattices.fodo_ring()
+    expect = (roofline.lattice_flops_per_pet(fodo) * len(fodo) + 64 * 381) / n
+    assert abs(per_pet - expect) < 1e-9
+    assert abs(roofline.lattice_flops_per_element(ring.cbuffer) - per_pet) < 1e-9
