@@ -774,6 +774,12 @@ const char *st_engine_build_info(void);
 /* Measured dense FP64 FMA throughput of `device` in TFLOP/s (FMA = 2 flops);
  * the denominator of the tracking kernel's roofline. */
 double st_engine_measure_fp64_peak(int device);
+/* The fast arithmetic policy's exponential (a table-driven e^x, within one
+ * ulp) on n values of device memory x, into device memory y, on `stream` (a
+ * cudaStream_t, NULL: the default stream); the CUDA error code of the
+ * launch.  For checking the policy's arithmetic; the tracking maps call it
+ * inline. */
+int32_t st_engine_exp_fast(const double *x, double *y, int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

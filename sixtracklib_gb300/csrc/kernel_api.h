@@ -77,6 +77,9 @@ size_t track_smem_bytes(int stages, int chunk_words);
 int launch_tricub_cells(const double *nodes, double *cells, int64_t nx, int64_t ny, int64_t nz,
                         void *stream);
 
+// The fast policy's exponential (maps.cuh exp_fast) on n device values.
+int launch_exp_fast(const double *x, double *y, int64_t n, void *stream);
+
 // Batched tracking (track_kernel.cu): a work item is a tile of particles of
 // one lattice variant, starting at particle `first`.
 struct BatchItem {

@@ -14,6 +14,7 @@
 
 #include <cstdint>
 
+#include "exp_table.h"
 #include "stream.h"
 
 namespace stg {
@@ -30,6 +31,33 @@ struct PState {
 };
 
 __device__ __forceinline__ double W(uint64_t w) { return __longlong_as_double((long long)w); }
+
+// e^x for the fast arithmetic policy: P. T. P. Tang's table-driven method
+// (ACM Trans. Math. Softw. 15 (1989) 144).  x = (256 m + j) ln2/256 + r with
+// |r| <= ln2/512; e^x = 2^m 2^(j/256) e^r, e^r - 1 by its degree-4 Taylor
+// polynomial (truncation below 4e-17 relative), 2^(j/256) from a table of
+// double pairs (exp_table.h), 2^m added to the exponent field on the integer
+// pipe.  Ten FP64 instructions (CUDA's exp: fifteen); within one ulp of e^x.
+// |x| >= 700 (results near or beyond the normal range) and NaN take CUDA's
+// exp; the test of |x| runs on the integer pipe.
+__device__ __forceinline__ double exp_fast(double x)
+{
+    if (((uint32_t)__double2hiint(x) & 0x7FFFFFFFu) >= 0x4085E000u) return exp(x);  // |x| >= 700
+    constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52: rounds to an integer
+    double const t = fma(x, kExpInvLn2N, kMagic);
+    double const n = t - kMagic;
+    int const N = __double2loint(t);
+    double r = fma(-n, __longlong_as_double((long long)kExpL1Bits), x);
+    r = fma(-n, __longlong_as_double((long long)kExpL2Bits), r);
+    double q = fma(r, 1.0 / 24.0, 1.0 / 6.0);
+    q = fma(q, r, 0.5);
+    double const p = fma(q, r * r, r);
+    int const j = N & 255;
+    double const s_hi = __ldg(&kExpTable[2 * j]);
+    double const s_lo = __ldg(&kExpTable[2 * j + 1]);
+    double const v = s_hi + fma(s_hi, p, s_lo);
+    return __hiloint2double(__double2hiint(v) + (N >> 8) * (1 << 20), __double2loint(v));
+}
 
 constexpr double kPiD = 3.1415926535897932384626433832795028841971693993751;
 constexpr double kClightD = 299792458.0;
@@ -580,7 +608,7 @@ __device__ __forceinline__ void fields_round_g_fast(double x, double y, double s
     double const inv_s2 = 1.0 / sigma2;
     double const r2 = x * x + y * y;
     double const inv_r2 = 1.0 / r2;
-    double const e = exp(-0.5 * r2 * inv_s2);
+    double const e = exp_fast(-0.5 * r2 * inv_s2);
     double const t = (r2 < 1e-20) ? k * sqrt(r2 * inv_s2) : (1 - e) * k * inv_r2;
     double const exv = t * x, eyv = t * y;
     double const c = k * inv_s2;
@@ -808,7 +836,7 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
         if (u < 0.0) u = 0.0;
         e = pow(u, W(c[14]));
     } else {
-        e = exp(arg);
+        e = FAST ? exp_fast(arg) : exp(arg);
     }
     fk *= W(c[13]) * e;
     double ex, ey, gx, gy;
@@ -817,8 +845,8 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
             double const x = p.x - W(c[5]), y = p.y - W(c[6]);
             double const r2 = x * x + y * y;
             double const t = (r2 < 1e-20) ? sqrt(r2) * W(c[16])
-                                          : (1.0 - exp(-r2 * W(c[15]))) *
-                                                (1.0 / (2. * kPiD * kEps0D)) / r2;
+                                          : (1.0 - exp_fast(-r2 * W(c[15]))) *
+                                                (1.0 / (2. * kPiD * kEps0D)) * (1.0 / r2);
             ex = t * x;
             ey = t * y;
         } else if (aux & (SC_ELL_X | SC_ELL_Y)) {
@@ -826,7 +854,7 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
             double const x = p.x - W(c[5]), y = p.y - W(c[6]);
             double const abx = fabs(x), aby = fabs(y);
             double const is = W(c[17]), fact = W(c[18]);
-            double const e = exp(-(abx * abx * W(c[21])) - aby * aby * W(c[22]));
+            double const e = exp_fast(-(abx * abx * W(c[21])) - aby * aby * W(c[22]));
             double wz_re, wz_im, we_re, we_im;
             if (aux & SC_ELL_X) {
                 cerrf(abx * is, aby * is, &wz_re, &wz_im);

@@ -10,6 +10,7 @@
 
 #include "sixtracklib_gb300.h"
 #include "device_guard.h"
+#include "kernel_api.h"
 
 namespace {
 
@@ -62,4 +63,11 @@ extern "C" double st_engine_measure_fp64_peak(int device)
     if (cudaGetLastError() != cudaSuccess) return -1.0;
     double const flops = 2.0 * 8.0 * (double)iters * (double)threads * (double)blocks;
     return flops / (best_ms * 1e-3) / 1e12;  // TFLOP/s, FMA counted as 2
+}
+
+// The fast arithmetic policy's exponential on device arrays, for checking it
+// against e^x.
+extern "C" int32_t st_engine_exp_fast(const double *x, double *y, int64_t n, void *stream)
+{
+    return stg::launch_exp_fast(x, y, n, stream);
 }

@@ -597,6 +597,24 @@ STG_INSTANTIATE(true, 2, true)
 
 namespace stg {
 
+namespace {
+__global__ void __launch_bounds__(256) exp_fast_kernel(const double *x, double *y, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = exp_fast(x[i]);
+}
+}  // namespace
+
+int launch_exp_fast(const double *x, double *y, int64_t n, void *stream)
+{
+    if (n <= 0) return 0;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    exp_fast_kernel<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, n);
+    return (int)cudaGetLastError();
+}
+
 size_t track_smem_bytes(int stages, int chunk_words)
 {
     return (size_t)(16 + (size_t)stages * chunk_words) * sizeof(uint64_t);
