@@ -780,6 +780,10 @@ double st_engine_measure_fp64_peak(int device);
  * launch.  For checking the policy's arithmetic; the tracking maps call it
  * inline. */
 int32_t st_engine_exp_fast(const double *x, double *y, int64_t n, void *stream);
+/* The fast arithmetic policy's reciprocal (the hardware estimate refined by
+ * one third-order step, within about one ulp of 1 / x) on n values of device
+ * memory x, into device memory y, as st_engine_exp_fast. */
+int32_t st_engine_rcp_fast(const double *x, double *y, int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -150,6 +150,7 @@ _SIGNATURES = {
     "st_engine_build_info": ([], cstr),
     "st_engine_measure_fp64_peak": ([C.c_int], C.c_double),
     "st_engine_exp_fast": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int32),
+    "st_engine_rcp_fast": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p], C.c_int32),
 }
 
 

@@ -79,6 +79,8 @@ int launch_tricub_cells(const double *nodes, double *cells, int64_t nx, int64_t 
 
 // The fast policy's exponential (maps.cuh exp_fast) on n device values.
 int launch_exp_fast(const double *x, double *y, int64_t n, void *stream);
+// The fast arithmetic policy's reciprocal (maps.cuh rcp_fast) on n values.
+int launch_rcp_fast(const double *x, double *y, int64_t n, void *stream);
 
 // Batched tracking (track_kernel.cu): a work item is a tile of particles of
 // one lattice variant, starting at particle `first`.

@@ -59,6 +59,25 @@ __device__ __forceinline__ double exp_fast(double x)
     return __hiloint2double(__double2hiint(v) + (N >> 8) * (1 << 20), __double2loint(v));
 }
 
+// 1 / d for the fast arithmetic policy: the hardware's reciprocal estimate
+// (PTX rcp.approx.ftz.f64, computed from the upper 32 bits of d: about 20
+// correct bits) refined by one step of the third-order iteration
+// y' = y + y (e + e^2), e = 1 - d y (Householder's method of order 2 for
+// f(y) = 1/y - d), which cubes the estimate's relative error to below
+// 2^-57: the result is within about one ulp of 1/d.  Three FP64
+// instructions.  |d| outside [2^-1000, 2^1001) -- zero, subnormals, huge
+// values, inf, NaN -- takes the IEEE division; the test runs on the integer
+// pipe.
+__device__ __forceinline__ double rcp_fast(double d)
+{
+    uint32_t const e = ((uint32_t)__double2hiint(d) >> 20) & 0x7FFu;
+    if (e - 23u > 2000u) return 1.0 / d;  // biased exponent outside [23, 2023]
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+    double const r = fma(-d, y, 1.0);
+    return fma(y, fma(r, r, r), y);
+}
+
 constexpr double kPiD = 3.1415926535897932384626433832795028841971693993751;
 constexpr double kClightD = 299792458.0;
 constexpr double kEps0D = 8.854187817620e-12;
@@ -350,6 +369,21 @@ static __device__ __noinline__ PState rf_multipole(PState p, const uint64_t *rec
 // ~1e30); 0.5 / h is taken as 0.5 (3.2 q), the product h = 1 / (3.2 q) was
 // formed from.  The values agree with the term-by-term evaluation to
 // rounding (a few 1e-15 relative).
+// The recurrence runs on a warp-uniform index: every lane of the warp steps
+// through the same n, from the largest nu of the warp down, and a lane
+// takes part from its own nu on (the warp issues max(nu) steps either way).
+// n / 2 then comes from a table indexed by the uniform n instead of an FP64
+// subtraction per step; the arithmetic of every lane is unchanged.
+__constant__ double kHalfN[32] = {0.0,  0.5,  1.0,  1.5,  2.0,  2.5,  3.0,  3.5,
+                                  4.0,  4.5,  5.0,  5.5,  6.0,  6.5,  7.0,  7.5,
+                                  8.0,  8.5,  9.0,  9.5,  10.0, 10.5, 11.0, 11.5,
+                                  12.0, 12.5, 13.0, 13.5, 14.0, 14.5, 15.0, 15.5};
+
+// FAST: the region parameter q takes products with 1 / ylim and 1 / xlim
+// (within an ulp of the quotients; nc and nu can differ only where 23 q or
+// 21 q lies within an ulp of an integer), and the final complex division
+// takes rcp_fast.
+template <bool FAST = false>
 static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_re, double *w_im)
 {
     double const a_const = 1.12837916709551;
@@ -358,29 +392,34 @@ static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_
     double wx, wy;
     double q1r = 1.0, q1i = 0.0, q2r = 0.0, q2i = 0.0;  // Q(n+1), Q(n+2)
     if (y < ylim && x < xlim) {
-        double const q = (1.0 - y / ylim) * sqrt(1.0 - (x / xlim) * (x / xlim));
+        double const xr = FAST ? x * (1.0 / xlim) : x / xlim;
+        double const q = (1.0 - (FAST ? y * (1.0 / ylim) : y / ylim)) * sqrt(1.0 - xr * xr);
         double const q32 = 3.2 * q;
         double const inv_2h = 0.5 * q32;  // 0.5 / h
         int const nc = 7 + (int)(23.0 * q);
         int const nu = 10 + (int)(21.0 * q);
         double const w0r = y + inv_2h, w0i = x;
         double ar = 0.0, ai = 0.0;  // A(n)
-        double hn = 0.5 * nu;       // n / 2, exact in steps of 0.5
-        for (int n = nu; n > 0; n--) {
-            if (n <= nc) {
-                ar = fma(ar, inv_2h, q1r);
-                ai = fma(ai, inv_2h, q1i);
+        // nu <= 31: q <= 1 for y >= 0 and x >= 0 inside the region
+        int const n_top = __reduce_max_sync(__activemask(), (unsigned)nu);
+        for (int n = n_top; n > 0; n--) {
+            if (n <= nu) {
+                double const hn = kHalfN[n];  // n / 2
+                if (n <= nc) {
+                    ar = fma(ar, inv_2h, q1r);
+                    ai = fma(ai, inv_2h, q1i);
+                }
+                double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
+                double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
+                q2r = q1r;
+                q2i = q1i;
+                q1r = qr;
+                q1i = qi;
             }
-            double const qr = fma(w0r, q1r, fma(-w0i, q1i, hn * q2r));
-            double const qi = fma(w0r, q1i, fma(w0i, q1r, hn * q2i));
-            q2r = q1r;
-            q2i = q1i;
-            q1r = qr;
-            q1i = qi;
-            hn -= 0.5;
         }
         // w = a_const conj(V(1)), V(1) = 0.5 A(1) / Q(1)
-        double const inv = 0.5 * a_const / fma(q1r, q1r, q1i * q1i);
+        double const q1sq = fma(q1r, q1r, q1i * q1i);
+        double const inv = FAST ? (0.5 * a_const) * rcp_fast(q1sq) : 0.5 * a_const / q1sq;
         wx = fma(ar, q1r, ai * q1i) * inv;
         wy = fma(ar, q1i, -ai * q1r) * inv;
     } else {
@@ -401,7 +440,8 @@ static __device__ __noinline__ void cerrf(double in_re, double in_im, double *w_
             q1i = qi;
         }
         // w = a_const conj(U(1)), U(1) = 0.5 Q(2) / Q(1) = 0.5 Q'(2) / (s Q'(1))
-        double const inv = 0.5 * a_const * is / fma(q1r, q1r, q1i * q1i);
+        double const q1sq = fma(q1r, q1r, q1i * q1i);
+        double const inv = FAST ? (0.5 * a_const * is) * rcp_fast(q1sq) : 0.5 * a_const * is / q1sq;
         wx = fma(q2r, q1r, q2i * q1i) * inv;
         wy = fma(q2r, q1i, -q2i * q1r) * inv;
     }
@@ -512,6 +552,10 @@ static __device__ __noinline__ PState beam_beam_4d(PState p, const uint64_t *rec
 __device__ __forceinline__ double sgn(double a) { return (double)((a >= 0) - (a < 0)); }
 
 // be_beamfields/be_beamfields.h:2232-2385 (NS(BeamBeam6D_propagate_Sigma_matrix))
+// FAST (the general branch): one reciprocal of sqrt(T) for the three
+// divisions by it outside c2t, rcp_fast for 1 / (4 cos theta) and
+// 1 / (4 sin theta).
+template <bool FAST>
 static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, double thr, double *out)
 {
     double const S11_0 = W(sg[0]), S12_0 = W(sg[1]), S13_0 = W(sg[2]), S14_0 = W(sg[3]),
@@ -568,6 +612,26 @@ static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, dou
             ds11h = 0.5 * dS_W + sgn(a) * sq;
             ds33h = 0.5 * dS_W - sgn(a) * sq;
         }
+    } else if (FAST) {
+        // c2t keeps the IEEE square root and division: for an uncoupled
+        // beam (S13 = 0) sqrt(R^2) is |R| and c2t is exactly 1, so sin theta
+        // is exactly 0 -- a product with an approximate 1 / sqrt(T) would
+        // leave it an ulp off 1 and sin theta ~1e-8 (or NaN above 1)
+        double const sqrtT = sqrt(T);
+        double const isT = rcp_fast(sqrtT);
+        c2t = signR * R / sqrtT;
+        ct = sqrt(0.5 * (1. + c2t));
+        st = signR * sgn(S13) * sqrt(0.5 * (1. - c2t));
+        s11h = 0.5 * (Wv + signR * sqrtT);
+        s33h = 0.5 * (Wv - signR * sqrtT);
+        dc2t = signR * (dS_R * isT - R * (0.5 * isT * isT * isT) * dS_T);
+        dct = 0.25 * rcp_fast(ct) * dc2t;
+        if (fabs(st) < thr)
+            dst = (S14 + S23) / R;
+        else
+            dst = -0.25 * rcp_fast(st) * dc2t;
+        ds11h = 0.5 * (dS_W + signR * 0.5 * isT * dS_T);
+        ds33h = 0.5 * (dS_W - signR * 0.5 * isT * dS_T);
     } else {
         double const sqrtT = sqrt(T);
         c2t = signR * R / sqrtT;
@@ -599,15 +663,16 @@ static __device__ __noinline__ void bb6d_sigma(const uint64_t *sg, double S, dou
 // second exponential, exp(-(x^2 + y^2) / (2 sigma^2)), is the same number as
 // the first, exp(-0.5 r2 / sigma^2) (both arguments are r2 / sigma^2 scaled
 // by -1/2 exactly), so it is evaluated once.
-// The same field and G terms from sigma^2 with two divisions and no square
-// root (the fast arithmetic policy; within a few ulp of fields_round_g).
+// The same field and G terms from sigma^2 with two reciprocals (rcp_fast)
+// and no square root (the fast arithmetic policy; within a few ulp of
+// fields_round_g).
 __device__ __forceinline__ void fields_round_g_fast(double x, double y, double sigma2, double *ex,
                                                     double *ey, double *gx, double *gy)
 {
     constexpr double k = 1.0 / (2. * kPiD * kEps0D);
-    double const inv_s2 = 1.0 / sigma2;
+    double const inv_s2 = rcp_fast(sigma2);
     double const r2 = x * x + y * y;
-    double const inv_r2 = 1.0 / r2;
+    double const inv_r2 = rcp_fast(r2);
     double const e = exp_fast(-0.5 * r2 * inv_s2);
     double const t = (r2 < 1e-20) ? k * sqrt(r2 * inv_s2) : (1 - e) * k * inv_r2;
     double const exv = t * x, eyv = t * y;
@@ -633,6 +698,60 @@ __device__ __forceinline__ void fields_round_g(double x, double y, double sigma,
     *ey = eyv;
     *gx = h * (y * eyv - x * exv + c * x * x * e);
     *gy = h * (x * exv - y * eyv + c * y * y * e);
+}
+
+// NS(get_Ex_Ey_Gx_Gy_gauss) for the fast arithmetic policy, from the
+// variances sxx = sigma_x^2 and syy = sigma_y^2 (the 6D beam-beam map has
+// them before any square root): reciprocal square roots in place of the
+// reference's thirteen divisions and three square roots, the Faddeeva
+// function's fast form, and one exponential for the field and the G terms
+// (the reference evaluates the same exponent twice).  Within a few ulp of
+// fields_gauss.
+static __device__ __noinline__ void fields_gauss_fast(double x, double y, double sxx, double syy,
+                                                      double min_sigma_diff, double *ex_p,
+                                                      double *ey_p, double *gx_p, double *gy_p)
+{
+    double const isx = rsqrt(sxx), isy = rsqrt(syy);
+    double const sx = sxx * isx, sy = syy * isy;
+    if (fabs(sx - sy) < min_sigma_diff) {
+        double const sigma = 0.5 * (sx + sy);
+        fields_round_g_fast(x, y, sigma * sigma, ex_p, ey_p, gx_p, gy_p);
+        return;
+    }
+    constexpr double kFact = 1. / (2. * kEps0D * kSqrtPiD);
+    constexpr double kG = 1. / (2 * kPiD * kEps0D);
+    double const abx = fabs(x), aby = fabs(y);
+    double const rx = abx * isx, ry = aby * isy;
+    double const e = exp_fast(-0.5 * (rx * rx + ry * ry));
+    double ex, ey, i2;
+    double wz_re, wz_im, we_re, we_im;
+    if (sxx > syy) {  // the branches on the variances: 2 (sxx - syy) keeps its sign
+        double const iS = rsqrt(2. * (sxx - syy));  // 1 / S
+        double const fact = kFact * iS;
+        cerrf<true>(abx * iS, aby * iS, &wz_re, &wz_im);
+        cerrf<true>((sy * isx) * abx * iS, (sx * isy) * aby * iS, &we_re, &we_im);
+        ex = fact * (wz_im - we_im * e);
+        ey = fact * (wz_re - we_re * e);
+        i2 = iS * iS;  // 1 / (2 (sxx - syy))
+    } else if (sxx < syy) {
+        double const iS = rsqrt(2. * (syy - sxx));
+        double const fact = kFact * iS;
+        cerrf<true>(aby * iS, abx * iS, &wz_re, &wz_im);
+        cerrf<true>((sx * isy) * aby * iS, (sy * isx) * abx * iS, &we_re, &we_im);
+        ey = fact * (wz_im - we_im * e);
+        ex = fact * (wz_re - we_re * e);
+        i2 = -(iS * iS);
+    } else {
+        ex = ey = __longlong_as_double(0x7FF0000000000000ll);  // 1/0
+        i2 = ex;
+    }
+    if (x < 0) ex = -ex;
+    if (y < 0) ey = -ey;
+    double const xe = x * ex + y * ey;
+    *ex_p = ex;
+    *ey_p = ey;
+    *gx_p = -i2 * (xe + kG * ((sy * isx) * e - 1.));
+    *gy_p = i2 * (xe + kG * ((sx * isy) * e - 1.));
 }
 
 // be_beamfields/track.h:342-507 with NS(BeamBeam6D_boost / inv_boost)
@@ -722,14 +841,17 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
             Fz = 0.5 * (Ksl * gx * ds_hat + Ksl * gy * ds_hat);
         } else {
             double sm[8];
-            bb6d_sigma(d + 6, S, thr, sm);
+            bb6d_sigma<FAST>(d + 6, S, thr, sm);
             double const ct = sm[2], st = sm[3];
             double const xbh = xb * ct + yb * st;
             double const ybh = -xb * st + yb * ct;
             double const dxbh = xb * sm[6] + yb * sm[7];
             double const dybh = -xb * sm[7] + yb * sm[6];
             double ex, ey, gx = 0.0, gy = 0.0;
-            fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
+            if (FAST)
+                fields_gauss_fast(xbh, ybh, sm[0], sm[1], msd, &ex, &ey, &gx, &gy);
+            else
+                fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
             double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
             Fx = Fxh * ct - Fyh * st;
             Fy = Fxh * st + Fyh * ct;
@@ -846,7 +968,7 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
             double const r2 = x * x + y * y;
             double const t = (r2 < 1e-20) ? sqrt(r2) * W(c[16])
                                           : (1.0 - exp_fast(-r2 * W(c[15]))) *
-                                                (1.0 / (2. * kPiD * kEps0D)) * (1.0 / r2);
+                                                (1.0 / (2. * kPiD * kEps0D)) * rcp_fast(r2);
             ex = t * x;
             ey = t * y;
         } else if (aux & (SC_ELL_X | SC_ELL_Y)) {
@@ -857,13 +979,13 @@ static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, u
             double const e = exp_fast(-(abx * abx * W(c[21])) - aby * aby * W(c[22]));
             double wz_re, wz_im, we_re, we_im;
             if (aux & SC_ELL_X) {
-                cerrf(abx * is, aby * is, &wz_re, &wz_im);
-                cerrf(W(c[19]) * abx * is, W(c[20]) * aby * is, &we_re, &we_im);
+                cerrf<true>(abx * is, aby * is, &wz_re, &wz_im);
+                cerrf<true>(W(c[19]) * abx * is, W(c[20]) * aby * is, &we_re, &we_im);
                 ex = fact * (wz_im - we_im * e);
                 ey = fact * (wz_re - we_re * e);
             } else {
-                cerrf(aby * is, abx * is, &wz_re, &wz_im);
-                cerrf(W(c[20]) * aby * is, W(c[19]) * abx * is, &we_re, &we_im);
+                cerrf<true>(aby * is, abx * is, &wz_re, &wz_im);
+                cerrf<true>(W(c[20]) * aby * is, W(c[19]) * abx * is, &we_re, &we_im);
                 ey = fact * (wz_im - we_im * e);
                 ex = fact * (wz_re - we_re * e);
             }
@@ -950,7 +1072,8 @@ static __device__ __noinline__ PState sc_interpolated(PState p, const uint64_t *
 // (state 0 on return).
 //   exact: the three derivative sums term by term in the reference's order
 //          (i, then j, then k; each term ((c x^i) y^j) z^k times the power);
-//   fast:  the sums as nested Horner forms over z, y and x with FMAs.
+//   fast:  the sums as nested Horner forms over z, y and x with FMAs, the
+//          derivative weights (2u, 3u^2) taken into the powers once.
 template <bool FAST>
 static __device__ __noinline__ PState tricub(PState p, const uint64_t *rec, uint32_t aux)
 {
@@ -976,26 +1099,33 @@ static __device__ __noinline__ PState tricub(PState p, const uint64_t *rec, uint
                        64 * (ix + (int64_t)c[18] * (iy + (int64_t)c[19] * iz));
     double kpx, kpy, kpt;
     if (FAST) {
-        double dfx = 0.0, dfy = 0.0, dfz = 0.0;
+        // derivative weights taken into the powers once: d/du of
+        // c0 + c1 u + c2 u^2 + c3 u^3 is c1 + c2 (2u) + c3 (3u^2)
+        double const z2 = 2.0 * zn, z3 = 3.0 * (zn * zn);
+        double const y2 = 2.0 * yn, y3 = 3.0 * (yn * yn);
+        double const x2 = 2.0 * xn, x3 = 3.0 * (xn * xn);
+        double dfy = 0.0, dfz = 0.0, R1 = 0.0, R2 = 0.0, R3 = 0.0;
 #pragma unroll
         for (int i = 3; i >= 0; --i) {
-            double R = 0.0, S = 0.0, T = 0.0;  // sums over j of P, j P y^-1, Q
+            double P[4], Q[4];
 #pragma unroll
-            for (int j = 3; j >= 0; --j) {
+            for (int j = 0; j < 4; ++j) {
                 double2 const a = __ldg(reinterpret_cast<const double2 *>(cf + 4 * j + 16 * i));
                 double2 const b = __ldg(reinterpret_cast<const double2 *>(cf + 4 * j + 16 * i + 2));
                 // P = sum_k c_ijk z^k, Q = dP/dz
-                double const P = fma(fma(fma(b.y, zn, b.x), zn, a.y), zn, a.x);
-                double const Q = fma(fma(3.0 * b.y, zn, 2.0 * b.x), zn, a.y);
-                if (j >= 1) S = fma(S, yn, (double)j * P);
-                R = fma(R, yn, P);
-                T = fma(T, yn, Q);
+                P[j] = fma(fma(fma(b.y, zn, b.x), zn, a.y), zn, a.x);
+                Q[j] = fma(b.y, z3, fma(b.x, z2, a.y));
             }
-            if (i >= 1) dfx = fma(dfx, xn, (double)i * R);
+            double const R = fma(fma(fma(P[3], yn, P[2]), yn, P[1]), yn, P[0]);  // sum_j P y^j
+            double const S = fma(P[3], y3, fma(P[2], y2, P[1]));                 // d/dy
+            double const T = fma(fma(fma(Q[3], yn, Q[2]), yn, Q[1]), yn, Q[0]);  // d/dz
+            if (i == 3) R3 = R;
+            if (i == 2) R2 = R;
+            if (i == 1) R1 = R;
             dfy = fma(dfy, xn, S);
             dfz = fma(dfz, xn, T);
         }
-        kpx = dfx;
+        kpx = fma(R3, x3, fma(R2, x2, R1));
         kpy = dfy;
         kpt = dfz;
     } else {

@@ -71,3 +71,10 @@ extern "C" int32_t st_engine_exp_fast(const double *x, double *y, int64_t n, voi
 {
     return stg::launch_exp_fast(x, y, n, stream);
 }
+
+// The fast arithmetic policy's reciprocal on device arrays, for checking it
+// against 1 / x.
+extern "C" int32_t st_engine_rcp_fast(const double *x, double *y, int64_t n, void *stream)
+{
+    return stg::launch_rcp_fast(x, y, n, stream);
+}

@@ -606,6 +606,24 @@ __global__ void __launch_bounds__(256) exp_fast_kernel(const double *x, double *
 }
 }  // namespace
 
+namespace {
+__global__ void __launch_bounds__(256) rcp_fast_kernel(const double *x, double *y, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = rcp_fast(x[i]);
+}
+}  // namespace
+
+int launch_rcp_fast(const double *x, double *y, int64_t n, void *stream)
+{
+    if (n <= 0) return 0;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    rcp_fast_kernel<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_exp_fast(const double *x, double *y, int64_t n, void *stream)
 {
     if (n <= 0) return 0;
