@@ -151,15 +151,37 @@ __device__ __forceinline__ void horner2(const uint64_t *bal, int n, double x, do
     pi = W(bal[2 * n + 1]);
     dr = 0.0;
     di = 0.0;
+    // a zero top-order skew coefficient (a lattice without skew components)
+    // drops the products with it from the first step of P and of P' (the
+    // forward map does the same; equal values up to the sign of an exact zero)
+    bool const real_top = (bal[2 * n + 1] << 1) == 0u;
+    int k = n - 2;
     if (n > 0) {  // first step: P' = a_n, P = a_n z + a_(n-1)
         dr = pr;
         di = pi;
-        double const npr = fma(pr, x, fma(-pi, y, W(bal[2 * n - 2])));
-        double const npi = fma(pr, y, fma(pi, x, W(bal[2 * n - 1])));
+        double npr, npi;
+        if (real_top) {
+            npr = fma(pr, x, W(bal[2 * n - 2]));
+            npi = fma(pr, y, W(bal[2 * n - 1]));
+        } else {
+            npr = fma(pr, x, fma(-pi, y, W(bal[2 * n - 2])));
+            npi = fma(pr, y, fma(pi, x, W(bal[2 * n - 1])));
+        }
         pr = npr;
         pi = npi;
+        if (real_top && k >= 0) {  // P' = a_n z + P with di = 0
+            double const ndr = fma(dr, x, pr);
+            double const ndi = fma(dr, y, pi);
+            double const npr2 = fma(pr, x, fma(-pi, y, W(bal[2 * k])));
+            double const npi2 = fma(pr, y, fma(pi, x, W(bal[2 * k + 1])));
+            dr = ndr;
+            di = ndi;
+            pr = npr2;
+            pi = npi2;
+            --k;
+        }
     }
-    for (int k = n - 2; k >= 0; --k) {
+    for (; k >= 0; --k) {
         double const ndr = fma(dr, x, fma(-di, y, pr));
         double const ndi = fma(dr, y, fma(di, x, pi));
         double const npr = fma(pr, x, fma(-pi, y, W(bal[2 * k])));

@@ -260,6 +260,14 @@ bool compile_lattice(const ImageView &img, uint64_t begin, uint64_t end,
                                  ell ? 1.0 / (2.0 * sy * sy) : 0.0})
                     p.push_back(d2w(v));
                 if (ell) aux |= (sx > sy) ? SC_ELL_X : SC_ELL_Y;
+                // the fast policy's round Gaussian kick in one factor:
+                // length N sqrt_beta / cq / (2 pi eps0), and 1 / sigma for
+                // the kick near the axis
+                if (abs_omq < 1e-6) aux |= SC_Q1;
+                p.push_back(d2w(round ? w2d(w[4]) * w2d(w[0]) * (sqrt_beta / w2d(w[9])) *
+                                            (1.0 / (2.0 * kPi * kEps0))
+                                      : 0.0));
+                p.push_back(d2w(round ? 1.0 / sigma : 0.0));
             }
             break;
         case ST_OBJECT_TYPE_SC_INTERPOLATED_PROF: {

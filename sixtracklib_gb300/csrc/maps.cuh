@@ -202,6 +202,12 @@ __device__ __forceinline__ bool inside_global(const PState &p, uint64_t xlim, ui
 }
 
 // be_multipole/track.h:38-112 (bal[2k] = knl[k]/k!, bal[2k+1] = ksl[k]/k!)
+// FAST: when the top-order skew coefficient is zero (a lattice without skew
+// components: every multipole), the first Horner step's two products with
+// it vanish and the step is two FMAs instead of four; the values are the
+// four-FMA step's (a product with +-0 added to b gives b), up to the sign of
+// an exact zero.  The test is on the record's bits (warp-uniform, integer
+// pipe).
 template <bool FAST, bool CURV>
 __device__ __forceinline__ void multipole(PState &p, const uint64_t *rec, int order)
 {
@@ -209,7 +215,14 @@ __device__ __forceinline__ void multipole(PState &p, const uint64_t *rec, int or
     double dpx = W(bal[2 * order]);
     double dpy = W(bal[2 * order + 1]);
     double const x = p.x, y = p.y, chi = p.chi;
-    for (int k = order - 1; k >= 0; --k) {
+    int k = order - 1;
+    if (FAST && k >= 0 && (bal[2 * order + 1] << 1) == 0u) {
+        double const nx = fma(dpx, x, W(bal[2 * k]));
+        dpy = fma(dpx, y, W(bal[2 * k + 1]));
+        dpx = nx;
+        --k;
+    }
+    for (; k >= 0; --k) {
         if (FAST) {
             double const tx = fma(-dpy, y, W(bal[2 * k]));
             double const ty = fma(dpy, x, W(bal[2 * k + 1]));
@@ -816,52 +829,83 @@ static __device__ __noinline__ PState beam_beam_6d(PState p, const uint64_t *rec
     double const thr = W(d[17]);
     double const msd = W(d[16]);
     double const kq = FAST ? W(d[0]) * q0 * (1. / (P0 * kClightD)) : 0.;
-    for (int i = 0; i < n_slices; ++i) {
-        double const Ksl = FAST ? W(np_[i]) * kq : W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
-        double const S = 0.5 * (sg - W(ss_[i]));
-        double const xb = x + px * S - W(xs_[i]);
-        double const yb = y + py * S - W(ys_[i]);
-        double Fx, Fy, Fz;
-        if (ROUND) {
-            const uint64_t *sgm = d + 6;  // S11 S12 S13 S14 S22 S23 S24 S33 S34 S44
-            double const S11_0 = W(sgm[0]), S12_0 = W(sgm[1]), S22_0 = W(sgm[4]);
-            double const S33_0 = W(sgm[7]), S34_0 = W(sgm[8]), S44_0 = W(sgm[9]);
-            double const S11 = S11_0 + 2. * S12_0 * S + S22_0 * S * S;
-            double const S33 = S33_0 + 2. * S34_0 * S + S44_0 * S * S;
-            double const dS_W = 2. * (S12_0 + S34_0) + 2 * S * (S22_0 + S44_0);
-            double const s_hat = 0.5 * (S11 + S33);
-            double const ds_hat = 0.5 * dS_W;
-            double ex, ey, gx, gy;
-            if (FAST)
-                fields_round_g_fast(xb, yb, s_hat, &ex, &ey, &gx, &gy);
-            else
-                fields_round_g(xb, yb, sqrt(s_hat), &ex, &ey, &gx, &gy);
-            Fx = Ksl * ex;
-            Fy = Ksl * ey;
-            Fz = 0.5 * (Ksl * gx * ds_hat + Ksl * gy * ds_hat);
-        } else {
-            double sm[8];
-            bb6d_sigma<FAST>(d + 6, S, thr, sm);
-            double const ct = sm[2], st = sm[3];
-            double const xbh = xb * ct + yb * st;
-            double const ybh = -xb * st + yb * ct;
-            double const dxbh = xb * sm[6] + yb * sm[7];
-            double const dybh = -xb * sm[7] + yb * sm[6];
-            double ex, ey, gx = 0.0, gy = 0.0;
-            if (FAST)
-                fields_gauss_fast(xbh, ybh, sm[0], sm[1], msd, &ex, &ey, &gx, &gy);
-            else
-                fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
-            double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
-            Fx = Fxh * ct - Fyh * st;
-            Fy = Fxh * st + Fyh * ct;
-            Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * sm[4] + Gyh * sm[5]);
+    if (ROUND && FAST) {
+        // the round, uncoupled slice under the fast policy: as below, with
+        // the slice's drift, Sigma terms, field and kick as FMAs, one
+        // product Ksl t for both kick components, and the longitudinal kick
+        // from the G terms' sum c e / 2 (the +-(y Ey - x Ex) terms of Gx
+        // and Gy cancel in it)
+        constexpr double k = 1.0 / (2. * kPiD * kEps0D);
+        const uint64_t *sgm = d + 6;  // S11 S12 S13 S14 S22 S23 S24 S33 S34 S44
+        double const S11_0 = W(sgm[0]), S12_0 = W(sgm[1]), S22_0 = W(sgm[4]);
+        double const S12x2 = 2. * S12_0;
+        for (int i = 0; i < n_slices; ++i) {
+            double const Ksl = W(np_[i]) * kq;
+            double const S = 0.5 * (sg - W(ss_[i]));
+            double const xb = fma(px, S, x) - W(xs_[i]);
+            double const yb = fma(py, S, y) - W(ys_[i]);
+            double const s_hat = fma(fma(S22_0, S, S12x2), S, S11_0);
+            double const ds_hat = 2. * fma(S, S22_0, S12_0);
+            double const r2 = fma(xb, xb, yb * yb);
+            double const inv_s2 = rcp_fast(s_hat);
+            double const e = exp_fast(-0.5 * r2 * inv_s2);
+            double const t = (r2 < 1e-20) ? k * sqrt(r2 * inv_s2) : (1 - e) * k * rcp_fast(r2);
+            double const kt = Ksl * t;
+            double const Fx = kt * xb, Fy = kt * yb;
+            bool const on_axis = ((uint64_t)__double_as_longlong(r2) << 1) == 0u;
+            double const Fz = on_axis ? __longlong_as_double(0x7FF8000000000000ll)
+                                      : (0.25 * k) * Ksl * ds_hat * (e * inv_s2);
+            dl = fma(0.5, fma(Fy, fma(0.5, Fy, py), Fx * fma(0.5, Fx, px)), dl + Fz);
+            x = fma(-S, Fx, x);
+            px = px + Fx;
+            y = fma(-S, Fy, y);
+            py = py + Fy;
         }
-        dl = dl + Fz + 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy));
-        x = x - S * Fx;
-        px = px + Fx;
-        y = y - S * Fy;
-        py = py + Fy;
+    } else {
+        for (int i = 0; i < n_slices; ++i) {
+            double const Ksl = FAST ? W(np_[i]) * kq : W(np_[i]) * W(d[0]) * q0 / (P0 * kClightD);
+            double const S = 0.5 * (sg - W(ss_[i]));
+            double const xb = x + px * S - W(xs_[i]);
+            double const yb = y + py * S - W(ys_[i]);
+            double Fx, Fy, Fz;
+            if (ROUND) {
+                // S11_0 = S33_0, S12_0 = S34_0, S22_0 = S44_0 bitwise (BB6D_ROUND),
+                // so the reference's S33 is S11 to the bit, 0.5 (S11 + S33) is
+                // S11, and 0.5 (2 (S12 + S34) + 2 S (S22 + S44)) is
+                // 2 (S12 + S S22) exactly (scalings by powers of two)
+                const uint64_t *sgm = d + 6;  // S11 S12 S13 S14 S22 S23 S24 S33 S34 S44
+                double const S11_0 = W(sgm[0]), S12_0 = W(sgm[1]), S22_0 = W(sgm[4]);
+                double const s_hat = S11_0 + 2. * S12_0 * S + S22_0 * S * S;
+                double const ds_hat = 2. * (S12_0 + S * S22_0);
+                double ex, ey, gx, gy;
+                fields_round_g(xb, yb, sqrt(s_hat), &ex, &ey, &gx, &gy);
+                Fx = Ksl * ex;
+                Fy = Ksl * ey;
+                Fz = 0.5 * (Ksl * gx * ds_hat + Ksl * gy * ds_hat);
+            } else {
+                double sm[8];
+                bb6d_sigma<FAST>(d + 6, S, thr, sm);
+                double const ct = sm[2], st = sm[3];
+                double const xbh = xb * ct + yb * st;
+                double const ybh = -xb * st + yb * ct;
+                double const dxbh = xb * sm[6] + yb * sm[7];
+                double const dybh = -xb * sm[7] + yb * sm[6];
+                double ex, ey, gx = 0.0, gy = 0.0;
+                if (FAST)
+                    fields_gauss_fast(xbh, ybh, sm[0], sm[1], msd, &ex, &ey, &gx, &gy);
+                else
+                    fields_gauss(xbh, ybh, sqrt(sm[0]), sqrt(sm[1]), msd, 0, &ex, &ey, &gx, &gy);
+                double const Fxh = Ksl * ex, Fyh = Ksl * ey, Gxh = Ksl * gx, Gyh = Ksl * gy;
+                Fx = Fxh * ct - Fyh * st;
+                Fy = Fxh * st + Fyh * ct;
+                Fz = 0.5 * (Fxh * dxbh + Fyh * dybh + Gxh * sm[4] + Gyh * sm[5]);
+            }
+            dl = dl + Fz + 0.5 * (Fx * (px + 0.5 * Fx) + Fy * (py + 0.5 * Fy));
+            x = x - S * Fx;
+            px = px + Fx;
+            y = y - S * Fy;
+            py = py + Fy;
+        }
     }
     {  // inverse boost
         double const pz = sqrt((1. + dl) * (1. + dl) - px * px - py * py);
@@ -933,6 +977,24 @@ template <bool FAST>
 static __device__ __noinline__ PState sc_qgauss(PState p, const uint64_t *rec, uint32_t aux)
 {
     const uint64_t *c = rec + 1;
+    if (FAST && (aux & SC_ROUND) && (aux & SC_Q1)) {
+        // round beam, Gaussian profile: the kick is g (x, y) with
+        // g = chi ... (1 - beta0 beta) / (pc0 beta) [p.sc_k]
+        //     x length N sqrt_beta / cq / (2 pi eps0) [c[23]]
+        //     x exp(-sqrt_beta^2 z^2) x (1 - exp(-r^2 / (2 sigma^2))) / r^2,
+        // one product chain and two FMAs in place of the field vector and
+        // the two kicks
+        double const z = p.zeta * p.inv_rvv;
+        double const ez = exp_fast(-(W(c[12]) * z * z));
+        double const x = p.x - W(c[5]), y = p.y - W(c[6]);
+        double const r2 = fma(x, x, y * y);
+        double const fr = (r2 < 1e-20) ? sqrt(r2) * W(c[24])
+                                       : (1.0 - exp_fast(-r2 * W(c[15]))) * rcp_fast(r2);
+        double const g = (p.sc_k * W(c[23])) * (ez * fr);
+        p.px = fma(g, x, p.px);
+        p.py = fma(g, y, p.py);
+        return p;
+    }
     double const charge = kCharge0SiD * p.q0;
     double const beta0 = p.beta0;
     double const beta = beta0 * p.rvv;

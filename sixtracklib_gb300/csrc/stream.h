@@ -37,11 +37,14 @@ enum Op : uint32_t {
                             //  0.5 / sigma^2, 1 / (2 pi eps0 sigma),
                             //  1 / S, 1 / (2 eps0 sqrt(pi) S), sigma_y / sigma_x,
                             //  sigma_x / sigma_y, 1 / (2 sigma_x^2),
-                            //  1 / (2 sigma_y^2)], S = sqrt(2 |sigma_x^2 - sigma_y^2|)
+                            //  1 / (2 sigma_y^2), length N sqrt_beta / cq /
+                            //  (2 pi eps0) and 1 / sigma (round; else 0)],
+                            //  S = sqrt(2 |sigma_x^2 - sigma_y^2|)
                             // aux bit0 (SC_ROUND): |sigma_x - sigma_y| <
                             //  min_sigma_diff, sigma = (sigma_x + sigma_y) / 2;
                             // bit1 / bit2 (SC_ELL_X / SC_ELL_Y): elliptic with
-                            //  sigma_x > sigma_y / sigma_x < sigma_y
+                            //  sigma_x > sigma_y / sigma_x < sigma_y;
+                            // bit3 (SC_Q1): |1 - q| < 1e-6 (Gaussian profile)
     OP_MONITOR = 17,        // [num_stores, start, skip, max_pid, min_pid, rolling,
                             //  turn_ordered, out_ptr, out_capacity]
     OP_NOP = 18,            // success, no effect (disabled beam-beam)
@@ -77,6 +80,7 @@ constexpr uint32_t TRICUB_MIRROR_Z = 4u;
 constexpr uint32_t SC_ROUND = 1u;
 constexpr uint32_t SC_ELL_X = 2u;
 constexpr uint32_t SC_ELL_Y = 4u;
+constexpr uint32_t SC_Q1 = 8u;
 
 // BB6D aux flag: the strong beam's Sigma matrix is round and uncoupled
 // (S11 = S33, S12 = S34, S22 = S44, S13 = S14 = S23 = S24 = 0) with
