@@ -211,13 +211,29 @@ def test_fodo_ring_10k_particles_1000_turns(torch_cuda, oracle, mode):
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
 def test_synthetic_ring_sample(torch_cuda, oracle, mode):
+    """2,048 polar-grid protons, 5 turns of the 20k ring.  Exact mode within
+    1e-12 of every column's scale.  Fast mode: the particles start at
+    zeta = 0, so the zeta column's scale is small (2.5e-4 m after a turn),
+    and the contracted drift sum moves the rounding of 1 + (xp^2 + yp^2) / 2
+    at scale 1 for a few large-amplitude particles per turn (about 2e-16 m
+    of zeta each): zeta sits at 0.76e-12 of its column after one turn and
+    0.9-1.0e-12 after five (a CPU restatement of the fast policy gives the
+    same figures, with the Horner and with the Goertzel form of the kick),
+    so it is held to 2e-12 and every other column to 1e-13."""
     lat = lattices.synthetic_ring().cbuffer.to_image()
     p = lattices.polar_grid_particles(2048, seed=5)
     exp = p.block.copy()
     oracle.track_until(lat, exp, 5)
     st, got = run_device(torch_cuda, lat, p.block, until=5, mode=mode)
     assert st == 0
-    assert_parity(got, exp, tol=1e-12)
+    if mode == "exact":
+        assert_parity(got, exp, tol=1e-12)
+        return
+    assert_parity(got, exp, tol=2e-12)
+    no_zeta = got.copy()
+    no_zeta[10] = exp[10]  # every real column but zeta
+    dev = max_col_dev(no_zeta, exp)
+    assert dev <= 1e-13, f"columns other than zeta: {dev:.3e}"
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
