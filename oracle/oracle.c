@@ -7,6 +7,16 @@
  * Every function cites the reference file:line whose arithmetic it restates;
  * the operation order inside each expression follows the reference so that
  * results are bit-identical to it (checked against oracle/_ref).
+ *
+ * Built with -DORC_FAST_POLICY=1 (oracle/liboracle_fast.so) the plain-ring
+ * maps -- drift, multipole, rotation, elliptic aperture -- instead take the
+ * CUDA engine's fast arithmetic policy: explicit fused multiply-adds, the
+ * multipole's first Horner step without the products with a zero top-order
+ * skew coefficient, and the Goertzel recurrence for multipoles of order >= 3
+ * with real coefficients; =2 keeps the Horner kick for every multipole.
+ * Those libraries measure on the CPU how far the fast policy departs from
+ * the reference (tests/test_fast_policy_cpu.py); every other map is the
+ * reference's in them as well.
  */
 #include "oracle.h"
 
@@ -244,11 +254,19 @@ static int m_drift(prec *p, double L)
     double const rpp = p->rpp;
     double const xp = p->px * rpp;
     double const yp = p->py * rpp;
+#if ORC_FAST_POLICY
+    double const u = fma(fma(yp, yp, xp * xp), 0.5, 1.0);
+    p->x = fma(xp, L, p->x);
+    p->y = fma(yp, L, p->y);
+    p->s += L;
+    p->zeta = fma(L, p->rvv - u, p->zeta);
+#else
     double const dzeta = p->rvv - (1.0 + (xp * xp + yp * yp) / 2.0);
     p->x += xp * L;
     p->y += yp * L;
     p->s += L;
     p->zeta += L * dzeta;
+#endif
     return ST_OK;
 }
 
@@ -289,6 +307,49 @@ static int m_multipole(const lattice_t *L, prec *p, const uint64_t *w)
     double dpx = bal[ix];
     double dpy = bal[iy];
     double const x = p->x, y = p->y, chi = p->chi;
+    int const curved = (hxl > 0.0) || (hyl > 0.0) || (hxl < 0.0) || (hyl < 0.0);
+#if ORC_FAST_POLICY
+    {
+        const uint64_t *bw = (const uint64_t *)bal;
+        int64_t k = order - 1;
+        int real = 0;
+        if (ORC_FAST_POLICY == 1 && order >= 3) {
+            uint64_t im = 0;
+            for (int64_t j = 0; j <= order; ++j) im |= bw[2 * j + 1];
+            real = (im << 1) == 0;
+        }
+        if (real) {
+            double const r = x + x, s = fma(x, x, y * y);
+            double c1 = dpx, c0 = fma(r, c1, bal[2 * k]);
+            for (int64_t j = order - 2; j >= 1; --j) {
+                double const cj = fma(r, c0, fma(-s, c1, bal[2 * j]));
+                c1 = c0;
+                c0 = cj;
+            }
+            dpx = fma(x, c0, fma(-s, c1, bal[0]));
+            dpy = y * c0;
+            k = -1;
+        } else if (k >= 0 && (bw[2 * order + 1] << 1) == 0) {
+            double const nx = fma(dpx, x, bal[2 * k]);
+            dpy = fma(dpx, y, bal[2 * k + 1]);
+            dpx = nx;
+            --k;
+        }
+        for (; k >= 0; --k) {
+            double const tx = fma(-dpy, y, bal[2 * k]);
+            double const ty = fma(dpy, x, bal[2 * k + 1]);
+            double const nx = fma(dpx, x, tx);
+            dpy = fma(dpx, y, ty);
+            dpx = nx;
+        }
+        if (!curved) {
+            p->px = fma(-chi, dpx, p->px);
+            p->py = fma(chi, dpy, p->py);
+            return ST_OK;
+        }
+        ix = 0;
+    }
+#endif
     while (ix > 0) {
         double const zre = dpx * x - dpy * y;
         double const zim = dpx * y + dpy * x;
@@ -299,7 +360,7 @@ static int m_multipole(const lattice_t *L, prec *p, const uint64_t *w)
     }
     dpx = -chi * dpx;
     dpy = chi * dpy;
-    if ((hxl > 0.0) || (hyl > 0.0) || (hxl < 0.0) || (hyl < 0.0)) {
+    if (curved) {
         double const delta = p->delta;
         double const hxlx = x * hxl;
         double const hyly = y * hyl;
@@ -346,10 +407,17 @@ static int m_srotation(prec *p, const double *c)
 {
     double const cz = c[0], sz = c[1];
     double const x = p->x, y = p->y, px = p->px, py = p->py;
+#if ORC_FAST_POLICY
+    double const xh = fma(cz, x, sz * y);
+    double const yh = fma(-sz, x, cz * y);
+    double const pxh = fma(cz, px, sz * py);
+    double const pyh = fma(-sz, px, cz * py);
+#else
     double const xh = cz * x + sz * y;
     double const yh = -sz * x + cz * y;
     double const pxh = cz * px + sz * py;
     double const pyh = -sz * px + cz * py;
+#endif
     p->x = xh;
     p->y = yh;
     p->px = pxh;
@@ -370,6 +438,9 @@ static int m_limit_rect(prec *p, const double *c)
 /* be_limit/track.h:113-137 */
 static int m_limit_ellipse(prec *p, const double *c)
 {
+#if ORC_FAST_POLICY
+    double const t = fma(p->y * p->y, c[0], (p->x * p->x) * c[1]);
+#else
     double t = p->x;
     double ys = p->y;
     t *= t;
@@ -377,6 +448,7 @@ static int m_limit_ellipse(prec *p, const double *c)
     ys *= ys;
     ys *= c[0];
     t += ys;
+#endif
     p->state &= (int64_t)(t <= c[2]);
     return ST_OK;
 }

@@ -7,7 +7,12 @@ bench.py's CPU-baseline leg, never by the product package.
   compiling it first if needed;
 * ``Oracle.reference()`` loads oracle/_ref/libstref.so, the reference's own
   tracking code built by oracle/build_ref.sh (only where the reference
-  sources exist; None otherwise).
+  sources exist; None otherwise);
+* ``Oracle.fast_policy(goertzel)`` loads oracle.c built with the CUDA
+  engine's fast arithmetic in the plain-ring maps (``ORC_FAST_POLICY``),
+  with the Goertzel kick for real-coefficient multipoles or with the Horner
+  kick only: it measures on the CPU how far that policy departs from the
+  reference.
 
 Both expose identical calls on a CObjects lattice image (bytes / u64 array)
 and a particle column block (21 x n u64 array, edited in place).
@@ -36,16 +41,31 @@ CFLAGS = ["-O2", "-fPIC", "-shared", "-std=gnu99", "-fno-fast-math",
           "-ffp-contract=off", "-fopenmp"]
 
 
+FAST_LIBS = {True: os.path.join(HERE, "liboracle_fast.so"),
+             False: os.path.join(HERE, "liboracle_fast_horner.so")}
+
+
+def _compile(lib: str, defines, force: bool) -> str:
+    src = os.path.join(HERE, "oracle.c")
+    newest = max(os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "oracle.h")))
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= newest:
+        return lib
+    tmp = lib + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", *CFLAGS, *defines, src, "-o", tmp, "-lm"])
+    os.replace(tmp, lib)
+    return lib
+
+
 def build_oracle(force: bool = False) -> str:
     """Compile oracle.c into oracle/liboracle.so (gcc, no FMA contraction)."""
-    src = os.path.join(HERE, "oracle.c")
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
-        return LIB
-    tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", *CFLAGS, src, "-o", tmp, "-lm"])
-    os.replace(tmp, LIB)
-    return LIB
+    return _compile(LIB, [], force)
+
+
+def build_fast_policy(goertzel: bool = True, force: bool = False) -> str:
+    """Compile oracle.c with the engine's fast arithmetic in the plain-ring
+    maps (ORC_FAST_POLICY=1: Goertzel kick for real coefficients, 2: Horner
+    kick only)."""
+    return _compile(FAST_LIBS[goertzel], [f"-DORC_FAST_POLICY={1 if goertzel else 2}"], force)
 
 
 def build_reference(ref_root: str | None = None) -> str | None:
@@ -125,6 +145,11 @@ class Oracle:
         if prefix == "orc_":
             self.lib.orc_set_aperture_mode.argtypes = [C.c_int, C.c_double,
                                                        C.c_double, C.c_double]
+
+    @classmethod
+    def fast_policy(cls, goertzel: bool = True):
+        """The oracle with the engine's fast arithmetic in the plain-ring maps."""
+        return cls(path=build_fast_policy(goertzel))
 
     @classmethod
     def reference(cls, omp: bool = False, flags: str | None = None):

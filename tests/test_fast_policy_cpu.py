@@ -1,0 +1,82 @@
+"""The fast arithmetic policy restated on the CPU (oracle.c built with
+ORC_FAST_POLICY): how far it departs from the reference, measured without a
+GPU.  The plain-ring maps take the engine's fast forms -- explicit FMAs, the
+multipole's first Horner step without the zero skew products, the Goertzel
+recurrence for real-coefficient multipoles of order >= 3 (or, in the second
+build, the Horner kick throughout); `tests/test_gpu_parity.py` compares the
+GPU's fast mode with this restatement."""
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from sixtracklib_gb300 import lattices
+from sixtracklib_gb300.beam_elements import Elements
+
+from .test_gpu_parity import max_col_dev
+
+
+@pytest.fixture(scope="module")
+def oracles():
+    return Oracle(), Oracle.fast_policy(goertzel=True), Oracle.fast_policy(goertzel=False)
+
+
+def _kick_devs(ref, fast, n_lat=400, n_part=512, seed=3):
+    """Relative deviation of the px / py kicks of single real-coefficient
+    multipoles (orders 3-10, the benchmark ring's coefficient scales) from
+    the reference's Horner kick."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_lat):
+        order = int(rng.integers(3, 11))
+        knl = np.zeros(order + 1)
+        knl[1] = rng.choice([-1, 1]) * rng.uniform(0.01, 0.05)
+        for n in range(2, order + 1):
+            knl[n] = rng.normal(0.0, 1e-4 * 10.0 ** (-n))
+        e = Elements()
+        e.Multipole(knl=list(knl))
+        img = e.cbuffer.to_image()
+        p = lattices.gaussian_particles(n_part, seed=int(rng.integers(1 << 30)), sx=5e-3, sy=5e-3)
+        a, b = p.block.copy(), p.block.copy()
+        ref.track_line(img, a, 0, 1, False)
+        fast.track_line(img, b, 0, 1, False)
+        k0 = p.block[8:10].view(np.float64)
+        ka = a[8:10].view(np.float64) - k0
+        kb = b[8:10].view(np.float64) - k0
+        out.append(np.abs(kb - ka) / np.maximum(np.abs(ka), 1e-300))
+    return np.concatenate(out, axis=1)
+
+
+def test_goertzel_kick_rounds_like_the_horner_kick(oracles):
+    """Per-component deviation of the kick from the reference's Horner: the
+    Goertzel form's distribution matches the FMA Horner's."""
+    ref, goertzel, horner = oracles
+    dg, dh = _kick_devs(ref, goertzel), _kick_devs(ref, horner)
+    rg, rh = float(np.sqrt(np.mean(dg ** 2))), float(np.sqrt(np.mean(dh ** 2)))
+    print(f"kick deviation rms: Goertzel {rg:.3e}, FMA Horner {rh:.3e}; "
+          f"max {dg.max():.2e} / {dh.max():.2e}")
+    assert dg.max() < 2e-14 and dh.max() < 2e-14
+    assert rg < 1.5 * rh
+
+
+@pytest.mark.parametrize("goertzel", [True, False])
+def test_fast_policy_on_the_20k_ring(oracles, goertzel):
+    """2,048 polar-grid protons on the 20k ring: identical losses and
+    counters; x, y, px, py and the energy columns within 1e-13 of their
+    column scale after 1 and 5 turns; zeta -- whose column starts at zero --
+    within 1e-12 after one turn and 2e-12 after five."""
+    ref, fast = oracles[0], oracles[1 if goertzel else 2]
+    lat = lattices.synthetic_ring().cbuffer.to_image()
+    p = lattices.polar_grid_particles(2048, seed=5)
+    for turns, zeta_tol in ((1, 1e-12), (5, 2e-12)):
+        exp, got = p.block.copy(), p.block.copy()
+        assert ref.track_until(lat, exp, turns) == 0
+        assert fast.track_until(lat, got, turns) == 0
+        assert np.array_equal(got[17:], exp[17:])
+        no_zeta = got.copy()
+        no_zeta[10] = exp[10]
+        dev, dz = max_col_dev(no_zeta, exp), max_col_dev(got, exp)
+        print(f"{'Goertzel' if goertzel else 'Horner'} {turns} turns: zeta {dz:.2e}, "
+              f"other columns {dev:.2e}")
+        assert dev <= 1e-13
+        assert dz <= zeta_tol

@@ -219,7 +219,8 @@ def test_synthetic_ring_sample(torch_cuda, oracle, mode):
     of zeta each): zeta sits at 0.76e-12 of its column after one turn and
     0.9-1.0e-12 after five (a CPU restatement of the fast policy gives the
     same figures, with the Horner and with the Goertzel form of the kick),
-    so it is held to 2e-12 and every other column to 1e-13."""
+    so it is held to 2e-12 and every other column to 1e-13
+    (`tests/test_fast_policy_cpu.py` measures the same on the CPU)."""
     lat = lattices.synthetic_ring().cbuffer.to_image()
     p = lattices.polar_grid_particles(2048, seed=5)
     exp = p.block.copy()
@@ -234,6 +235,23 @@ def test_synthetic_ring_sample(torch_cuda, oracle, mode):
     no_zeta[10] = exp[10]  # every real column but zeta
     dev = max_col_dev(no_zeta, exp)
     assert dev <= 1e-13, f"columns other than zeta: {dev:.3e}"
+
+
+def test_fast_mode_equals_its_cpu_restatement(torch_cuda):
+    """The GPU's fast policy and its CPU restatement (oracle.c with
+    ORC_FAST_POLICY=1: the same FMAs, zero-skew first Horner step and
+    Goertzel kick) agree bit for bit on the 20k ring without its cavities
+    (whose sin() is CUDA's on one side and the host libm's on the other):
+    2,048 polar-grid protons, 5 turns, losses included, every column."""
+    from oracle.pyoracle import Oracle
+
+    lat = lattices.synthetic_ring(n_cav=0).cbuffer.to_image()
+    p = lattices.polar_grid_particles(2048, seed=5)
+    exp = p.block.copy()
+    assert Oracle.fast_policy(goertzel=True).track_until(lat, exp, 5) == 0
+    st, got = run_device(torch_cuda, lat, p.block, until=5, mode="fast")
+    assert st == 0
+    assert_parity(got, exp, 0.0, bit_exact=True)
 
 
 @pytest.mark.parametrize("mode", ["exact", "fast"])
