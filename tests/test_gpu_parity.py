@@ -60,6 +60,21 @@ def max_col_dev(got, exp):
     return float(np.nanmax(d)) if d.size else 0.0
 
 
+def assert_fast_parity(got, exp, tol, zeta_tol):
+    """The fast policy on polar-grid samples, whose particles start at
+    zeta = 0: zeta within `zeta_tol` of its (small) column scale, every
+    other column within `tol`.  The contracted drift sum and the kick's
+    forms move the rounding of 1 + (xp^2 + yp^2) / 2 at scale 1 for a few
+    large-amplitude particles per turn, about 2e-16 m of zeta each, 1e-12 of
+    a zeta column that spans 2.5e-4 m (tests/test_fast_policy_cpu.py
+    measures the same on the CPU)."""
+    assert_parity(got, exp, tol=zeta_tol)
+    no_zeta = got.copy()
+    no_zeta[10] = exp[10]
+    dev = max_col_dev(no_zeta, exp)
+    assert dev <= tol, f"columns other than zeta: {dev:.3e}"
+
+
 def assert_parity(got, exp, tol, bit_exact=False):
     assert np.array_equal(got[17:], exp[17:]), "particle ids / at_element / at_turn / state differ"
     if bit_exact:
@@ -229,12 +244,8 @@ def test_synthetic_ring_sample(torch_cuda, oracle, mode):
     assert st == 0
     if mode == "exact":
         assert_parity(got, exp, tol=1e-12)
-        return
-    assert_parity(got, exp, tol=2e-12)
-    no_zeta = got.copy()
-    no_zeta[10] = exp[10]  # every real column but zeta
-    dev = max_col_dev(no_zeta, exp)
-    assert dev <= 1e-13, f"columns other than zeta: {dev:.3e}"
+    else:
+        assert_fast_parity(got, exp, tol=1e-13, zeta_tol=2e-12)
 
 
 def test_fast_mode_equals_its_cpu_restatement(torch_cuda):
@@ -468,7 +479,9 @@ def test_full_size_config_properties(torch_cuda, oracle):
     """1M particles on the 20k-element ring (the benchmark workload):
     (a) 2 turns in one call == 2 calls of 1 turn, bit for bit;
     (b) the result of a particle does not depend on its slot;
-    (c) a strided sample of 1024 particles agrees with the oracle."""
+    (c) a strided sample of 1024 particles agrees with the oracle (zeta,
+    whose column starts at zero on the polar grid, within 2e-12 of its
+    scale, every other column within 1e-13: assert_fast_parity)."""
     torch = torch_cuda
     from sixtracklib_gb300.device import DeviceTracker
 
@@ -490,7 +503,7 @@ def test_full_size_config_properties(torch_cuda, oracle):
     sample = p.block[:, idx].copy()
     oracle.track_until(e.cbuffer.to_image(), sample, 2)
     got = a.cpu().numpy().view(np.uint64)[:, idx]
-    assert_parity(got, sample, tol=1e-12)
+    assert_fast_parity(got, sample, tol=1e-13, zeta_tol=2e-12)
 
 
 def test_trackjob_until_line_collect(torch_cuda, oracle):
