@@ -302,3 +302,73 @@ def test_elem_by_elem_config_matches_the_oracle(lib):
                         C.byref(cfg), pid, elem, turn)
                     assert got == orc.ebe_store_index(ocfg, pid, elem, turn), \
                         (order, rolling, pid, elem, turn)
+
+
+def test_jobs_and_single_particle_calls_fail_loudly_without_a_gpu(lib):
+    """No CPU fallback for jobs either: every TrackJob / TrackJobNew /
+    CudaTrackJob constructor returns NULL on a machine without a GPU and
+    names the reason; the reference's other architectures are refused by
+    name; the single-particle tracking calls fail and leave the particle as
+    it was; the CUDA node list is empty."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = lib
+    e = Elements()
+    e.Drift(length=1.0)
+    img = e.cbuffer.to_image()
+    from sixtracklib_gb300 import ParticlesSet, lattices
+
+    ps = ParticlesSet()
+    ps.Particles(num_particles=2).set_block(lattices.gaussian_particles(2).block)
+    pimg = ps.cbuffer.to_image()
+    eb = capi.c_buffer_from_image(img)
+    pb = capi.c_buffer_from_image(pimg)
+    cs = C.c_char_p
+    try:
+        calls = [
+            ("st_TrackJob_create", [cs, cs], (b"cuda", b"")),
+            ("st_TrackJob_new", [cs, VP, VP, cs], (b"cuda", pb, eb, b"")),
+            ("st_TrackJob_new_with_output", [cs, VP, VP, VP, U64, cs], (b"cuda", pb, eb, None, 0, b"")),
+            ("st_TrackJobNew_create", [cs, cs], (b"cuda", b"")),
+            ("st_CudaTrackJob_create", [], ()),
+            ("st_CudaTrackJob_new_from_config_str", [cs], (b"mode=fast",)),
+            ("st_CudaTrackJob_new", [cs, VP, VP], (b"0.0", pb, eb)),
+            ("st_CudaTrackJob_new_with_output", [cs, VP, VP, VP, U64], (b"0.0", pb, eb, None, 0)),
+            ("st_CudaTrackJob_new_detailed", [cs, VP, U64, VP, VP, VP, U64, cs],
+             (b"0.0", pb, 0, None, eb, None, 0, b"")),
+        ]
+        for name, args, vals in calls:
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = VP
+            assert not fn(*vals), name
+            err = _native.last_error()
+            assert "GPU" in err or "CUDA" in err or "device" in err, (name, err)
+        L.st_TrackJob_create.argtypes = [cs, cs]
+        L.st_TrackJob_create.restype = VP
+        for arch in (b"cpu", b"opencl"):
+            assert not L.st_TrackJob_create(arch, b"")
+            assert "architecture" in _native.last_error()
+        fn = L.st_CudaTrackJob_get_available_node_indices_list
+        fn.argtypes = [U64, VP]
+        fn.restype = U64
+        out = (C.c_int64 * 4)(-7, -7, -7, -7)
+        assert fn(4, out) == 0 and list(out) == [-7] * 4
+        # single-particle free functions (track.h:86-132)
+        q = lattices.gaussian_particles(3)
+        blk = q.block.copy()
+        sp = capi.particles_view(blk)
+        L.st_Track_particle_line.argtypes = [VP, I64, VP, U64, U64, C.c_bool]
+        L.st_Track_particle_line.restype = C.c_int32
+        assert L.st_Track_particle_line(C.byref(sp), 1, eb, 0, 1, True) == -1
+        cfg = capi.StElemByElemConfig()
+        assert L.st_ElemByElemConfig_init_detailed(C.byref(cfg), 0, 0, 2, 0, 0, 0, 0, False) == 0
+        fn = L.st_Track_particle_element_by_element_until_turn
+        fn.argtypes = [VP, I64, VP, VP, I64]
+        fn.restype = C.c_int32
+        assert fn(C.byref(sp), 1, C.byref(cfg), eb, 1) == -1
+        assert np.array_equal(blk, q.block)
+    finally:
+        L.st_Buffer_delete(eb)
+        L.st_Buffer_delete(pb)
