@@ -90,3 +90,34 @@ def test_fast_policy_on_the_20k_ring(oracles, goertzel):
               f"other columns {dev:.2e}")
         assert dev <= 1e-13
         assert dz <= zeta_tol
+
+
+@pytest.mark.parametrize("amp", [1e-3, 0.1, 0.99])
+@pytest.mark.parametrize("order", [3, 10, 40])
+def test_goertzel_kick_at_large_amplitudes_and_orders(oracles, amp, order):
+    """The Goertzel form keeps its accuracy where the high orders matter:
+    coefficients b_n ~ 10^-n (not 10^-n / n!), coordinates up to the global
+    aperture (1 m), orders up to 40; every kick within 1e-15 of the
+    sample's largest, as the FMA Horner form's."""
+    ref, goertzel, horner = oracles
+    rng = np.random.default_rng(order * 100 + int(amp * 1000))
+    for trial in range(5):
+        knl = np.zeros(order + 1)
+        knl[1] = 0.03
+        for n in range(2, order + 1):
+            knl[n] = rng.normal(0.0, 1.0) * 10.0 ** (-n)
+        e = Elements()
+        e.Multipole(knl=list(knl))
+        img = e.cbuffer.to_image()
+        blk = lattices.gaussian_particles(256, seed=trial, sx=amp, sy=amp).block
+        blk[15] = np.full(256, 0.5).view(np.uint64)  # chi
+        a, b, c = blk.copy(), blk.copy(), blk.copy()
+        ref.track_line(img, a, 0, 1, False)
+        goertzel.track_line(img, b, 0, 1, False)
+        horner.track_line(img, c, 0, 1, False)
+        k0 = blk[8:10].view(np.float64)
+        ka = a[8:10].view(np.float64) - k0
+        scale = np.max(np.abs(ka), axis=1, keepdims=True)
+        for other in (b, c):
+            kick = other[8:10].view(np.float64) - k0
+            assert np.max(np.abs(kick - ka) / scale) < 1e-15
