@@ -372,3 +372,50 @@ def test_jobs_and_single_particle_calls_fail_loudly_without_a_gpu(lib):
     finally:
         L.st_Buffer_delete(eb)
         L.st_Buffer_delete(pb)
+
+
+def test_every_job_call_is_null_safe(lib):
+    """A NULL job is an error, not a crash (internal/track_job.cpp:417-445):
+    every TrackJob / TrackJobNew / CudaTrackJob call the header declares,
+    given NULL for the job and zeros for the rest, returns -1 where it
+    returns a status and 0 / false / NULL from the getters (an empty string
+    for the string getters)."""
+    import re
+
+    import os
+
+    header = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                          "include", "sixtracklib_gb300.h")
+    with open(header) as f:
+        hdr = f.read()
+    decls = re.findall(r"^([A-Za-z_][A-Za-z0-9_ \*]*?)\b(st_(?:TrackJob|TrackJobNew|CudaTrackJob)"
+                       r"_[A-Za-z0-9_]+)\s*\(([^;]*?)\);", hdr, re.M | re.S)
+    called = 0
+    for ret, name, args in decls:
+        args = [a.strip() for a in " ".join(args.split()).split(",")]
+        if not args or args == ["void"] or "TrackJob" not in args[0]:
+            continue
+        ret = " ".join(ret.split())
+        fn = getattr(lib, name)
+        fn.argtypes = [C.c_void_p] * len(args)
+        if ret == "void":
+            fn.restype = None
+        elif ret in ("st_track_status_t", "int32_t"):
+            fn.restype = C.c_int32
+        elif ret == "const char *":
+            fn.restype = C.c_char_p
+        elif ret == "bool":
+            fn.restype = C.c_bool
+        else:
+            fn.restype = C.c_uint64
+        r = fn(*([None] * len(args)))
+        called += 1
+        if ret in ("st_track_status_t", "int32_t"):
+            assert r == -1, name
+        elif ret == "const char *":
+            assert r == b"", name
+        elif ret == "bool":
+            assert r is False, name
+        elif ret.endswith("*"):
+            assert r in (0, None), name
+    assert called > 100
