@@ -19,7 +19,17 @@ D, I64, U64, VP, B = C.c_double, C.c_int64, C.c_uint64, C.c_void_p, C.c_bool
 
 @pytest.fixture(scope="module")
 def lib():
-    L = _native.load()
+    _native.load()
+    L = C.CDLL(_native.lib_path())  # own prototypes, not the shared handle's
+    for name, args, res in (("st_Buffer_new", [U64], VP), ("st_Buffer_delete", [VP], None),
+                            ("st_Buffer_get_size", [VP], U64),
+                            ("st_Buffer_get_const_data_begin", [VP], VP),
+                            ("st_Buffer_get_num_of_objects", [VP], U64),
+                            ("st_Buffer_get_const_object", [VP, U64], VP),
+                            ("st_Particles_new", [VP, U64], VP)):
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
     sigs = {
         "st_Drift_new": [VP], "st_Drift_add": [VP, D],
         "st_DriftExact_new": [VP], "st_DriftExact_add": [VP, D],
@@ -388,6 +398,9 @@ def test_every_job_call_is_null_safe(lib):
                           "include", "sixtracklib_gb300.h")
     with open(header) as f:
         hdr = f.read()
+    # a handle of its own: the prototypes set below must not leak into the
+    # shared one the other tests use
+    lib = C.CDLL(_native.lib_path())
     decls = re.findall(r"^([A-Za-z_][A-Za-z0-9_ \*]*?)\b(st_(?:TrackJob|TrackJobNew|CudaTrackJob)"
                        r"_[A-Za-z0-9_]+)\s*\(([^;]*?)\);", hdr, re.M | re.S)
     called = 0

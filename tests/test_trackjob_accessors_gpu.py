@@ -23,8 +23,11 @@ def L():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.fail("GPU tests need a CUDA device")
-    L = _native.load()
+    _native.load()
+    L = C.CDLL(_native.lib_path())  # own prototypes, not the shared handle's
     sigs = [
+        ("st_Buffer_new_on_data", [VP, U64], VP), ("st_Buffer_delete", [VP], None),
+        ("st_Buffer_get_num_of_objects", [VP], U64),
         ("st_TrackJob_new_detailed", [C.c_char_p, VP, U64, VP, VP, VP, U64, C.c_char_p], VP),
         ("st_TrackJob_delete", [VP], None), ("st_TrackJob_clear", [VP], None),
         ("st_TrackJob_reset", [VP, VP, VP, VP], B),
