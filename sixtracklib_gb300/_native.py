@@ -75,6 +75,18 @@ _SIGNATURES = {
     "st_TrackJob_has_output_buffer": ([vp], cbool),
     "st_TrackJob_owns_output_buffer": ([vp], cbool),
     "st_TrackJob_is_collecting_particles": ([vp], cbool),
+    "st_TrackJob_is_collecting_beam_elements": ([vp], cbool),
+    "st_TrackJob_is_collecting_output": ([vp], cbool),
+    "st_TrackJob_get_collect_flags": ([vp], C.c_uint16),
+    "st_TrackJob_has_config_str": ([vp], cbool),
+    "st_TrackJob_has_elem_by_elem_config": ([vp], cbool),
+    "st_TrackJob_has_beam_monitors": ([vp], cbool),
+    "st_TrackJob_get_num_elem_by_elem_turns": ([vp], u64),
+    "st_TrackJobNew_is_in_debug_mode": ([vp], cbool),
+    "st_TrackJobNew_enable_debug_mode": ([vp], i32),
+    "st_TrackJobNew_disable_debug_mode": ([vp], i32),
+    "st_TrackJobNew_collect_debug_flag": ([vp], i32),
+    "st_TrackJobNew_get_debug_register": ([vp], u64),
     "st_TrackJob_can_fetch_particles_addr": ([vp], cbool),
     "st_TrackJob_has_particles_addr": ([vp], cbool),
     "st_TrackJob_fetch_particle_addresses": ([vp], i32),

@@ -14,6 +14,7 @@ buffer in place, ``collect_output`` refreshes :attr:`output`.
 from __future__ import annotations
 
 import ctypes as C
+import warnings
 
 import numpy as np
 
@@ -136,9 +137,34 @@ class TrackJob:
 
     @property
     def is_in_debug_mode(self):
-        """The engine has no debug mode (kernel-side status words are always
-        read back)."""
-        return False
+        """Debug mode (track/track_job_base.h:182-189): every tracking call
+        first validates its inputs and records the outcome in the debug
+        register."""
+        return bool(self._lib.st_TrackJobNew_is_in_debug_mode(self.ptr_st_track_job))
+
+    def _status(self, st, what):
+        """raise_error_if_status_not_success (control.py:181-189)."""
+        self._last_status = int(st)
+        if st != 0:
+            raise RuntimeError(f"unsuccessful {what} op; status:{st}")
+        return self
+
+    def enable_debug_mode(self):
+        return self._status(self._lib.st_TrackJobNew_enable_debug_mode(self.ptr_st_track_job),
+                            "enable debug mode")
+
+    def disable_debug_mode(self):
+        return self._status(self._lib.st_TrackJobNew_disable_debug_mode(self.ptr_st_track_job),
+                            "disable debug mode")
+
+    def collect_debug_flag(self):
+        """Reads the debug register back (fails outside debug mode)."""
+        return self._status(self._lib.st_TrackJobNew_collect_debug_flag(self.ptr_st_track_job),
+                            "debug flag collection")
+
+    @property
+    def debug_register(self):
+        return int(self._lib.st_TrackJobNew_get_debug_register(self.ptr_st_track_job))
 
     @property
     def is_collecting_particles(self):
@@ -251,6 +277,78 @@ class TrackJob:
     @property
     def requires_collecting(self):
         return True
+
+    # --------------- TrackJobBaseNew names (python/sixtracklib/trackjob.py)
+    @property
+    def pointer(self):
+        return self.ptr_st_track_job
+
+    @property
+    def total_num_particles(self):
+        return int(self._lib.st_TrackJob_get_total_num_particles_in_sets(self.ptr_st_track_job))
+
+    @property
+    def collecting_flags(self):
+        return int(self._lib.st_TrackJob_get_collect_flags(self.ptr_st_track_job))
+
+    @property
+    def is_collecting_beam_elements(self):
+        return bool(self._lib.st_TrackJob_is_collecting_beam_elements(self.ptr_st_track_job))
+
+    @property
+    def is_collecting_output(self):
+        return bool(self._lib.st_TrackJob_is_collecting_output(self.ptr_st_track_job))
+
+    @property
+    def has_config_str(self):
+        return bool(self._lib.st_TrackJob_has_config_str(self.ptr_st_track_job))
+
+    @property
+    def has_elem_by_elem_config(self):
+        return bool(self._lib.st_TrackJob_has_elem_by_elem_config(self.ptr_st_track_job))
+
+    @property
+    def has_beam_monitors(self):
+        return bool(self._lib.st_TrackJob_has_beam_monitors(self.ptr_st_track_job))
+
+    @property
+    def num_elem_by_elem_turn(self):
+        """The number of turns the elem-by-elem output stores (the reference's
+        property returns the output's buffer offset under this name)."""
+        return int(self._lib.st_TrackJob_get_num_elem_by_elem_turns(self.ptr_st_track_job))
+
+    elem_by_elem_output_buffer_offset = property(lambda self: self.elem_by_elem_output_offset)
+    beam_monitor_output_buffer_offset = property(lambda self: self.beam_monitor_output_offset)
+    # the job keeps its device data as the reference's CUDA job keeps its
+    # arguments, bound to its node as the reference's controller is
+    uses_arguments = property(lambda self: self.ptr_st_track_job is not None)
+    uses_controller = property(lambda self: self.ptr_st_track_job is not None)
+
+    def collect_particle_addresses(self):
+        """The device addresses of the particle sets (the reference collects
+        them from its device argument; here they are formed on the host)."""
+        return self.fetch_particle_addresses()
+
+    # deprecated spellings of the reference (DeprecationWarning, then the call)
+    def _deprecated(self, old, new):
+        warnings.warn(f"{old}() is deprecated; use {new}() instead", DeprecationWarning,
+                      stacklevel=3)
+        return getattr(self, new)()
+
+    def collectParticles(self):  # noqa: N802
+        return self._deprecated("collectParticles", "collect_particles")
+
+    def collectBeamElements(self):  # noqa: N802
+        return self._deprecated("collectBeamElements", "collect_beam_elements")
+
+    def collectOutput(self):  # noqa: N802
+        return self._deprecated("collectOutput", "collect_output")
+
+    def collectDebugFlag(self):  # noqa: N802
+        return self._deprecated("collectDebugFlag", "collect_debug_flag")
+
+    def collectParticlesAddresses(self):  # noqa: N802
+        return self._deprecated("collectParticlesAddresses", "collect_particle_addresses")
 
     # ------------------------------------------------------------ tracking
     def _check(self, st, what):

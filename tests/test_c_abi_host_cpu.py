@@ -432,3 +432,44 @@ def test_every_job_call_is_null_safe(lib):
         elif ret.endswith("*"):
             assert r in (0, None), name
     assert called > 100
+
+
+def test_python_job_names_of_the_reference_over_a_null_job():
+    """The Python job's TrackJobBaseNew names (debug mode, collect flags,
+    output offsets, deprecated camelCase spellings; trackjob.py:150-1210)
+    reach the C ABI; on a NULL job they answer as a NULL job does: status
+    operations raise, getters are empty."""
+    import warnings as w
+
+    from sixtracklib_gb300 import CBuffer
+    from sixtracklib_gb300.trackjob import CudaTrackJob
+
+    job = object.__new__(CudaTrackJob)
+    job._lib = _native.load()
+    job.ptr_st_track_job = None
+    job._pset_indices = []
+    job._last_status = 0
+    job._particles_buffer = CBuffer()
+    job._stored = {}
+    assert job.is_in_debug_mode is False and job.debug_register == 0
+    for op in (job.enable_debug_mode, job.disable_debug_mode, job.collect_debug_flag,
+               job.collect_particle_addresses):
+        with pytest.raises(RuntimeError):
+            op()
+    assert job.last_status == -1
+    assert job.pointer is None and job.total_num_particles == 0 and job.collecting_flags == 0
+    assert not (job.is_collecting_beam_elements or job.is_collecting_output or
+                job.has_config_str or job.has_elem_by_elem_config or job.has_beam_monitors)
+    assert job.num_elem_by_elem_turn == 0
+    assert job.elem_by_elem_output_buffer_offset == job.beam_monitor_output_buffer_offset == 0
+    assert not job.uses_arguments and not job.uses_controller
+    with w.catch_warnings(record=True) as caught:
+        w.simplefilter("always")
+        assert job.collectOutput() is job
+        assert job.collectParticles() is job
+        with pytest.raises(RuntimeError):
+            job.collectDebugFlag()
+        with pytest.raises(RuntimeError):
+            job.collectParticlesAddresses()
+    assert sum(issubclass(c.category, DeprecationWarning) for c in caught) == 4
+    job.ptr_st_track_job = None  # __del__ has nothing to release
