@@ -313,6 +313,115 @@ int64_t st_ElemByElemConfig_get_particles_store_index_details(
     int64_t at_turn);
 int64_t st_ElemByElemConfig_get_stored_num_particles(const st_ElemByElemConfig *config);
 
+/* ------------------------------------------------------ output buffer */
+/* Host-side planning of the tracking output (output/output_buffer.h:42-260,
+ * be_monitor/output_buffer.h:20-135, output/elem_by_elem_output_buffer.h,
+ * output/elem_by_elem_config.c:366-375).  The particle-id / element-id /
+ * turn ranges come from the particles (ids by magnitude) and from the
+ * lattice's beam elements; the output holds the elem-by-elem Particles block
+ * first (when until_turn_elem_by_elem exceeds the first turn), then one
+ * block of (max_id - min_id + 1) * num_stores particles per beam monitor
+ * that starts at or after the first turn.  Flags: 0x01 elem-by-elem,
+ * 0x02 beam monitors.  Status 0 on success, -1 otherwise; slot_size must
+ * be 8.  With particle ids >= 0 and a lattice of beam elements only, a
+ * TrackJob's output buffer has this layout too. */
+bool st_OutputBuffer_requires_output_buffer_ext(uint32_t flags);
+bool st_OutputBuffer_requires_elem_by_elem_output_ext(uint32_t flags);
+bool st_OutputBuffer_requires_beam_monitor_output_ext(uint32_t flags);
+uint32_t st_OutputBuffer_required_for_tracking(const st_Particles *particles,
+                                               const st_Buffer *beam_elements,
+                                               st_buffer_size_t until_turn_elem_by_elem);
+uint32_t st_OutputBuffer_required_for_tracking_of_particle_sets(
+    const st_Buffer *particles_buffer, st_buffer_size_t num_particle_sets,
+    const st_buffer_size_t *particle_set_indices, const st_Buffer *beam_elements,
+    st_buffer_size_t until_turn_elem_by_elem);
+uint32_t st_OutputBuffer_required_for_tracking_detailed(
+    const st_Buffer *beam_elements, int64_t min_particle_id, int64_t max_particle_id,
+    int64_t min_element_id, int64_t max_element_id, int64_t min_turn_id, int64_t max_turn_id,
+    st_buffer_size_t until_turn_elem_by_elem);
+int32_t st_OutputBuffer_prepare(st_Buffer *beam_elements, st_Buffer *output_buffer,
+                                const st_Particles *particles,
+                                st_buffer_size_t until_turn_elem_by_elem,
+                                st_buffer_size_t *elem_by_elem_out_index_offset,
+                                st_buffer_size_t *beam_monitor_out_index_offset,
+                                int64_t *min_turn_id);
+int32_t st_OutputBuffer_prepare_for_particle_sets(
+    st_Buffer *beam_elements, st_Buffer *output_buffer, const st_Buffer *particles_buffer,
+    st_buffer_size_t num_particle_sets, const st_buffer_size_t *particle_set_indices,
+    st_buffer_size_t until_turn_elem_by_elem, st_buffer_size_t *elem_by_elem_out_index_offset,
+    st_buffer_size_t *beam_monitor_out_index_offset, int64_t *min_turn_id);
+int32_t st_OutputBuffer_prepare_detailed(
+    st_Buffer *beam_elements, st_Buffer *output_buffer, int64_t min_particle_id,
+    int64_t max_particle_id, int64_t min_element_id, int64_t max_element_id,
+    int64_t min_turn_id, int64_t max_turn_id, st_buffer_size_t until_turn_elem_by_elem,
+    st_buffer_size_t *elem_by_elem_out_index_offset,
+    st_buffer_size_t *beam_monitor_out_index_offset, int64_t *max_elem_by_elem_turn_id);
+int32_t st_OutputBuffer_calculate_output_buffer_params(
+    const st_Buffer *beam_elements, const st_Particles *particles,
+    st_buffer_size_t until_turn_elem_by_elem, st_buffer_size_t *num_objects,
+    st_buffer_size_t *num_slots, st_buffer_size_t *num_dataptrs, st_buffer_size_t *num_garbage,
+    st_buffer_size_t slot_size);
+int32_t st_OutputBuffer_calculate_output_buffer_params_for_particles_sets(
+    const st_Buffer *beam_elements, const st_Buffer *particles_buffer,
+    st_buffer_size_t num_particle_sets, const st_buffer_size_t *particle_set_indices,
+    st_buffer_size_t until_turn_elem_by_elem, st_buffer_size_t *num_objects,
+    st_buffer_size_t *num_slots, st_buffer_size_t *num_dataptrs, st_buffer_size_t *num_garbage,
+    st_buffer_size_t slot_size);
+int32_t st_OutputBuffer_calculate_output_buffer_params_detailed(
+    const st_Buffer *beam_elements, int64_t min_particle_id, int64_t max_particle_id,
+    int64_t min_element_id, int64_t max_element_id, int64_t min_turn_id, int64_t max_turn_id,
+    st_buffer_size_t until_turn_elem_by_elem, st_buffer_size_t *num_objects,
+    st_buffer_size_t *num_slots, st_buffer_size_t *num_dataptrs, st_buffer_size_t *num_garbage,
+    st_buffer_size_t slot_size);
+/* be_monitor/output_buffer.h:20-135.  assign_output_buffer points every
+ * storing monitor at its block: from object 1 when an elem-by-elem block
+ * precedes them, else from object 0. */
+int32_t st_BeamMonitor_calculate_output_buffer_params(
+    const st_Buffer *beam_elements, const st_Particles *particles,
+    st_buffer_size_t *num_objects, st_buffer_size_t *num_slots, st_buffer_size_t *num_dataptrs,
+    st_buffer_size_t *num_garbage, st_buffer_size_t slot_size);
+int32_t st_BeamMonitor_calculate_output_buffer_params_detailed(
+    const st_Buffer *beam_elements, int64_t min_particle_id, int64_t max_particle_id,
+    int64_t min_turn_id, st_buffer_size_t *num_objects, st_buffer_size_t *num_slots,
+    st_buffer_size_t *num_dataptrs, st_buffer_size_t *num_garbage, st_buffer_size_t slot_size);
+int32_t st_BeamMonitor_prepare_output_buffer(st_Buffer *beam_elements, st_Buffer *output_buffer,
+                                             const st_Particles *particles,
+                                             st_buffer_size_t *out_index_offset);
+int32_t st_BeamMonitor_prepare_output_buffer_detailed(st_Buffer *beam_elements,
+                                                      st_Buffer *output_buffer,
+                                                      int64_t min_particle_id,
+                                                      int64_t max_particle_id,
+                                                      int64_t min_turn_id,
+                                                      st_buffer_size_t *out_index_offset);
+int32_t st_BeamMonitor_assign_output_buffer(st_Buffer *beam_elements, st_Buffer *output_buffer,
+                                            int64_t min_turn_id,
+                                            st_buffer_size_t until_turn_elem_by_elem);
+int32_t st_BeamMonitor_assign_output_buffer_from_offset(st_Buffer *beam_elements,
+                                                        st_Buffer *output_buffer,
+                                                        int64_t min_turn_id,
+                                                        st_buffer_size_t out_index_offset);
+int32_t st_BeamMonitor_setup_for_particles_all(st_Buffer *beam_elements,
+                                               const st_Particles *particles);
+/* output/elem_by_elem_output_buffer.h:24-115, elem_by_elem_config.c:366-375 */
+int32_t st_ElemByElemConfig_calculate_output_buffer_params_detailed(
+    int64_t min_particle_id, int64_t max_particle_id, int64_t min_element_id,
+    int64_t max_element_id, int64_t min_turn_id, int64_t max_turn_id,
+    st_buffer_size_t until_turn_elem_by_elem, st_buffer_size_t *num_objects,
+    st_buffer_size_t *num_slots, st_buffer_size_t *num_dataptrs, st_buffer_size_t *num_garbage,
+    st_buffer_size_t slot_size);
+int32_t st_ElemByElemConfig_prepare_output_buffer_detailed(
+    st_Buffer *output_buffer, int64_t min_particle_id, int64_t max_particle_id,
+    int64_t min_element_id, int64_t max_element_id, int64_t min_turn_id,
+    int64_t max_elem_by_elem_turn_id, st_buffer_size_t *out_index_offset);
+int32_t st_ElemByElemConfig_assign_output_buffer(st_ElemByElemConfig *config,
+                                                 st_Buffer *output_buffer,
+                                                 st_buffer_size_t out_index_offset);
+/* particles.h:515-562, 3121-3230: the particle count over every Particles
+ * object of a buffer; diff = lhs - rhs per column (all three of one size). */
+st_buffer_size_t st_Particles_buffer_get_total_num_of_particles(const st_Buffer *buffer);
+void st_Particles_calculate_difference(const st_Particles *lhs, const st_Particles *rhs,
+                                       st_Particles *diff);
+
 /* ------------------------------------------------------------- TrackJob */
 /* Legacy TrackJob, common/track_job.h:139-190 and
  * common/internal/track_job.cpp:47-186.  `arch` is "cuda" (also accepted:

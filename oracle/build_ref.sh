@@ -85,4 +85,15 @@ for v in "a 1 0 1 2" "b 0 1 0 1"; do
     gcc $CFLAGS -shared -I "$INC" -I "$REF_ROOT" -I "$HERE" \
         "$HERE/ref_driver.c" -o "$OUT/libstref_flags_$1.so" -lm
 done
+# The reference's host-side output-buffer planning (output/output_buffer.c
+# and what it calls: the elem-by-elem and beam-monitor output helpers, its
+# NS(Buffer) and NS(Particles) host functions), compiled from its own eight
+# source files.  -Bsymbolic keeps its st_Buffer_* calls inside this library
+# when the engine's library (same C names) is loaded in the same process.
+C="$REF_ROOT/sixtracklib/common"
+gcc $CFLAGS -shared -Wl,-Bsymbolic -I "$OUT/include" -I "$REF_ROOT" \
+    "$C/output/output_buffer.c" "$C/output/elem_by_elem_output_buffer.c" \
+    "$C/output/elem_by_elem_config.c" "$C/be_monitor/output_buffer.c" \
+    "$C/be_monitor/be_monitor.c" "$C/buffer/buffer.c" "$C/buffer/mem_pool.c" \
+    "$C/particles/particles.c" -o "$OUT/libstref_output.so" -lm
 echo "built $OUT/libstref.so"

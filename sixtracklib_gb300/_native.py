@@ -19,6 +19,7 @@ i32 = C.c_int32
 i64 = C.c_int64
 u64 = C.c_uint64
 u16 = C.c_uint16
+u32 = C.c_uint32
 cstr = C.c_char_p
 cbool = C.c_bool
 
@@ -61,6 +62,36 @@ _SIGNATURES = {
     "st_Multipole_add": ([vp, i64, vp, C.c_double, C.c_double, C.c_double], vp),
     "st_Particles_new": ([vp, u64], vp),
     "st_Particles_buffer_get_particles": ([vp, u64], vp),
+    "st_Particles_get_num_of_particles": ([vp], i64),
+    "st_Particles_buffer_get_num_of_particle_blocks": ([vp], u64),
+    "st_Particles_buffer_get_total_num_of_particles": ([vp], u64),
+    "st_Particles_calculate_difference": ([vp, vp, vp], None),
+    "st_OutputBuffer_requires_output_buffer_ext": ([u32], cbool),
+    "st_OutputBuffer_requires_elem_by_elem_output_ext": ([u32], cbool),
+    "st_OutputBuffer_requires_beam_monitor_output_ext": ([u32], cbool),
+    "st_OutputBuffer_required_for_tracking": ([vp, vp, u64], u32),
+    "st_OutputBuffer_required_for_tracking_of_particle_sets": ([vp, u64, vp, vp, u64], u32),
+    "st_OutputBuffer_required_for_tracking_detailed": ([vp] + [i64] * 6 + [u64], u32),
+    "st_OutputBuffer_prepare": ([vp, vp, vp, u64, vp, vp, vp], i32),
+    "st_OutputBuffer_prepare_for_particle_sets": ([vp, vp, vp, u64, vp, u64, vp, vp, vp], i32),
+    "st_OutputBuffer_prepare_detailed": ([vp, vp] + [i64] * 6 + [u64, vp, vp, vp], i32),
+    "st_OutputBuffer_calculate_output_buffer_params": ([vp, vp, u64, vp, vp, vp, vp, u64], i32),
+    "st_OutputBuffer_calculate_output_buffer_params_for_particles_sets":
+        ([vp, vp, u64, vp, u64, vp, vp, vp, vp, u64], i32),
+    "st_OutputBuffer_calculate_output_buffer_params_detailed":
+        ([vp] + [i64] * 6 + [u64, vp, vp, vp, vp, u64], i32),
+    "st_BeamMonitor_calculate_output_buffer_params": ([vp, vp, vp, vp, vp, vp, u64], i32),
+    "st_BeamMonitor_calculate_output_buffer_params_detailed":
+        ([vp, i64, i64, i64, vp, vp, vp, vp, u64], i32),
+    "st_BeamMonitor_prepare_output_buffer": ([vp, vp, vp, vp], i32),
+    "st_BeamMonitor_prepare_output_buffer_detailed": ([vp, vp, i64, i64, i64, vp], i32),
+    "st_BeamMonitor_assign_output_buffer": ([vp, vp, i64, u64], i32),
+    "st_BeamMonitor_assign_output_buffer_from_offset": ([vp, vp, i64, u64], i32),
+    "st_BeamMonitor_setup_for_particles_all": ([vp, vp], i32),
+    "st_ElemByElemConfig_calculate_output_buffer_params_detailed":
+        ([i64] * 6 + [u64, vp, vp, vp, vp, u64], i32),
+    "st_ElemByElemConfig_prepare_output_buffer_detailed": ([vp] + [i64] * 6 + [vp], i32),
+    "st_ElemByElemConfig_assign_output_buffer": ([vp, vp, u64], i32),
     "st_TrackJob_new_detailed": ([cstr, vp, u64, vp, vp, vp, u64, cstr], vp),
     "st_TrackJob_delete": ([vp], None),
     "st_TrackJob_track_until": ([vp, u64], i32),
