@@ -897,4 +897,7 @@ int32_t st_engine_rcp_fast(const double *x, double *y, int64_t n, void *stream);
 #ifdef __cplusplus
 }
 #endif
+
+#include "sixtracklib_gb300_aliases.h"
+
 #endif /* SIXTRACKLIB_GB300_H */

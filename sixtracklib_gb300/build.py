@@ -22,7 +22,7 @@ LIB = os.path.join(OUT_DIR, "libsixtracklib_gb300.so")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["buffer.cpp", "lattice.cpp", "output_buffer.cpp"]
+HOST_SOURCES = ["buffer.cpp", "lattice.cpp", "output_buffer.cpp", "aliases.cpp"]
 CUDA_SOURCES = {
     "track_kernel.cu": ["-fmad=false"],
     "engine.cu": [],
