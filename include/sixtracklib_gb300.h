@@ -416,6 +416,34 @@ int32_t st_ElemByElemConfig_prepare_output_buffer_detailed(
 int32_t st_ElemByElemConfig_assign_output_buffer(st_ElemByElemConfig *config,
                                                  st_Buffer *output_buffer,
                                                  st_buffer_size_t out_index_offset);
+/* Field accessors and lifecycle of the configuration (the reference's
+ * "_ext" copies of output/elem_by_elem_config.h:532-1160; create / delete
+ * of elem_by_elem_config.c).  clear: ids -1, counts 0, no store address;
+ * preset: clear, order -1 (invalid), rolling; active: an order and
+ * something to store. */
+st_ElemByElemConfig *st_ElemByElemConfig_create(void);
+void st_ElemByElemConfig_delete(st_ElemByElemConfig *config);
+st_ElemByElemConfig *st_ElemByElemConfig_preset_ext(st_ElemByElemConfig *config);
+void st_ElemByElemConfig_clear_ext(st_ElemByElemConfig *config);
+bool st_ElemByElemConfig_is_active_ext(const st_ElemByElemConfig *config);
+int32_t st_ElemByElemConfig_get_order_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_num_particles_to_store_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_num_elements_to_store_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_num_turns_to_store_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_out_store_num_particles_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_min_particle_id_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_max_particle_id_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_min_element_id_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_max_element_id_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_min_turn_ext(const st_ElemByElemConfig *config);
+int64_t st_ElemByElemConfig_get_max_turn_ext(const st_ElemByElemConfig *config);
+bool st_ElemByElemConfig_is_rolling_ext(const st_ElemByElemConfig *config);
+st_buffer_addr_t st_ElemByElemConfig_get_output_store_address_ext(
+    const st_ElemByElemConfig *config);
+void st_ElemByElemConfig_set_order_ext(st_ElemByElemConfig *config, int64_t order);
+void st_ElemByElemConfig_set_is_rolling_ext(st_ElemByElemConfig *config, bool is_rolling);
+void st_ElemByElemConfig_set_output_store_address_ext(st_ElemByElemConfig *config,
+                                                      st_buffer_addr_t out_address);
 /* particles.h:515-562, 3121-3230: the particle count over every Particles
  * object of a buffer; diff = lhs - rhs per column (all three of one size). */
 st_buffer_size_t st_Particles_buffer_get_total_num_of_particles(const st_Buffer *buffer);

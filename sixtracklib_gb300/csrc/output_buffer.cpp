@@ -16,6 +16,7 @@
 // element id, and the last id is the first plus the number of beam
 // elements minus one.
 #include <climits>
+#include <cstdlib>
 
 #include "common.h"
 
@@ -567,6 +568,96 @@ int32_t st_ElemByElemConfig_assign_output_buffer(st_ElemByElemConfig *c, st_Buff
     if (!blk) return -1;
     c->out_store_addr = (st_buffer_addr_t)(uintptr_t)blk;
     return 0;
+}
+
+// The configuration's field accessors and lifecycle (the reference's
+// out-of-line "_ext" copies of elem_by_elem_config.h:532-1160, create and
+// delete of elem_by_elem_config.c).  clear empties the ranges (ids -1,
+// counts 0, no store address); preset also makes the order invalid (-1)
+// and the store rolling.
+void st_ElemByElemConfig_clear_ext(st_ElemByElemConfig *c)
+{
+    if (!c) return;
+    c->num_particles_to_store = c->num_elements_to_store = c->num_turns_to_store = 0;
+    c->min_particle_id = c->max_particle_id = -1;
+    c->min_element_id = c->max_element_id = -1;
+    c->min_turn = c->max_turn = -1;
+    c->out_store_addr = 0;
+}
+st_ElemByElemConfig *st_ElemByElemConfig_preset_ext(st_ElemByElemConfig *c)
+{
+    if (!c) return c;
+    st_ElemByElemConfig_clear_ext(c);
+    c->order = -1;
+    c->is_rolling = 1;
+    return c;
+}
+st_ElemByElemConfig *st_ElemByElemConfig_create(void)
+{
+    return st_ElemByElemConfig_preset_ext(
+        static_cast<st_ElemByElemConfig *>(std::malloc(sizeof(st_ElemByElemConfig))));
+}
+void st_ElemByElemConfig_delete(st_ElemByElemConfig *c) { std::free(c); }
+bool st_ElemByElemConfig_is_active_ext(const st_ElemByElemConfig *c)
+{
+    return c && c->num_particles_to_store > 0 && c->num_elements_to_store > 0 &&
+           c->num_turns_to_store > 0 && c->order != -1;
+}
+int32_t st_ElemByElemConfig_get_order_ext(const st_ElemByElemConfig *c)
+{
+    return c ? (int32_t)c->order : -1;  // the reference returns its order enum
+}
+int64_t st_ElemByElemConfig_get_num_particles_to_store_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->num_particles_to_store : 0;
+}
+int64_t st_ElemByElemConfig_get_num_elements_to_store_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->num_elements_to_store : 0;
+}
+int64_t st_ElemByElemConfig_get_num_turns_to_store_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->num_turns_to_store : 0;
+}
+int64_t st_ElemByElemConfig_get_out_store_num_particles_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->num_particles_to_store * c->num_elements_to_store * c->num_turns_to_store : 0;
+}
+int64_t st_ElemByElemConfig_get_min_particle_id_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->min_particle_id : -1;
+}
+int64_t st_ElemByElemConfig_get_max_particle_id_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->max_particle_id : -1;
+}
+int64_t st_ElemByElemConfig_get_min_element_id_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->min_element_id : -1;
+}
+int64_t st_ElemByElemConfig_get_max_element_id_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->max_element_id : -1;
+}
+int64_t st_ElemByElemConfig_get_min_turn_ext(const st_ElemByElemConfig *c) { return c ? c->min_turn : -1; }
+int64_t st_ElemByElemConfig_get_max_turn_ext(const st_ElemByElemConfig *c) { return c ? c->max_turn : -1; }
+bool st_ElemByElemConfig_is_rolling_ext(const st_ElemByElemConfig *c) { return c && c->is_rolling != 0; }
+st_buffer_addr_t st_ElemByElemConfig_get_output_store_address_ext(const st_ElemByElemConfig *c)
+{
+    return c ? c->out_store_addr : 0;
+}
+void st_ElemByElemConfig_set_order_ext(st_ElemByElemConfig *c, int64_t order)
+{
+    if (c) c->order = order;
+}
+void st_ElemByElemConfig_set_is_rolling_ext(st_ElemByElemConfig *c, bool is_rolling)
+{
+    if (c) c->is_rolling = is_rolling ? 1 : 0;
+}
+void st_ElemByElemConfig_set_output_store_address_ext(st_ElemByElemConfig *c,
+                                                      st_buffer_addr_t addr)
+{
+    if (c) c->out_store_addr = addr;
 }
 
 // ------------------------------------------------------------ particles

@@ -41,6 +41,10 @@ class EbeConfig(C.Structure):
         "max_turn", "is_rolling")] + [("out_store_addr", U64)]
 
 
+EBE_GETTERS = ("order", "num_particles_to_store", "num_elements_to_store",
+               "num_turns_to_store", "out_store_num_particles", "min_particle_id",
+               "max_particle_id", "min_element_id", "max_element_id", "min_turn", "max_turn")
+
 COMMON = {
     "st_Buffer_new": ([U64], VP), "st_Buffer_delete": ([VP], None),
     "st_Buffer_new_from_file": ([C.c_char_p], VP),
@@ -59,6 +63,16 @@ COMMON = {
     "st_BeamMonitor_calculate_output_buffer_params": ([VP, VP] + [VP] * 4 + [U64], I64),
     "st_BeamMonitor_prepare_output_buffer": ([VP, VP, VP, VP], I64),
     "st_ElemByElemConfig_assign_output_buffer": ([VP, VP, U64], I64),
+    "st_ElemByElemConfig_create": ([], VP), "st_ElemByElemConfig_delete": ([VP], None),
+    "st_ElemByElemConfig_preset_ext": ([VP], VP), "st_ElemByElemConfig_clear_ext": ([VP], None),
+    "st_ElemByElemConfig_is_active_ext": ([VP], B),
+    "st_ElemByElemConfig_is_rolling_ext": ([VP], B),
+    "st_ElemByElemConfig_get_output_store_address_ext": ([VP], U64),
+    "st_ElemByElemConfig_set_order_ext": ([VP, I64], None),
+    "st_ElemByElemConfig_set_is_rolling_ext": ([VP, B], None),
+    "st_ElemByElemConfig_set_output_store_address_ext": ([VP, U64], None),
+    **{f"st_ElemByElemConfig_get_{f}_ext": ([VP], I64) for f in EBE_GETTERS},
+    "st_ElemByElemConfig_get_order_ext": ([VP], C.c_int32),  # an enum
 }
 OURS = {"st_Buffer_get_num_of_objects": ([VP], U64),
         "st_Buffer_get_const_object": ([VP, U64], VP),
@@ -314,6 +328,36 @@ def _particle_helpers(s, files):
     return res
 
 
+def _ebe_accessors(s):
+    """Every accessor of the elem-by-elem configuration over create, preset,
+    set, clear and a hand-filled configuration (the struct layouts agree)."""
+    L = s.L
+
+    def read(c):
+        return ([L.st_ElemByElemConfig_is_active_ext(c), L.st_ElemByElemConfig_is_rolling_ext(c),
+                 L.st_ElemByElemConfig_get_output_store_address_ext(c)] +
+                [getattr(L, f"st_ElemByElemConfig_get_{f}_ext")(c) for f in EBE_GETTERS] +
+                [bytes(C.string_at(c, C.sizeof(EbeConfig)))])
+
+    rows = []
+    c = L.st_ElemByElemConfig_create()
+    rows.append(read(c))
+    L.st_ElemByElemConfig_set_order_ext(c, 0)
+    L.st_ElemByElemConfig_set_is_rolling_ext(c, False)
+    L.st_ElemByElemConfig_set_output_store_address_ext(c, 4096)
+    rows.append(read(c))
+    cfg = EbeConfig(0, 3, 4, 5, 2, 1, 7, 4, 4, 11, 0, 8192)
+    rows.append(read(C.byref(cfg)))
+    L.st_ElemByElemConfig_clear_ext(C.byref(cfg))
+    rows.append(read(C.byref(cfg)))
+    rows.append(L.st_ElemByElemConfig_preset_ext(C.byref(cfg)) == C.addressof(cfg))
+    rows.append(read(C.byref(cfg)))
+    L.st_ElemByElemConfig_delete(c)
+    rows.append((L.st_ElemByElemConfig_is_active_ext(None),
+                 L.st_ElemByElemConfig_preset_ext(None)))
+    return rows
+
+
 def _all_results(s, files):
     """Every comparison of this file, for one library."""
     out = {("flags", lat, ps): _flags(s, files, lat, ps) for lat, ps in CASES}
@@ -327,6 +371,7 @@ def _all_results(s, files):
                              s.L.st_OutputBuffer_requires_beam_monitor_output_ext(f))
                             for f in range(4)]
     out[("particles",)] = _particle_helpers(s, files)
+    out[("ebe_accessors",)] = _ebe_accessors(s)
     return out
 
 
@@ -386,3 +431,9 @@ def test_particle_helpers_match_the_reference(results):
     mine, theirs = (r[("particles",)] for r in results)
     assert mine == theirs
     assert mine[0] == 5 and mine[1] == [0.0] * 3 + [0] * 3 and mine[2]
+
+
+def test_elem_by_elem_accessors_match_the_reference(results):
+    mine, theirs = (r[("ebe_accessors",)] for r in results)
+    assert mine == theirs
+    assert mine[2][0] is True and mine[3][0] is False  # filled: active; cleared: not
