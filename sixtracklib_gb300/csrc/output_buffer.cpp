@@ -15,6 +15,7 @@
 // are not beam elements (particles, lines, configurations) shift the first
 // element id, and the last id is the first plus the number of beam
 // elements minus one.
+#include <algorithm>
 #include <climits>
 #include <cstdlib>
 
