@@ -131,6 +131,14 @@ void st_TrackJobNew_set_default_elem_by_elem_config_rolling_flag(st_TrackJobBase
 st_Buffer *st_TrackJobNew_stored_buffer(st_TrackJobBaseNew *job, st_buffer_size_t buffer_id);
 st_buffer_size_t st_TrackJobNew_total_num_assign_items(const st_TrackJobBaseNew *job);
 
+/* The legacy TrackJob's names for the particle-address calls
+ * (common/track_job.h:478-492) */
+int32_t st_TrackJob_fetch_particles_addr(st_TrackJob *job);
+int32_t st_TrackJob_clear_particles_addr(st_TrackJob *job, st_buffer_size_t index);
+int32_t st_TrackJob_clear_all_particles_addr(st_TrackJob *job);
+const st_ParticlesAddr *st_TrackJob_particles_addr(const st_TrackJob *job,
+                                                   st_buffer_size_t index);
+
 #ifdef __cplusplus
 }
 #endif

@@ -200,4 +200,22 @@ st_Buffer *st_TrackJobNew_stored_buffer(st_TrackJobBaseNew *job, st_buffer_size_
 st_buffer_size_t st_TrackJobNew_total_num_assign_items(const st_TrackJobBaseNew *job) { return
     st_TrackJob_total_num_assign_items(job); }
 
+// The legacy TrackJob's names for the particle-address calls (track_job.h:478-492)
+int32_t st_TrackJob_fetch_particles_addr(st_TrackJob *job)
+{
+    return st_TrackJob_fetch_particle_addresses(job);
+}
+int32_t st_TrackJob_clear_particles_addr(st_TrackJob *job, st_buffer_size_t index)
+{
+    return st_TrackJob_clear_particle_addresses(job, index);
+}
+int32_t st_TrackJob_clear_all_particles_addr(st_TrackJob *job)
+{
+    return st_TrackJob_clear_all_particle_addresses(job);
+}
+const st_ParticlesAddr *st_TrackJob_particles_addr(const st_TrackJob *job, st_buffer_size_t index)
+{
+    return st_TrackJob_particle_addresses(job, index);
+}
+
 }  // extern "C"
